@@ -1,0 +1,196 @@
+/*
+ * lla_gb300.h — C ABI of the GB300 (sm_103a) SPD factor-and-solve library.
+ *
+ * The first group of entry points replaces, one for one, the trait methods of
+ * linfa-linalg 0.2.1 on the SPD path (src/cholesky.rs, src/triangular.rs).
+ * Matrices are passed as ndarray-style strided views of HOST memory:
+ *     (ptr, rows, cols, row_stride, col_stride)
+ * where element (i, j) lives at ptr[i*row_stride + j*col_stride] and the
+ * strides are signed element counts, so reversed axes (negative strides) and
+ * transposed (column-major) views are accepted exactly like the reference's
+ * ArrayBase<S, Ix2> arguments.  Each call copies the view to the GPU,
+ * computes there, and writes the result back into the same view.  There is no
+ * CPU fallback: without a CUDA device every compute call returns
+ * LLA_ERR_NO_DEVICE.
+ *
+ * Error precedence follows the reference exactly (see each declaration).
+ * Every entry point returns the status code and, when `err` is non-NULL,
+ * fills it with the variant's fields.
+ *
+ * The second group (lla_*_device, lla_plan_*, lla_batch_*, lla_serve_*) has no
+ * counterpart in the reference: device-resident, mixed-precision, batched and
+ * serving entry points built on the same kernels.
+ */
+#ifndef LLA_GB300_H
+#define LLA_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------
+ * 0..3 mirror linfa_linalg::LinalgError (src/lib.rs:33-60) for the variants
+ * this path can raise; 16.. are device-side conditions the reference cannot
+ * have. */
+enum lla_status {
+    LLA_OK = 0,
+    LLA_NOT_SQUARE = 1,            /* LinalgError::NotSquare { rows, cols }      src/lib.rs:38 */
+    LLA_NOT_POSITIVE_DEFINITE = 2, /* LinalgError::NotPositiveDefinite           src/lib.rs:44 */
+    LLA_WRONG_ROWS = 3,            /* LinalgError::WrongRows { expected, actual } src/lib.rs:56 */
+    LLA_ERR_CUDA = 16,             /* a CUDA runtime call failed (cuda_error set) */
+    LLA_ERR_NO_MEMORY = 17,        /* device or pinned-host allocation failed */
+    LLA_ERR_INVALID_ARG = 18,      /* NULL pointer, negative size, bad option */
+    LLA_ERR_TIMEOUT = 19,          /* a bounded device wait gave up */
+    LLA_ERR_NO_DEVICE = 20,        /* no CUDA device visible */
+    LLA_ERR_NOT_CONVERGED = 21,    /* refinement stalled and fallback was disabled */
+    LLA_ERR_BUSY = 22              /* admission refused (serving loop at its HBM budget) */
+};
+
+typedef struct lla_error {
+    int32_t code;       /* one of lla_status */
+    int32_t cuda_error; /* raw cudaError_t when code == LLA_ERR_CUDA */
+    int64_t rows;       /* NotSquare.rows */
+    int64_t cols;       /* NotSquare.cols */
+    int64_t expected;   /* WrongRows.expected */
+    int64_t actual;     /* WrongRows.actual */
+    int64_t index;      /* NotPositiveDefinite: first row j whose pivot d <= 0 */
+} lla_error;
+
+/* UPLO (src/triangular.rs:8-13) */
+enum lla_uplo { LLA_UPPER = 0, LLA_LOWER = 1 };
+
+/* Factorisation algorithm used by the host-view entry points.
+ *  LLA_ALGO_EXACT : the reference's own operation order (row-oriented
+ *                   Cholesky-Banachiewicz sums, column-axpy substitution),
+ *                   reorganised into blocked GPU kernels that keep every
+ *                   per-element accumulation order; separate multiply and add
+ *                   (no FMA), IEEE division and square root.  Results are
+ *                   bit-identical to the reference.
+ *  LLA_ALGO_FAST  : blocked right-looking FP64/FP32 with fused multiply-add
+ *                   (normwise errors within 10*n*eps of the reference).
+ *                   NotPositiveDefinite is still decided with the reference's
+ *                   arithmetic: a failed or near-singular fast factorisation
+ *                   is re-run in EXACT order before an error is returned.
+ *  LLA_ALGO_AUTO  : EXACT for n <= 1024, FAST above (the default). */
+enum lla_algo { LLA_ALGO_AUTO = 0, LLA_ALGO_EXACT = 1, LLA_ALGO_FAST = 2 };
+
+/* Sets the process-wide algorithm for the host-view entry points; returns the
+ * previous value, or -1 for an invalid argument. */
+int lla_set_algorithm(int algo);
+int lla_get_algorithm(void);
+
+/* Number of CUDA devices (0 when none); never fails. */
+int lla_device_count(void);
+/* Library version string. */
+const char *lla_version(void);
+/* Human-readable text for a status code. */
+const char *lla_status_string(int code);
+
+/* ---- drop-in entry points (host views) ---------------------------------
+ * f64 ("d") and f32 ("s") variants of each trait method.  `dirty` selects
+ * cholesky_inplace_dirty (upper triangle left untouched) versus
+ * cholesky_inplace (upper triangle zeroed). */
+
+/* CholeskyInplace::cholesky_inplace_dirty / ::cholesky_inplace
+ * (src/cholesky.rs:19,33,51-82; also backs cholesky_into[_dirty] :24-43 and
+ * Cholesky::cholesky[_dirty] :86-115, whose to_owned() copy the caller makes).
+ * Errors: NotSquare{rows,cols} (src/lib.rs:64-71), then NotPositiveDefinite
+ * at the first row j with d <= 0 (src/cholesky.rs:69-71).  On
+ * NotPositiveDefinite the view holds exactly what the reference leaves: rows
+ * < j factored, row j's strict lower part written, the rest untouched. */
+int lla_dcholesky_inplace(double *a, int64_t rows, int64_t cols, int64_t rs, int64_t cs,
+                          int dirty, lla_error *err);
+int lla_scholesky_inplace(float *a, int64_t rows, int64_t cols, int64_t rs, int64_t cs,
+                          int dirty, lla_error *err);
+
+/* SolveCInplace::solvec_inplace (src/cholesky.rs:122,136-144; backs
+ * solvec_into :127-130 and SolveC::solvec :148-163).  `a` is left holding the
+ * dirty factor, `b` holds X.  Errors: NotSquare(a), NotPositiveDefinite, then
+ * WrongRows{expected=n, actual=b.rows} -- the row check runs after the
+ * factorisation, so a mismatched b still leaves `a` factored, as in the
+ * reference. */
+int lla_dsolvec_inplace(double *a, int64_t rows, int64_t cols, int64_t rs, int64_t cs,
+                        double *b, int64_t brows, int64_t bcols, int64_t brs, int64_t bcs,
+                        lla_error *err);
+int lla_ssolvec_inplace(float *a, int64_t rows, int64_t cols, int64_t rs, int64_t cs,
+                        float *b, int64_t brows, int64_t bcols, int64_t brs, int64_t bcs,
+                        lla_error *err);
+
+/* InverseCInplace::invc_inplace (src/cholesky.rs:172,178-181; backs
+ * InverseC::invc :186-199).  `out` is an n x n view that receives the
+ * inverse; `a` is left holding the dirty factor. */
+int lla_dinvc_inplace(double *a, int64_t rows, int64_t cols, int64_t rs, int64_t cs,
+                      double *out, int64_t out_rs, int64_t out_cs, lla_error *err);
+int lla_sinvc_inplace(float *a, int64_t rows, int64_t cols, int64_t rs, int64_t cs,
+                      float *out, int64_t out_rs, int64_t out_cs, lla_error *err);
+
+/* SolveTriangularInplace::solve_triangular_inplace (src/triangular.rs:149,
+ * 161-168; backs solve_triangular_into :152-155 and
+ * SolveTriangular::solve_triangular :172-187).  Only the `uplo` triangle and
+ * the diagonal of `a` are read.  Errors: NotSquare(a), then WrongRows.  A zero
+ * diagonal is not an error (inf/NaN, as in the reference). */
+int lla_dsolve_triangular_inplace(const double *a, int64_t rows, int64_t cols, int64_t rs,
+                                  int64_t cs, double *b, int64_t brows, int64_t bcols,
+                                  int64_t brs, int64_t bcs, int uplo, lla_error *err);
+int lla_ssolve_triangular_inplace(const float *a, int64_t rows, int64_t cols, int64_t rs,
+                                  int64_t cs, float *b, int64_t brows, int64_t bcols,
+                                  int64_t brs, int64_t bcs, int uplo, lla_error *err);
+
+/* solve_triangular_system with a caller-supplied diagonal
+ * (src/triangular.rs:133-144): the closure `diag_fn(i)` becomes the array
+ * diag[0..n).  This is the form QR's solve uses (src/qr.rs:145-150,172-177
+ * pass |R[i,i]|). */
+int lla_dsolve_triangular_diag(const double *a, int64_t rows, int64_t cols, int64_t rs,
+                               int64_t cs, const double *diag, double *b, int64_t brows,
+                               int64_t bcols, int64_t brs, int64_t bcs, int uplo,
+                               lla_error *err);
+int lla_ssolve_triangular_diag(const float *a, int64_t rows, int64_t cols, int64_t rs,
+                               int64_t cs, const float *diag, float *b, int64_t brows,
+                               int64_t bcols, int64_t brs, int64_t bcs, int uplo,
+                               lla_error *err);
+
+/* IntoTriangular::triangular_inplace (src/triangular.rs:19,37-53). */
+int lla_dtriangular_inplace(double *a, int64_t rows, int64_t cols, int64_t rs, int64_t cs,
+                            int uplo, lla_error *err);
+int lla_striangular_inplace(float *a, int64_t rows, int64_t cols, int64_t rs, int64_t cs,
+                            int uplo, lla_error *err);
+
+/* Triangular::is_triangular (src/triangular.rs:59,67-90): *result = 1/0.
+ * A non-square view gives 0, not an error, as in the reference. */
+int lla_dis_triangular(const double *a, int64_t rows, int64_t cols, int64_t rs, int64_t cs,
+                       int uplo, int *result, lla_error *err);
+int lla_sis_triangular(const float *a, int64_t rows, int64_t cols, int64_t rs, int64_t cs,
+                       int uplo, int *result, lla_error *err);
+
+/* ---- device-resident entry points (no counterpart in the reference) ----
+ * Matrices are column-major device arrays with a leading dimension; `stream`
+ * is a cudaStream_t (NULL = the legacy default stream).  Calls are
+ * asynchronous unless stated; statuses that need device results (pivot
+ * failure) are written to device memory `d_info` (int64: -1 = success, else
+ * the failing row) so that calls can be captured in CUDA graphs. */
+
+/* In-place Cholesky of the lower triangle of the n x n column-major matrix
+ * dA (leading dimension ld >= n).  algo: LLA_ALGO_EXACT or LLA_ALGO_FAST.
+ * Uses library-owned device workspace (grown on demand). */
+int lla_dpotrf_device(double *dA, int64_t n, int64_t ld, int algo, int64_t *d_info,
+                      void *stream, lla_error *err);
+int lla_spotrf_device(float *dA, int64_t n, int64_t ld, int algo, int64_t *d_info,
+                      void *stream, lla_error *err);
+
+/* Triangular solve with the lower-triangular factor L (column-major, ld):
+ * trans = 0 solves L X = B, trans = 1 solves L^T X = B; dB (n x m, ldb) is
+ * overwritten with X.  algo as above (EXACT follows the reference's
+ * substitution order). */
+int lla_dtrsm_device(const double *dL, int64_t n, int64_t ld, int trans, double *dB, int64_t m,
+                     int64_t ldb, int algo, void *stream, lla_error *err);
+int lla_strsm_device(const float *dL, int64_t n, int64_t ld, int trans, float *dB, int64_t m,
+                     int64_t ldb, int algo, void *stream, lla_error *err);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LLA_GB300_H */
