@@ -1,0 +1,352 @@
+"""GB300 (sm_103a) SPD factor-and-solve -- Python mirror of linfa-linalg's
+`cholesky` and `triangular` trait methods over the C ABI in
+include/lla_gb300.h.
+
+Every function mirrors one reference method (src/cholesky.rs,
+src/triangular.rs) with the same name, argument meaning, mutation and error
+behaviour; numpy arrays play the role of ndarray views (any strides, including
+negative and transposed ones).  All computation happens in the CUDA library
+liblla_gb300.so: importing this module fails when the library has not been
+built, and every compute call raises `DeviceError` when no GPU is present --
+there is no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblla_gb300.so")
+
+OK, NOT_SQUARE, NOT_POSITIVE_DEFINITE, WRONG_ROWS = 0, 1, 2, 3
+ERR_CUDA, ERR_NO_MEMORY, ERR_INVALID_ARG, ERR_TIMEOUT, ERR_NO_DEVICE = 16, 17, 18, 19, 20
+ERR_NOT_CONVERGED, ERR_BUSY = 21, 22
+UPPER, LOWER = 0, 1
+ALGO_AUTO, ALGO_EXACT, ALGO_FAST = 0, 1, 2
+
+
+class LinalgError(Exception):
+    """Mirror of linfa_linalg::LinalgError (src/lib.rs:33-60)."""
+
+
+class NotSquare(LinalgError):
+    def __init__(self, rows, cols):
+        super().__init__(f"Matrix of ({rows}, {cols}) is not square")
+        self.rows, self.cols = rows, cols
+
+
+class NotPositiveDefinite(LinalgError):
+    def __init__(self, index=None):
+        super().__init__("Matrix is not positive definite")
+        self.index = index
+
+
+class WrongRows(LinalgError):
+    def __init__(self, expected, actual):
+        super().__init__(f"Matrix must have {expected} rows, not {actual}")
+        self.expected, self.actual = expected, actual
+
+
+class DeviceError(RuntimeError):
+    """A device-side condition the reference cannot have (CUDA error, no
+    device, out of memory, bounded wait timed out, ...)."""
+
+    def __init__(self, code, cuda_error=0, msg=""):
+        super().__init__(f"lla status {code} (cuda error {cuda_error}) {msg}".strip())
+        self.code, self.cuda_error = code, cuda_error
+
+
+class Error(ctypes.Structure):
+    _fields_ = [("code", ctypes.c_int32), ("cuda_error", ctypes.c_int32),
+                ("rows", ctypes.c_int64), ("cols", ctypes.c_int64),
+                ("expected", ctypes.c_int64), ("actual", ctypes.c_int64),
+                ("index", ctypes.c_int64)]
+
+
+_V = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64]
+_E = ctypes.POINTER(Error)
+
+EXPORTS = {
+    "lla_set_algorithm": ([ctypes.c_int], ctypes.c_int),
+    "lla_get_algorithm": ([], ctypes.c_int),
+    "lla_device_count": ([], ctypes.c_int),
+    "lla_version": ([], ctypes.c_char_p),
+    "lla_status_string": ([ctypes.c_int], ctypes.c_char_p),
+}
+for _p in "ds":
+    EXPORTS.update({
+        f"lla_{_p}cholesky_inplace": (_V + [ctypes.c_int, _E], ctypes.c_int),
+        f"lla_{_p}solvec_inplace": (_V + _V + [_E], ctypes.c_int),
+        f"lla_{_p}invc_inplace": (_V + [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, _E],
+                                  ctypes.c_int),
+        f"lla_{_p}solve_triangular_inplace": (_V + _V + [ctypes.c_int, _E], ctypes.c_int),
+        f"lla_{_p}solve_triangular_diag": (_V + [ctypes.c_void_p] + _V + [ctypes.c_int, _E],
+                                           ctypes.c_int),
+        f"lla_{_p}triangular_inplace": (_V + [ctypes.c_int, _E], ctypes.c_int),
+        f"lla_{_p}is_triangular": (_V + [ctypes.c_int, ctypes.POINTER(ctypes.c_int), _E],
+                                   ctypes.c_int),
+        f"lla_{_p}potrf_device": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
+                                   ctypes.c_void_p, ctypes.c_void_p, _E], ctypes.c_int),
+        f"lla_{_p}trsm_device": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
+                                  ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
+                                  ctypes.c_void_p, _E], ctypes.c_int),
+    })
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is not built; run __graft_entry__.build() "
+                          "(the CUDA library is required: there is no CPU fallback)")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (args, res) in EXPORTS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    return lib
+
+
+lib = _load()
+
+
+def _raise(e):
+    c = e.code
+    if c == OK:
+        return
+    if c == NOT_SQUARE:
+        raise NotSquare(e.rows, e.cols)
+    if c == NOT_POSITIVE_DEFINITE:
+        raise NotPositiveDefinite(e.index)
+    if c == WRONG_ROWS:
+        raise WrongRows(e.expected, e.actual)
+    raise DeviceError(c, e.cuda_error, lib.lla_status_string(c).decode())
+
+
+def _prefix(a):
+    if a.dtype == np.float64:
+        return "d"
+    if a.dtype == np.float32:
+        return "s"
+    raise TypeError(f"unsupported dtype {a.dtype} (f32 and f64, like NdFloat)")
+
+
+def _view(a):
+    if not isinstance(a, np.ndarray) or a.ndim != 2:
+        raise TypeError("expected a 2-D numpy array")
+    isz = a.itemsize
+    rs, cs = a.strides
+    if rs % isz or cs % isz:
+        raise ValueError("strides must be multiples of the element size")
+    return [ctypes.c_void_p(a.__array_interface__["data"][0]), a.shape[0], a.shape[1],
+            rs // isz, cs // isz]
+
+
+def _writable(a):
+    if not a.flags.writeable:
+        raise ValueError("array is read-only")
+
+
+def _uplo(uplo):
+    if isinstance(uplo, str):
+        u = uplo.lower()
+        if u not in ("upper", "lower"):
+            raise ValueError(uplo)
+        return UPPER if u == "upper" else LOWER
+    if uplo not in (UPPER, LOWER):
+        raise ValueError(uplo)
+    return uplo
+
+
+def _same_dtype(a, b):
+    if a.dtype != b.dtype:
+        raise TypeError("both arrays must have the same element type")
+
+
+# ---- algorithm selection -------------------------------------------------
+
+def set_algorithm(algo):
+    """ALGO_EXACT (the reference's operation order, bit-identical results),
+    ALGO_FAST (blocked FMA; errors still decided in exact order) or ALGO_AUTO
+    (exact up to n = 1024).  Returns the previous setting."""
+    prev = lib.lla_set_algorithm(int(algo))
+    if prev < 0:
+        raise ValueError(algo)
+    return prev
+
+
+def get_algorithm():
+    return lib.lla_get_algorithm()
+
+
+def device_count():
+    return lib.lla_device_count()
+
+
+# ---- CholeskyInplace / Cholesky (src/cholesky.rs:16-115) -------------------
+
+def cholesky_inplace_dirty(a):
+    """CholeskyInplace::cholesky_inplace_dirty: A = L L^T in place, upper triangle untouched."""
+    _writable(a)
+    e = Error()
+    getattr(lib, f"lla_{_prefix(a)}cholesky_inplace")(*_view(a), 1, ctypes.byref(e))
+    _raise(e)
+    return a
+
+
+def cholesky_inplace(a):
+    """CholeskyInplace::cholesky_inplace: in place, upper triangle zeroed."""
+    _writable(a)
+    e = Error()
+    getattr(lib, f"lla_{_prefix(a)}cholesky_inplace")(*_view(a), 0, ctypes.byref(e))
+    _raise(e)
+    return a
+
+
+def cholesky_into_dirty(a):
+    return cholesky_inplace_dirty(a)
+
+
+def cholesky_into(a):
+    return cholesky_inplace(a)
+
+
+def cholesky_dirty(a):
+    """Cholesky::cholesky_dirty: factor of a copy (to_owned)."""
+    return cholesky_inplace_dirty(np.array(a))
+
+
+def cholesky(a):
+    """Cholesky::cholesky: factor of a copy (to_owned)."""
+    return cholesky_inplace(np.array(a))
+
+
+# ---- SolveCInplace / SolveC / InverseC (src/cholesky.rs:117-199) ------------
+
+def solvec_inplace(a, b):
+    """SolveCInplace::solvec_inplace: b <- A^{-1} b; `a` keeps the dirty factor."""
+    _writable(a)
+    _writable(b)
+    _same_dtype(a, b)
+    e = Error()
+    getattr(lib, f"lla_{_prefix(a)}solvec_inplace")(*_view(a), *_view(b), ctypes.byref(e))
+    _raise(e)
+    return b
+
+
+def solvec_into(a, b):
+    return solvec_inplace(a, b)
+
+
+def solvec(a, b):
+    """SolveC::solvec: solves into a copy of b (a is still used as scratch)."""
+    return solvec_inplace(a, np.array(b))
+
+
+def invc_inplace(a):
+    """InverseCInplace::invc_inplace: returns A^{-1}; `a` keeps the dirty factor."""
+    _writable(a)
+    n = a.shape[0]
+    out = np.zeros((n, n), dtype=a.dtype)
+    e = Error()
+    getattr(lib, f"lla_{_prefix(a)}invc_inplace")(*_view(a), ctypes.c_void_p(out.ctypes.data),
+                                                  n, 1, ctypes.byref(e))
+    _raise(e)
+    return out
+
+
+def invc(a):
+    """InverseC::invc: inverse of a copy."""
+    return invc_inplace(np.array(a))
+
+
+# ---- triangular.rs ----------------------------------------------------------
+
+def solve_triangular_inplace(a, b, uplo, diag=None):
+    """SolveTriangularInplace::solve_triangular_inplace (src/triangular.rs:147-169);
+    with `diag`, the crate-internal solve_triangular_system's diag_fn (:133-144)."""
+    _writable(b)
+    _same_dtype(a, b)
+    e = Error()
+    p = _prefix(a)
+    if diag is None:
+        getattr(lib, f"lla_{p}solve_triangular_inplace")(*_view(a), *_view(b), _uplo(uplo),
+                                                         ctypes.byref(e))
+    else:
+        d = np.ascontiguousarray(diag, dtype=a.dtype)
+        if d.shape != (min(a.shape),):
+            raise ValueError("diag must have one entry per row")
+        getattr(lib, f"lla_{p}solve_triangular_diag")(*_view(a), ctypes.c_void_p(d.ctypes.data),
+                                                      *_view(b), _uplo(uplo), ctypes.byref(e))
+    _raise(e)
+    return b
+
+
+def solve_triangular_into(a, b, uplo):
+    return solve_triangular_inplace(a, b, uplo)
+
+
+def solve_triangular(a, b, uplo):
+    """SolveTriangular::solve_triangular: solves into a copy of b."""
+    return solve_triangular_inplace(a, np.array(b), uplo)
+
+
+def triangular_inplace(a, uplo):
+    """IntoTriangular::triangular_inplace (src/triangular.rs:37-53)."""
+    _writable(a)
+    e = Error()
+    getattr(lib, f"lla_{_prefix(a)}triangular_inplace")(*_view(a), _uplo(uplo), ctypes.byref(e))
+    _raise(e)
+    return a
+
+
+def into_triangular(a, uplo):
+    return triangular_inplace(a, uplo)
+
+
+def is_triangular(a, uplo):
+    """Triangular::is_triangular (src/triangular.rs:67-90)."""
+    e = Error()
+    r = ctypes.c_int(0)
+    getattr(lib, f"lla_{_prefix(a)}is_triangular")(*_view(a), _uplo(uplo), ctypes.byref(r),
+                                                   ctypes.byref(e))
+    _raise(e)
+    return bool(r.value)
+
+
+# ---- device-resident helpers (torch tensors; column-major = transposed view) ----
+
+def _stream_ptr(stream):
+    return ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
+
+
+def potrf_device(A, algo=ALGO_FAST, info=None, stream=None):
+    """Cholesky of a column-major CUDA tensor in place.  `A` is a torch tensor
+    whose transpose is contiguous (A.T.is_contiguous(), i.e. Fortran order);
+    returns the device int64 info tensor (-1 = success, else failing row)."""
+    import torch
+    n = A.shape[0]
+    assert A.is_cuda and A.shape == (n, n) and A.stride(0) == 1
+    if info is None:
+        info = torch.empty(1, dtype=torch.int64, device=A.device)
+    e = Error()
+    p = "d" if A.dtype == torch.float64 else "s"
+    getattr(lib, f"lla_{p}potrf_device")(ctypes.c_void_p(A.data_ptr()), n, A.stride(1), algo,
+                                         ctypes.c_void_p(info.data_ptr()), _stream_ptr(stream),
+                                         ctypes.byref(e))
+    _raise(e)
+    return info
+
+
+def trsm_device(L, B, trans, algo=ALGO_FAST, stream=None):
+    """Solves L X = B (trans=0) or L^T X = B (trans=1) in place on the
+    column-major CUDA tensor B, with the lower factor in column-major L."""
+    import torch
+    n = L.shape[0]
+    assert L.stride(0) == 1 and B.stride(0) == 1 and B.shape[0] == n
+    e = Error()
+    p = "d" if L.dtype == torch.float64 else "s"
+    getattr(lib, f"lla_{p}trsm_device")(ctypes.c_void_p(L.data_ptr()), n, L.stride(1), trans,
+                                        ctypes.c_void_p(B.data_ptr()), B.shape[1],
+                                        max(1, B.stride(1)), algo, _stream_ptr(stream),
+                                        ctypes.byref(e))
+    _raise(e)
+    return B

@@ -1,0 +1,53 @@
+// lla_api_internal.h -- per-thread execution context of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/lla_gb300.h"
+
+namespace lla {
+
+// Grow-only device buffer.
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes);
+    ~DevBuf();
+};
+
+// Grow-only pinned host buffer.
+struct HostBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes);
+    ~HostBuf();
+};
+
+// One per calling host thread: its own stream and buffers, so concurrent
+// callers never share scratch memory.
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    DevBuf small_dev;                 // status words
+    HostBuf small_host;
+    DevBuf raw_a, raw_b;              // host views as uploaded
+    DevBuf work_a, work_b;            // column-major working copies
+    DevBuf aux_s, aux_d, aux_diag;    // factor scratch (EXACT S/D, FAST diag0), diag override
+    DevBuf ws;                        // triangular-solve tickets and flags
+    DevBuf dev_s, dev_d, dev_ws;      // scratch of the device-resident entry points
+    HostBuf stage_a, stage_b;         // pinned staging for strided views
+    ~Ctx();
+};
+
+Ctx *get_ctx(lla_error *err);
+
+template <typename T>
+cudaError_t factor_on_device(Ctx &c, T *W, int64_t n, int64_t ld, bool exact, const T *R,
+                             int64_t drs, int64_t dcs, int64_t *fail);
+template <typename T>
+cudaError_t trsm_on_device(Ctx &c, const T *M, int64_t ld, int64_t n, int lower, int trans,
+                           const T *diag, T *B, int64_t ldb, int64_t m, bool exact, int *timed_out);
+
+}  // namespace lla

@@ -1,0 +1,53 @@
+// lla_kernels.h -- internal launcher declarations shared by the .cu files and
+// the C-ABI layer.  All launchers are asynchronous on `st` and return 0 on a
+// successful launch, -1 when a CUDA call failed (cudaGetLastError tells why).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+namespace lla {
+
+// Cholesky, lower triangle of the n x n column-major W (leading dim ld).
+// *d_info (device, int64) must hold -1 on entry; it receives the first
+// failing row.  EXACT needs S (ld * n) and D (n) scratch.
+template <typename T>
+int potrf_exact_launch(T *W, T *S, T *D, int64_t n, int64_t ld, int64_t *d_info, cudaStream_t st);
+// FAST needs diag0 (n) scratch and min_ratio (device double, preset to a
+// large value) for the near-singular guard.
+template <typename T>
+int potrf_fast_launch(T *W, int64_t n, int64_t ld, int64_t *d_info, T *diag0, double *min_ratio,
+                      cudaStream_t st);
+
+// Triangular solve op(T) X = B in place (see lla_trsm.cu).  ws: trsm_ws_ints
+// ints of scratch; err_word: device int, 0 on entry.
+template <typename T>
+int trsm_launch(const T *M, int64_t ld, int64_t n, int lower, int trans, const T *diag, T *B,
+                int64_t ldb, int64_t m, bool exact, int *ws, int *err_word, cudaStream_t st);
+size_t trsm_ws_ints(int64_t n, int64_t m);
+
+// Layout kernels (lla_layout.cu).
+enum ExportMode { EXPORT_FULL = 0, EXPORT_LOWER = 1, EXPORT_LOWER_ZERO_UPPER = 2, EXPORT_FAIL = 3 };
+// W[i + j*ld] = R[i*rs + j*cs] for i < rows, j < cols.
+template <typename T>
+int import_launch(const T *R, int64_t rs, int64_t cs, int64_t rows, int64_t cols, T *W, int64_t ld,
+                  cudaStream_t st);
+// R[i*rs + j*cs] = W[i + j*ld] for the entries selected by mode (fail_row
+// for EXPORT_FAIL: rows < f with j <= i, and row f with j < f).
+template <typename T>
+int export_launch(const T *W, int64_t ld, T *R, int64_t rs, int64_t cs, int64_t rows, int64_t cols,
+                  int mode, int64_t fail_row, cudaStream_t st);
+// Zero the strict upper (uplo = LOWER) or strict lower (uplo = UPPER) part of R.
+template <typename T>
+int mask_launch(T *R, int64_t rs, int64_t cs, int64_t n, int uplo, cudaStream_t st);
+// *d_flag (device int, 1 on entry) becomes 0 when a non-zero lies outside the uplo triangle.
+template <typename T>
+int is_triangular_launch(const T *R, int64_t rs, int64_t cs, int64_t n, int uplo, int *d_flag,
+                         cudaStream_t st);
+// W = identity (n x n, ld).
+template <typename T>
+int eye_launch(T *W, int64_t ld, int64_t n, cudaStream_t st);
+
+}  // namespace lla
