@@ -79,12 +79,12 @@ def test_kats(exact):
         ora.solve_triangular_inplace(np.array(c["a"]), ref, c["uplo"])
     assert np.array_equal(np.isnan(out), np.isnan(ref))
     c = cases.kat("triangular_square")
-    sq = np.array(c["a"])
+    sq = np.array(c["a"], dtype=np.float64)  # the reference's mask tests use integers
     assert lla.into_triangular(sq.copy(), "upper").tolist() == c["upper"]
     assert lla.into_triangular(sq.copy(), "lower").tolist() == c["lower"]
     assert not lla.is_triangular(sq, "upper") and not lla.is_triangular(sq, "lower")
-    assert lla.is_triangular(np.array(c["upper"]), "upper")
-    assert lla.is_triangular(np.array(c["lower"]), "lower")
+    assert lla.is_triangular(np.array(c["upper"], dtype=np.float64), "upper")
+    assert lla.is_triangular(np.array(c["lower"], dtype=np.float64), "lower")
 
 
 # ---- property tests, bit-identical to the oracle ----------------------------
@@ -252,8 +252,11 @@ def test_wrong_rows_after_factor(gpu_lla):
 def test_nan_propagates_without_error(gpu_lla):
     lla = gpu_lla
     a = np.array([[np.nan, 0.0], [0.0, 1.0]])
-    out = lla.cholesky(a)
-    assert np.isnan(out[0, 0]) and out[1, 1] == 1.0
+    out = lla.cholesky(a)  # `d <= 0` is false for NaN (src/cholesky.rs:69)
+    ref = a.copy()
+    assert ora.cholesky_inplace(ref)["code"] == 0
+    assert np.isnan(out[0, 0]) and np.isnan(out[1, 1])
+    assert same_bits(np.isnan(out), np.isnan(ref))
 
 
 # ---- FAST mode: tolerance of the FP64 path ----------------------------------
