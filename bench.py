@@ -1,0 +1,350 @@
+"""Benchmark: SPD solves/s of the single large f64 system, n = 16384 with 64
+right-hand sides, A = Q diag(s) Q^T (Q from the QR of a seeded Gaussian,
+s log-uniform in [1, 1e6], kappa = 1e6), B ~ N(0, 1), on one GB300.
+
+A "step" is one complete solve of that system with the inputs resident in
+HBM: copy A into the working buffer, factor, and solve (plus refinement for
+the mixed-precision form).  Every solution is checked to reach normwise
+backward error <= 1e-13 before a number is reported.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm on the host cores (the C
+restatement of linfa-linalg's solvec in oracle/, the reference itself being a
+Rust crate that cannot be built here) on bounded samples of the same workload
+and scales them to the n = 16384 system by the flop model.
+
+Under torchrun (N > 1) each rank solves its own copy of the system (a single
+factorisation does not shard: replicas only); `value` is the solves of all
+ranks divided by the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT, NRHS_DEFAULT, KAPPA_DEFAULT, SEED = 16384, 64, 1e6, 20240611
+BE_TARGET = 1e-13
+METRIC = "SPD solves/s at backward error <= 1e-13 (n=16384, 64 RHS, kappa=1e6)"
+
+
+def flops_solve(n, m):
+    """Cholesky n^3/3 + two triangular solves 2 n^2 m."""
+    return n ** 3 / 3.0 + 2.0 * n * n * m
+
+
+# ---------------------------------------------------------------------------
+# reference arm / CPU baseline (oracle; test infrastructure, never the product)
+
+def _cpu_sample(args):
+    n, m, seed = args
+    from oracle import oracle as ora
+    rng = np.random.default_rng(seed)
+    g = rng.standard_normal((n, n))
+    a = g @ g.T / n + np.eye(n)
+    b = rng.standard_normal((n, m))
+    t0 = time.perf_counter()
+    st = ora.solvec_inplace(a, b)
+    dt = time.perf_counter() - t0
+    assert st["code"] == 0
+    return dt
+
+
+def cpu_rate(n_sample, m, workers, seed=1):
+    """Solves/s of the oracle on `workers` processes (one solve each),
+    scaled from n_sample to the n = 16384 system by the flop model."""
+    import multiprocessing as mp
+    if workers <= 1:
+        dt = _cpu_sample((n_sample, m, seed))
+        rate_sample = 1.0 / dt
+    else:
+        # concurrent independent solves; each worker times its own solve only
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(workers) as pool:
+            dts = pool.map(_cpu_sample, [(n_sample, m, seed + i) for i in range(workers)])
+        rate_sample = sum(1.0 / d for d in dts)
+        dt = max(dts)
+    scale = flops_solve(n_sample, m) / flops_solve(N_DEFAULT, NRHS_DEFAULT)
+    return rate_sample * scale, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as ora
+    ora.lib()  # builds the oracle if needed
+    workers = os.cpu_count() or 1
+    n_s = args.ref_sample_n
+    m = NRHS_DEFAULT
+    for _ in range(args.warmup):
+        cpu_rate(n_s, m, workers)
+    rates, secs = [], []
+    for _ in range(args.steps):
+        r, dt = cpu_rate(n_s, m, workers)
+        rates.append(r)
+        secs.append(dt)
+    value = statistics.median(rates)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * statistics.median(secs), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"single SPD solve n={N_DEFAULT} nrhs={NRHS_DEFAULT} kappa=1e6",
+                   "sample": f"solvec n={n_s} nrhs={m} per process, A = G G^T/n + I"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": workers, "kind": "port",
+                         "sample": f"{workers} concurrent oracle solvec n={n_s} m={m}, "
+                                   f"scaled by (n^3/3+2n^2m) to n={N_DEFAULT}"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        rows = []
+        with open(self.f.name) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def make_system(torch, n, m, kappa, seed, device):
+    """A = Q diag(s) Q^T, Q from QR of a seeded Gaussian, s log-uniform in
+    [1, kappa]; B ~ N(0,1).  Built in FP64 on the device."""
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    G = torch.randn(n, n, dtype=torch.float64, device=device, generator=g)
+    Q, _ = torch.linalg.qr(G)
+    del G
+    u = torch.rand(n, dtype=torch.float64, device=device, generator=g)
+    s = torch.exp(u * np.log(kappa))
+    s[0], s[-1] = 1.0, kappa
+    A = (Q * s) @ Q.T
+    del Q
+    A = (A + A.T) * 0.5
+    B = torch.randn(n, m, dtype=torch.float64, device=device, generator=g)
+    return A, B
+
+
+def backward_error(torch, A, X, B):
+    R = B - A @ X
+    num = R.abs().amax(dim=0)
+    den = A.abs().sum(dim=1).amax() * X.abs().amax(dim=0) + B.abs().amax(dim=0)
+    return float((num / den).max())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--nrhs", type=int, default=NRHS_DEFAULT)
+    ap.add_argument("--ref-sample-n", type=int, default=2048)
+    ap.add_argument("--cpu-sample-n", type=int, default=4096)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    import __graft_entry__
+    lla = __graft_entry__.load_package()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    n, m = args.n, args.nrhs
+
+    # CPU baseline first (before any GPU work), bounded sample, 1 core
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as ora
+        ora.lib()
+        rate, dt = cpu_rate(args.cpu_sample_n, m, 1)
+        cpu = {"value": rate, "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": f"oracle solvec n={args.cpu_sample_n} m={m} on 1 core took {dt:.2f} s; "
+                         f"scaled by (n^3/3+2n^2m) to n={n}"}
+
+    A0, B0 = make_system(torch, n, m, KAPPA_DEFAULT, SEED + rank, dev)
+    W = torch.empty_like(A0)  # column-major view: W.T is the row-major buffer
+    X = torch.empty_like(B0.T.contiguous()).T  # column-major (n, m)
+    info = torch.empty(1, dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def plain_step():
+        # A is symmetric: its row-major buffer is also its column-major buffer
+        W.copy_(A0)
+        lla.potrf_device(W.T, algo=lla.ALGO_FAST, info=info, stream=stream)
+        X.copy_(B0)
+        lla.trsm_device(W.T, X, 0, algo=lla.ALGO_FAST, stream=stream)
+        lla.trsm_device(W.T, X, 1, algo=lla.ALGO_FAST, stream=stream)
+
+    # correctness gate
+    plain_step()
+    torch.cuda.synchronize()
+    assert int(info.item()) == -1, "plain FP64 factorisation failed"
+    be_plain = backward_error(torch, A0, X, B0)
+    assert be_plain <= BE_TARGET, be_plain
+
+    def timed(step, k, w, profile=False):
+        for _ in range(w):
+            step()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        l0 = lla.kernel_launches()
+        if profile:
+            lla.profile_start()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with Clocks(local) as clk:
+            e0.record(stream)
+            for _ in range(k):
+                step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+        prof = lla.profile_stop() if profile else None
+        launches = lla.kernel_launches() - l0
+        ms = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+            dist.barrier()
+        return ms, launches, prof, clk.summary()
+
+    ms_plain, launches_plain, prof_plain, clocks = timed(plain_step, args.steps, args.warmup,
+                                                         profile=True)
+    plain_sps = world * args.steps / (ms_plain / 1e3)
+
+    # headline path: the plain FP64 GPU path (the mixed-precision form is added here
+    # when available); roofline of its dominant kernel
+    value, ms_step, launches = plain_sps, ms_plain / args.steps, launches_plain
+    prof = prof_plain
+    dom = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_n, dom_work = prof[dom]
+    fp64_peak = lla.measure_peak_tflops(0)
+    achieved = dom_work / (dom_ms * 1e-3) / 1e12
+    roofline = {"kernel": dom, "bound": "fp64-tensor", "achieved": achieved, "peak": fp64_peak,
+                "unit": "TFLOP/s", "frac": achieved / fp64_peak if fp64_peak > 0 else None,
+                "traffic": None, "share_of_step": dom_ms / ms_plain,
+                "avg_launch_ms": dom_ms / dom_n,
+                "peak_source": "measured live: mma.sync m16n8k16 f64 loop on all SMs "
+                               "(no FP64 entry in the measured peak table)"}
+
+    # end to end through the C ABI with host (pinned) buffers: lla_dsolvec_inplace
+    # writes the dirty factor back into A and X into B, as the reference's solvec_inplace
+    e2e = None
+    if rank == 0:
+        Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+        Bh = torch.empty((n, m), dtype=torch.float64, pin_memory=True)
+        A0_cpu, B0_cpu = A0.cpu(), B0.cpu()
+        prev = lla.set_algorithm(lla.ALGO_FAST)
+        tot = 0.0
+        k_e2e = max(1, min(args.steps, 2))
+        for it in range(k_e2e + 1):
+            Ah.copy_(A0_cpu)
+            Bh.copy_(B0_cpu)
+            t0 = time.perf_counter()
+            lla.solvec_inplace(Ah.numpy(), Bh.numpy())
+            dt = time.perf_counter() - t0
+            if it > 0:
+                tot += dt
+        lla.set_algorithm(prev)
+        be = backward_error(torch, A0, Bh.to(dev), B0)
+        assert be <= BE_TARGET, be
+        e2e = {"value": k_e2e / tot, "unit": "solves/s",
+               "h2d_bytes_per_step": (n * n + n * m) * 8, "d2h_bytes_per_step": (n * n + n * m) * 8,
+               "path": "lla_dsolvec_inplace (FAST FP64), pinned host row-major A and B"}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Q diag(s) Q^T, built on the device)",
+            "config": {"workload": f"single SPD solve n={n} nrhs={m} kappa=1e6",
+                       "path": "plain FP64 (blocked right-looking Cholesky, FP64 tensor-pipe "
+                               "trailing update, look-back triangular solves)",
+                       "l2": "inputs larger than L2 (A = %.2f GB)" % (n * n * 8 / 1e9),
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "backward_error": be_plain,
+            "plain_fp64": {"value": plain_sps, "unit": "solves/s", "ms_per_step": ms_plain / args.steps,
+                           "backward_error": be_plain},
+            "gflops": flops_solve(n, m) * value / 1e9,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": launches,
+            "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
+        }
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

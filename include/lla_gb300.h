@@ -189,6 +189,22 @@ int lla_dtrsm_device(const double *dL, int64_t n, int64_t ld, int trans, double 
 int lla_strsm_device(const float *dL, int64_t n, int64_t ld, int trans, float *dB, int64_t m,
                      int64_t ldb, int algo, void *stream, lla_error *err);
 
+
+/* ---- diagnostics (no counterpart in the reference) ----------------------
+ * Launch accounting and per-kernel CUDA-event timing used by the benchmark:
+ * while profiling is on, every kernel launch is bracketed by an event pair on
+ * its stream; lla_profile_stop() synchronises and sums the durations and the
+ * algorithmic work (flops, or bytes for data-movement kernels) per kernel
+ * name ("potrf_fast_update", "trsm", ...). */
+int64_t lla_kernel_launches(void);
+void lla_profile_start(void);
+int lla_profile_stop(void);
+int lla_profile_query(const char *kernel, double *total_ms, int64_t *launches, double *work);
+const char *lla_profile_kernel_name(int index);
+/* Measured arithmetic peak in TFLOP/s of this GPU: which = 0 FP64 tensor pipe
+ * (mma m16n8k16 .f64), 1 FP64 FMA, 2 FP32 FMA; negative on error. */
+double lla_measure_peak_tflops(int which);
+
 #ifdef __cplusplus
 }
 #endif

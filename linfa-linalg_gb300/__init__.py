@@ -72,6 +72,14 @@ EXPORTS = {
     "lla_device_count": ([], ctypes.c_int),
     "lla_version": ([], ctypes.c_char_p),
     "lla_status_string": ([ctypes.c_int], ctypes.c_char_p),
+    "lla_kernel_launches": ([], ctypes.c_int64),
+    "lla_profile_start": ([], None),
+    "lla_profile_stop": ([], ctypes.c_int),
+    "lla_profile_query": ([ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
+                           ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double)],
+                          ctypes.c_int),
+    "lla_profile_kernel_name": ([ctypes.c_int], ctypes.c_char_p),
+    "lla_measure_peak_tflops": ([ctypes.c_int], ctypes.c_double),
 }
 for _p in "ds":
     EXPORTS.update({
@@ -179,6 +187,39 @@ def get_algorithm():
 
 def device_count():
     return lib.lla_device_count()
+
+
+def kernel_launches():
+    """Kernels launched by the library since it was loaded."""
+    return lib.lla_kernel_launches()
+
+
+def profile_start():
+    lib.lla_profile_start()
+
+
+def profile_stop():
+    """Returns {kernel: (total_ms, launches, work)} for kernels launched while profiling."""
+    rc = lib.lla_profile_stop()
+    if rc:
+        raise DeviceError(rc)
+    out = {}
+    i = 0
+    while True:
+        name = lib.lla_profile_kernel_name(i)
+        if name is None:
+            break
+        ms, cnt, work = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
+        lib.lla_profile_query(name, ctypes.byref(ms), ctypes.byref(cnt), ctypes.byref(work))
+        if cnt.value:
+            out[name.decode()] = (ms.value, cnt.value, work.value)
+        i += 1
+    return out
+
+
+def measure_peak_tflops(which):
+    """0: FP64 tensor pipe (mma .f64), 1: DFMA, 2: FFMA -- measured on this GPU."""
+    return lib.lla_measure_peak_tflops(which)
 
 
 # ---- CholeskyInplace / Cholesky (src/cholesky.rs:16-115) -------------------

@@ -7,6 +7,7 @@
 // written in coalesced runs whichever way the view is laid out.
 #include "lla_common.cuh"
 #include "lla_kernels.h"
+#include "lla_prof.h"
 
 namespace lla {
 
@@ -101,6 +102,7 @@ template <typename T>
 int import_launch(const T *R, int64_t rs, int64_t cs, int64_t rows, int64_t cols, T *W, int64_t ld,
                   cudaStream_t st) {
     if (rows == 0 || cols == 0) return 0;
+    LaunchScope ls(K_LAYOUT, st);
     import_kernel<T><<<tiles2d(rows, cols), dim3(32, 8), 0, st>>>(R, rs, cs, rows, cols, W, ld);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
@@ -109,6 +111,7 @@ template <typename T>
 int export_launch(const T *W, int64_t ld, T *R, int64_t rs, int64_t cs, int64_t rows, int64_t cols,
                   int mode, int64_t fail_row, cudaStream_t st) {
     if (rows == 0 || cols == 0) return 0;
+    LaunchScope ls(K_LAYOUT, st);
     export_kernel<T><<<tiles2d(rows, cols), dim3(32, 8), 0, st>>>(W, ld, R, rs, cs, rows, cols,
                                                                   mode, fail_row);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
@@ -117,6 +120,7 @@ int export_launch(const T *W, int64_t ld, T *R, int64_t rs, int64_t cs, int64_t 
 template <typename T>
 int mask_launch(T *R, int64_t rs, int64_t cs, int64_t n, int uplo, cudaStream_t st) {
     if (n == 0) return 0;
+    LaunchScope ls(K_LAYOUT, st);
     mask_kernel<T><<<tiles2d(n, n), dim3(32, 32), 0, st>>>(R, rs, cs, n, uplo);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
@@ -125,6 +129,7 @@ template <typename T>
 int is_triangular_launch(const T *R, int64_t rs, int64_t cs, int64_t n, int uplo, int *d_flag,
                          cudaStream_t st) {
     if (n == 0) return 0;
+    LaunchScope ls(K_LAYOUT, st);
     is_triangular_kernel<T><<<tiles2d(n, n), dim3(32, 32), 0, st>>>(R, rs, cs, n, uplo, d_flag);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
@@ -133,6 +138,7 @@ template <typename T>
 int eye_launch(T *W, int64_t ld, int64_t n, cudaStream_t st) {
     if (n == 0) return 0;
     const unsigned gy = (unsigned)std::min<int64_t>(n, 65535);
+    LaunchScope ls(K_LAYOUT, st);
     eye_kernel<T><<<dim3((unsigned)ceil_div(n, 256), gy), 256, 0, st>>>(W, ld, n);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -18,6 +18,7 @@
 // (mma.sync m16n8k16 .f64), measured on GB300 at twice the DFMA rate.
 #include "lla_common.cuh"
 #include "lla_kernels.h"
+#include "lla_prof.h"
 
 namespace lla {
 
@@ -374,11 +375,18 @@ int potrf_exact_launch(T *W, T *S, T *D, int64_t n, int64_t ld, int64_t *d_info,
     if (cudaMemsetAsync(S, 0, sizeof(T) * ld * n, st) != cudaSuccess) return -1;
     for (int64_t p = 0; p < n; p += kNbExact) {
         const int b = (int)std::min<int64_t>(kNbExact, n - p);
-        potrf_exact_diag<T><<<1, dim3(32, 32), 0, st>>>(W, S, D, ld, p, b, d_info);
+        {
+            LaunchScope ls(K_POTRF_EXACT_DIAG, st, (double)b * b * b / 3.0);
+            potrf_exact_diag<T><<<1, dim3(32, 32), 0, st>>>(W, S, D, ld, p, b, d_info);
+        }
         const int64_t rest = n - p - b;
         if (rest > 0) {
-            potrf_exact_panel<T><<<(unsigned)ceil_div(rest, 128), 128, 0, st>>>(W, S, D, ld, n, p,
-                                                                             b, d_info);
+            {
+                LaunchScope ls(K_POTRF_EXACT_PANEL, st, (double)rest * b * b);
+                potrf_exact_panel<T><<<(unsigned)ceil_div(rest, 128), 128, 0, st>>>(
+                    W, S, D, ld, n, p, b, d_info);
+            }
+            LaunchScope ls(K_POTRF_EXACT_UPDATE, st, (double)rest * (rest - 1) * b);
             potrf_update_simt<T, true><<<(unsigned)tri_tiles(rest, kUpdTile), 256, 0, st>>>(
                 W, S, ld, n, p, b, d_info);
         }
@@ -389,14 +397,25 @@ int potrf_exact_launch(T *W, T *S, T *D, int64_t n, int64_t ld, int64_t *d_info,
 template <typename T>
 int potrf_fast_launch(T *W, int64_t n, int64_t ld, int64_t *d_info, T *diag0, double *min_ratio,
                       cudaStream_t st) {
-    copy_diag<T><<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(W, ld, n, diag0);
+    {
+        LaunchScope ls(K_MISC, st);
+        copy_diag<T><<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(W, ld, n, diag0);
+    }
     for (int64_t p = 0; p < n; p += kNbFast) {
         const int b = (int)std::min<int64_t>(kNbFast, n - p);
-        potrf_fast_diag<T><<<1, 1024, 0, st>>>(W, ld, p, b, diag0, d_info, min_ratio);
+        {
+            LaunchScope ls(K_POTRF_FAST_DIAG, st, (double)b * b * b / 3.0);
+            potrf_fast_diag<T><<<1, 1024, 0, st>>>(W, ld, p, b, diag0, d_info, min_ratio);
+        }
         const int64_t rest = n - p - b;
         if (rest > 0) {
-            potrf_fast_panel<T><<<(unsigned)ceil_div(rest, 128), 128, 0, st>>>(W, ld, n, p, b,
-                                                                            d_info);
+            {
+                LaunchScope ls(K_POTRF_FAST_PANEL, st, (double)rest * b * b);
+                potrf_fast_panel<T><<<(unsigned)ceil_div(rest, 128), 128, 0, st>>>(W, ld, n, p, b,
+                                                                                d_info);
+            }
+            // algorithmic work: rest*(rest+1)/2 lower entries x b multiply-adds x 2
+            LaunchScope ls(K_POTRF_FAST_UPDATE, st, (double)rest * (rest + 1) * b);
             if constexpr (sizeof(T) == 8)
                 potrf_fast_update_dmma<<<(unsigned)tri_tiles(rest, 64), 128, 0, st>>>(
                     (double *)W, ld, n, p, b, d_info);

@@ -25,6 +25,7 @@
 // the diagonal as the reference's diag_fn does (src/triangular.rs:133-144).
 #include "lla_common.cuh"
 #include "lla_kernels.h"
+#include "lla_prof.h"
 
 namespace lla {
 
@@ -160,6 +161,8 @@ int trsm_launch(const T *M, int64_t ld, int64_t n, int lower, int trans, const T
     if (cudaMemsetAsync(ws, 0, sizeof(int) * (1 + R * chunks), st) != cudaSuccess) return -1;
     const dim3 block(kTrsmNb, mc);
     const unsigned grid = (unsigned)(R * chunks);
+    // algorithmic work: n^2 * m flops (n(n-1)/2 multiply-adds and n divisions per column)
+    LaunchScope ls(K_TRSM, st, (double)n * n * m);
     if (exact)
         trsm_lookback<T, true><<<grid, block, 0, st>>>(M, ld, n, lower, trans, diag, B, ldb, m, mc,
                                                        (int)chunks, ws, err_word);
