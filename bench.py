@@ -199,7 +199,8 @@ def main():
     ap.add_argument("--nrhs", type=int, default=NRHS_DEFAULT)
     ap.add_argument("--ref-sample-n", type=int, default=2048)
     ap.add_argument("--cpu-sample-n", type=int, default=4096)
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI leg")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -300,7 +301,7 @@ def main():
     # end to end through the C ABI with host (pinned) buffers: lla_dsolvec_inplace
     # writes the dirty factor back into A and X into B, as the reference's solvec_inplace
     e2e = None
-    if rank == 0:
+    if rank == 0 and not args.no_e2e:
         Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
         Bh = torch.empty((n, m), dtype=torch.float64, pin_memory=True)
         A0_cpu, B0_cpu = A0.cpu(), B0.cpu()
