@@ -46,7 +46,8 @@ enum lla_status {
     LLA_ERR_TIMEOUT = 19,          /* a bounded device wait gave up */
     LLA_ERR_NO_DEVICE = 20,        /* no CUDA device visible */
     LLA_ERR_NOT_CONVERGED = 21,    /* refinement stalled and fallback was disabled */
-    LLA_ERR_BUSY = 22              /* admission refused (serving loop at its HBM budget) */
+    LLA_ERR_BUSY = 22,             /* admission refused (serving loop at its HBM budget) */
+    LLA_ERR_TOO_LARGE = 23         /* problem exceeds a fixed-size scratch area */
 };
 
 typedef struct lla_error {
@@ -188,6 +189,19 @@ int lla_dtrsm_device(const double *dL, int64_t n, int64_t ld, int trans, double 
                      int64_t ldb, int algo, void *stream, lla_error *err);
 int lla_strsm_device(const float *dL, int64_t n, int64_t ld, int trans, float *dB, int64_t m,
                      int64_t ldb, int algo, void *stream, lla_error *err);
+
+/* Allocation-free variant of lla_dtrsm_device (same arguments and results).
+ * It has no counterpart in the reference.  It exists for callers that must
+ * not allocate device memory (inside another allocator's callback, under a
+ * host framework that owns all device memory, in loops where an allocation
+ * would synchronise): its scratch is a fixed device array inside the library,
+ * so it never calls cudaMalloc/cudaFree.  Limit: ceil(n/32) * ceil(m/min(8,m))
+ * <= 65536 (e.g. n <= 16384 with m <= 1024); larger problems return
+ * LLA_ERR_TOO_LARGE.  The first call on each device looks up the array's
+ * device address (make it before any stream capture).  All calls share the
+ * array: calls that overlap on the GPU race. */
+int lla_dtrsm_device_noalloc(const double *dL, int64_t n, int64_t ld, int trans, double *dB,
+                             int64_t m, int64_t ldb, int algo, void *stream, lla_error *err);
 
 
 /* ---- diagnostics (no counterpart in the reference) ----------------------

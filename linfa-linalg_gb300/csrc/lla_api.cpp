@@ -120,6 +120,7 @@ extern "C" const char *lla_status_string(int code) {
         case LLA_ERR_NO_DEVICE: return "no CUDA device";
         case LLA_ERR_NOT_CONVERGED: return "refinement did not converge";
         case LLA_ERR_BUSY: return "admission refused";
+        case LLA_ERR_TOO_LARGE: return "problem exceeds the fixed scratch area";
         default: return "unknown status";
     }
 }

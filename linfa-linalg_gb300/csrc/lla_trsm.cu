@@ -184,3 +184,95 @@ template int trsm_launch<float>(const float *, int64_t, int64_t, int, int, const
                                 int64_t, int64_t, bool, int *, int *, cudaStream_t);
 
 }  // namespace lla
+
+// ---------------------------------------------------------------------------
+// Allocation-free triangular solve (lla_dtrsm_device_noalloc).
+//
+// Some callers cannot call cudaMalloc: code that runs inside another
+// library's memory-pool callback, processes whose device memory is carved up
+// once at start-up by a host framework that owns every allocation, or
+// latency-critical loops where an allocation would synchronise the device.
+// This entry point takes its ticket/flag scratch from a fixed, file-scope
+// device array instead of library-owned buffers.  The array is part of the
+// module image, so every GPU that loads the library holds it (a little over
+// 256 KiB) until the process exits.
+//
+// Host code cannot use the array's name as a device address (on the host it
+// names a stand-in object); the device address is obtained once per device
+// with cudaGetSymbolAddress, on the first call made while that device is
+// current, and cached.  That first call therefore also does the set-up and
+// should come before any stream capture.
+//
+// All calls share the one array and it keeps the last call's contents: each
+// call clears the part it uses before its launch, and calls whose work
+// overlaps on the GPU (different streams, or different host threads without
+// ordering) race on it.
+
+#include <mutex>
+
+namespace lla {
+
+constexpr int kNoAllocMaxFlags = 1 << 16;  // row blocks x RHS chunks
+constexpr int kNoAllocMaxDevices = 64;
+// [0] ticket counter, [1 .. kNoAllocMaxFlags] flags, [kNoAllocMaxFlags + 1] error word
+static __device__ __align__(256) int g_trsm_noalloc_scratch[kNoAllocMaxFlags + 2];
+
+static std::mutex g_noalloc_mu;
+static int *g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+static cudaError_t noalloc_scratch(int **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_trsm_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_addr[dev] = (int *)p;
+    }
+    *out = g_noalloc_addr[dev];
+    return cudaSuccess;
+}
+
+}  // namespace lla
+
+extern "C" int lla_dtrsm_device_noalloc(const double *dL, int64_t n, int64_t ld, int trans,
+                                        double *dB, int64_t m, int64_t ldb, int algo, void *stream,
+                                        lla_error *err) {
+    using namespace lla;
+    if (n < 0 || m < 0 || ld < std::max<int64_t>(1, n) || ldb < std::max<int64_t>(1, n) ||
+        (n > 0 && m > 0 && (!dL || !dB)) || (algo != LLA_ALGO_EXACT && algo != LLA_ALGO_FAST))
+        return lla__set_status(err, LLA_ERR_INVALID_ARG);
+    lla__set_status(err, LLA_OK);
+    if (n == 0 || m == 0) return LLA_OK;
+    const int mc = (int)std::min<int64_t>(kTrsmMaxMc, m);
+    const int64_t chunks = ceil_div(m, mc);
+    const int64_t R = ceil_div(n, kTrsmNb);
+    if (R * chunks > kNoAllocMaxFlags) return lla__set_status(err, LLA_ERR_TOO_LARGE);
+    int *scratch = nullptr;
+    cudaError_t e = noalloc_scratch(&scratch);
+    if (e != cudaSuccess) return lla__set_cuda_error(err, e);
+    cudaStream_t st = (cudaStream_t)stream;
+    int *err_word = scratch + kNoAllocMaxFlags + 1;
+    e = cudaMemsetAsync(scratch, 0, sizeof(int) * (size_t)(1 + R * chunks), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(err_word, 0, sizeof(int), st);
+    if (e != cudaSuccess) return lla__set_cuda_error(err, e);
+    prof_note_launch();
+    const dim3 block(kTrsmNb, mc);
+    const unsigned grid = (unsigned)(R * chunks);
+    // trans = 0: L X = B (lower, ascending); trans = 1: L^T X = B (descending)
+    const int lower = trans ? 0 : 1;
+    if (algo == LLA_ALGO_EXACT)
+        trsm_lookback<double, true><<<grid, block, 0, st>>>(dL, ld, n, lower, trans ? 1 : 0,
+                                                            nullptr, dB, ldb, m, mc, (int)chunks,
+                                                            scratch, err_word);
+    else
+        trsm_lookback<double, false><<<grid, block, 0, st>>>(dL, ld, n, lower, trans ? 1 : 0,
+                                                             nullptr, dB, ldb, m, mc, (int)chunks,
+                                                             scratch, err_word);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return lla__set_cuda_error(err, e);
+    return LLA_OK;
+}
