@@ -167,6 +167,13 @@ class Clocks:
 def make_system(torch, n, m, kappa, seed, device):
     """A = Q diag(s) Q^T, Q from QR of a seeded Gaussian, s log-uniform in
     [1, kappa]; B ~ N(0,1).  Built in FP64 on the device."""
+    # torch loads its CUDA linear-algebra library lazily by name; under a
+    # profiler that rewrites the loader environment that lookup can fail, so
+    # load it by path first.
+    import ctypes
+    lib = os.path.join(os.path.dirname(torch.__file__), "lib", "libtorch_cuda_linalg.so")
+    if os.path.exists(lib):
+        ctypes.CDLL(lib, mode=ctypes.RTLD_GLOBAL)
     g = torch.Generator(device=device)
     g.manual_seed(seed)
     G = torch.randn(n, n, dtype=torch.float64, device=device, generator=g)
