@@ -208,6 +208,9 @@ def main():
     ap.add_argument("--cpu-sample-n", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI leg")
+    ap.add_argument("--update", default="fp16x3",
+                    help="trailing-update form of the mixed path: fp32|bf16|bf16x3|bf16x6|fp16|fp16x3")
+    ap.add_argument("--plain-steps", type=int, default=2, help="timed steps of the plain FP64 leg")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -238,25 +241,37 @@ def main():
                          f"scaled by (n^3/3+2n^2m) to n={n}"}
 
     A0, B0 = make_system(torch, n, m, KAPPA_DEFAULT, SEED + rank, dev)
-    W = torch.empty_like(A0)  # column-major view: W.T is the row-major buffer
-    X = torch.empty_like(B0.T.contiguous()).T  # column-major (n, m)
+    A0c = A0.T  # A is symmetric: its row-major buffer is also its column-major buffer
+    B0c = B0.T.contiguous().T  # column-major (n, m)
+    W = torch.empty_like(A0)
+    X = torch.empty_like(B0c.T).T  # column-major (n, m)
+    Xm = torch.empty_like(B0c.T).T
     info = torch.empty(1, dtype=torch.int64, device=dev)
     stream = torch.cuda.current_stream()
 
     def plain_step():
-        # A is symmetric: its row-major buffer is also its column-major buffer
         W.copy_(A0)
         lla.potrf_device(W.T, algo=lla.ALGO_FAST, info=info, stream=stream)
-        X.copy_(B0)
+        X.copy_(B0c)
         lla.trsm_device(W.T, X, 0, algo=lla.ALGO_FAST, stream=stream)
         lla.trsm_device(W.T, X, 1, algo=lla.ALGO_FAST, stream=stream)
 
-    # correctness gate
+    reports = []
+
+    def mixed_step():
+        reports.append(lla.posv_refined_device(A0c, B0c, Xm, stream=stream, update=args.update))
+
+    # correctness gates (outside the timed regions)
     plain_step()
     torch.cuda.synchronize()
     assert int(info.item()) == -1, "plain FP64 factorisation failed"
     be_plain = backward_error(torch, A0, X, B0)
     assert be_plain <= BE_TARGET, be_plain
+    mixed_step()
+    torch.cuda.synchronize()
+    be_mixed = backward_error(torch, A0, Xm, B0)
+    assert be_mixed <= BE_TARGET, (be_mixed, reports[-1])
+    fwd_vs_fp64 = float((Xm - X).abs().max() / X.abs().max())
 
     def timed(step, k, w, profile=False):
         for _ in range(w):
@@ -286,68 +301,81 @@ def main():
             dist.barrier()
         return ms, launches, prof, clk.summary()
 
-    ms_plain, launches_plain, prof_plain, clocks = timed(plain_step, args.steps, args.warmup,
-                                                         profile=True)
-    plain_sps = world * args.steps / (ms_plain / 1e3)
+    k_plain = max(1, min(args.steps, args.plain_steps))
+    ms_plain, _, prof_plain, _ = timed(plain_step, k_plain, min(args.warmup, 3), profile=True)
+    plain_sps = world * k_plain / (ms_plain / 1e3)
+    reports.clear()
+    ms_mixed, launches, prof, clocks = timed(mixed_step, args.steps, args.warmup, profile=True)
+    timed_reports = reports[-args.steps:]
+    mixed_sps = world * args.steps / (ms_mixed / 1e3)
+    assert all(r["backward_error"] <= BE_TARGET for r in timed_reports), timed_reports
 
-    # headline path: the plain FP64 GPU path (the mixed-precision form is added here
-    # when available); roofline of its dominant kernel
-    value, ms_step, launches = plain_sps, ms_plain / args.steps, launches_plain
-    prof = prof_plain
+    # roofline of the dominant kernel of the headline (mixed) step
+    fp64_peak = lla.measure_peak_tflops(0)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
+        if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     dom = max(prof, key=lambda k: prof[k][0])
     dom_ms, dom_n, dom_work = prof[dom]
-    fp64_peak = lla.measure_peak_tflops(0)
     achieved = dom_work / (dom_ms * 1e-3) / 1e12
-    roofline = {"kernel": dom, "bound": "fp64-tensor", "achieved": achieved, "peak": fp64_peak,
-                "unit": "TFLOP/s", "frac": achieved / fp64_peak if fp64_peak > 0 else None,
-                "traffic": None, "share_of_step": dom_ms / ms_plain,
-                "avg_launch_ms": dom_ms / dom_n,
-                "peak_source": "measured live: mma.sync m16n8k16 f64 loop on all SMs "
-                               "(no FP64 entry in the measured peak table)"}
+    if dom in ("mixed_update",):
+        bound, peak, src = "tensor", peaks.get("bf16_tflops", 1891.6), \
+            "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks else "fallback 1.9 PF/s"
+    else:
+        bound, peak, src = "fp64-tensor", fp64_peak, \
+            "measured live: 8 independent mma.sync m16n8k16 f64 per step on all SMs " \
+            "(the measured peak table has HBM and bf16 only)"
+    roofline = {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak if peak and peak > 0 else None,
+                "traffic": None, "share_of_step": dom_ms / ms_mixed, "avg_launch_ms": dom_ms / dom_n,
+                "peak_source": src}
 
-    # end to end through the C ABI with host (pinned) buffers: lla_dsolvec_inplace
-    # writes the dirty factor back into A and X into B, as the reference's solvec_inplace
+    # end to end through the C ABI with host (pinned) buffers: lla_dposv_refined reads A
+    # and overwrites B with X
     e2e = None
     if rank == 0 and not args.no_e2e:
         Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
         Bh = torch.empty((n, m), dtype=torch.float64, pin_memory=True)
-        A0_cpu, B0_cpu = A0.cpu(), B0.cpu()
-        prev = lla.set_algorithm(lla.ALGO_FAST)
-        tot = 0.0
-        k_e2e = max(1, min(args.steps, 2))
+        Ah.copy_(A0.cpu())
+        B0_cpu = B0.cpu()
+        tot, k_e2e = 0.0, max(1, args.steps)
         for it in range(k_e2e + 1):
-            Ah.copy_(A0_cpu)
             Bh.copy_(B0_cpu)
             t0 = time.perf_counter()
-            lla.solvec_inplace(Ah.numpy(), Bh.numpy())
+            lla.posv_refined(Ah.numpy(), Bh.numpy(), update=args.update)
             dt = time.perf_counter() - t0
             if it > 0:
                 tot += dt
-        lla.set_algorithm(prev)
         be = backward_error(torch, A0, Bh.to(dev), B0)
         assert be <= BE_TARGET, be
         e2e = {"value": k_e2e / tot, "unit": "solves/s",
-               "h2d_bytes_per_step": (n * n + n * m) * 8, "d2h_bytes_per_step": (n * n + n * m) * 8,
-               "path": "lla_dsolvec_inplace (FAST FP64), pinned host row-major A and B"}
+               "h2d_bytes_per_step": (n * n + n * m) * 8, "d2h_bytes_per_step": n * m * 8,
+               "path": "lla_dposv_refined: pinned host row-major A (read) and B (overwritten by X)"}
 
     if rank == 0:
+        rep = timed_reports[-1]
         out = {
-            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "metric": METRIC, "value": mixed_sps, "unit": "solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mixed / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Q diag(s) Q^T, built on the device)",
             "config": {"workload": f"single SPD solve n={n} nrhs={m} kappa=1e6",
-                       "path": "plain FP64 (blocked right-looking Cholesky, FP64 tensor-pipe "
-                               "trailing update, look-back triangular solves)",
+                       "path": f"mixed: equilibrated low-precision Cholesky ({args.update} trailing "
+                               f"updates) + FP64 refinement, FP64 fallback",
                        "l2": "inputs larger than L2 (A = %.2f GB)" % (n * n * 8 / 1e9),
                        "parallelism": "replicas" if world > 1 else "single"},
-            "backward_error": be_plain,
-            "plain_fp64": {"value": plain_sps, "unit": "solves/s", "ms_per_step": ms_plain / args.steps,
-                           "backward_error": be_plain},
-            "gflops": flops_solve(n, m) * value / 1e9,
+            "backward_error": max(r["backward_error"] for r in timed_reports),
+            "refinement": {"iterations": rep["iterations"], "backward_error0": rep["backward_error0"],
+                           "fell_back": sum(r["fell_back"] for r in timed_reports),
+                           "ms_factor": rep["ms_factor"], "ms_refine": rep["ms_refine"],
+                           "forward_error_vs_fp64": fwd_vs_fp64},
+            "plain_fp64": {"value": plain_sps, "unit": "solves/s", "steps": k_plain,
+                           "ms_per_step": ms_plain / k_plain, "backward_error": be_plain,
+                           "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof_plain.items()}},
+            "mixed_over_plain": mixed_sps / plain_sps,
+            "gflops": flops_solve(n, m) * mixed_sps / 1e9,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": launches,
-            "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
+            "kernels": {k: {"ms": v[0], "launches": v[1], "work": v[2]} for k, v in prof.items()},
         }
         print(json.dumps(out))
     if dist:

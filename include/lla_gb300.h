@@ -204,6 +204,61 @@ int lla_dtrsm_device_noalloc(const double *dL, int64_t n, int64_t ld, int trans,
                              int64_t m, int64_t ldb, int algo, void *stream, lla_error *err);
 
 
+/* ---- mixed-precision refined solve (no counterpart in the reference) -----
+ * Solves A X = B for SPD A (only its lower triangle is read, as in the
+ * reference) by a low-precision Cholesky of the symmetrically equilibrated
+ * matrix (exact power-of-two scaling), FP64 iterative refinement to a normwise
+ * backward error max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf +
+ * ||b_j||_inf) <= tol, and a fallback to the plain FP64 factorisation when the
+ * low-precision factorisation breaks down or the refinement stalls.  The FP64
+ * fallback decides NotPositiveDefinite. */
+enum lla_update {
+    LLA_UPDATE_FP32 = 0,    /* FP32 SIMT trailing updates */
+    LLA_UPDATE_BF16 = 1,    /* tcgen05: one BF16 term per operand, FP32 accumulation */
+    LLA_UPDATE_BF16X3 = 3,  /* tcgen05: hi/lo BF16 split, three products */
+    LLA_UPDATE_BF16X6 = 6,  /* tcgen05: three-level BF16 split, six products */
+    LLA_UPDATE_FP16 = 11,   /* tcgen05: one FP16 term */
+    LLA_UPDATE_FP16X3 = 13  /* tcgen05: hi/lo FP16 split, three products */
+};
+
+typedef struct lla_refine_opts {
+    int32_t update;      /* lla_update (default LLA_UPDATE_FP16X3) */
+    int32_t max_iters;   /* refinement iterations before giving up (default 30) */
+    double tol;          /* target normwise backward error (default 1e-13) */
+    int32_t equilibrate; /* 1: symmetric power-of-two scaling (default) */
+    int32_t fallback;    /* 1: plain FP64 on breakdown or stall (default); 0: LLA_ERR_NOT_CONVERGED */
+    int32_t nb;          /* panel width (0: default) */
+    int32_t reserved[3];
+} lla_refine_opts;
+
+typedef struct lla_refine_report {
+    int32_t update;          /* update form used */
+    int32_t iterations;      /* residual evaluations */
+    int32_t converged;       /* 1 when the refinement reached tol */
+    int32_t fell_back;       /* 1 when the plain FP64 path produced X */
+    int32_t factor_failed;   /* 1 when the low-precision factorisation broke down */
+    int32_t reserved;
+    double backward_error;   /* final normwise backward error (max over columns) */
+    double backward_error0;  /* after the first low-precision solve */
+    double ms_factor, ms_refine, ms_fallback, ms_total;
+} lla_refine_report;
+
+void lla_refine_opts_default(lla_refine_opts *opts);
+
+/* Device-resident form: dA (n x n, column-major, lda), dB (n x m, ldb) are
+ * read; dX (n x m, ldx) receives X.  Synchronous on `stream` (the refinement
+ * reads the backward error on the host every iteration). */
+int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda, const double *dB, int64_t m,
+                             int64_t ldb, double *dX, int64_t ldx, const lla_refine_opts *opts,
+                             lla_refine_report *report, void *stream, lla_error *err);
+
+/* Host-view form (SolveC-like): `a` is read only; `b` (n x m) is overwritten
+ * with X.  Errors: NotSquare(a), WrongRows(b), NotPositiveDefinite (decided by
+ * the FP64 fallback). */
+int lla_dposv_refined(const double *a, int64_t rows, int64_t cols, int64_t rs, int64_t cs,
+                      double *b, int64_t brows, int64_t bcols, int64_t brs, int64_t bcs,
+                      const lla_refine_opts *opts, lla_refine_report *report, lla_error *err);
+
 /* ---- diagnostics (no counterpart in the reference) ----------------------
  * Launch accounting and per-kernel CUDA-event timing used by the benchmark:
  * while profiling is on, every kernel launch is bracketed by an event pair on

@@ -63,6 +63,27 @@ class Error(ctypes.Structure):
                 ("index", ctypes.c_int64)]
 
 
+class RefineOpts(ctypes.Structure):
+    _fields_ = [("update", ctypes.c_int32), ("max_iters", ctypes.c_int32), ("tol", ctypes.c_double),
+                ("equilibrate", ctypes.c_int32), ("fallback", ctypes.c_int32), ("nb", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 3)]
+
+
+class RefineReport(ctypes.Structure):
+    _fields_ = [("update", ctypes.c_int32), ("iterations", ctypes.c_int32),
+                ("converged", ctypes.c_int32), ("fell_back", ctypes.c_int32),
+                ("factor_failed", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("backward_error", ctypes.c_double), ("backward_error0", ctypes.c_double),
+                ("ms_factor", ctypes.c_double), ("ms_refine", ctypes.c_double),
+                ("ms_fallback", ctypes.c_double), ("ms_total", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+UPDATE_FP32, UPDATE_BF16, UPDATE_BF16X3, UPDATE_BF16X6, UPDATE_FP16, UPDATE_FP16X3 = 0, 1, 3, 6, 11, 13
+UPDATE_NAMES = {"fp32": 0, "bf16": 1, "bf16x3": 3, "bf16x6": 6, "fp16": 11, "fp16x3": 13}
+
 _V = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64]
 _E = ctypes.POINTER(Error)
 
@@ -80,6 +101,13 @@ EXPORTS = {
                           ctypes.c_int),
     "lla_profile_kernel_name": ([ctypes.c_int], ctypes.c_char_p),
     "lla_measure_peak_tflops": ([ctypes.c_int], ctypes.c_double),
+    "lla_refine_opts_default": ([ctypes.POINTER(RefineOpts)], None),
+    "lla_dposv_refined_device": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+                                  ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                  ctypes.POINTER(RefineOpts), ctypes.POINTER(RefineReport),
+                                  ctypes.c_void_p, _E], ctypes.c_int),
+    "lla_dposv_refined": (_V + _V + [ctypes.POINTER(RefineOpts), ctypes.POINTER(RefineReport), _E],
+                          ctypes.c_int),
 }
 for _p in "ds":
     EXPORTS.update({
@@ -391,3 +419,41 @@ def trsm_device(L, B, trans, algo=ALGO_FAST, stream=None):
                                         ctypes.byref(e))
     _raise(e)
     return B
+
+
+# ---- mixed-precision refined solve (no counterpart in the reference) --------
+
+def refine_opts(update="fp16x3", max_iters=30, tol=1e-13, equilibrate=True, fallback=True, nb=0):
+    o = RefineOpts()
+    lib.lla_refine_opts_default(ctypes.byref(o))
+    o.update = UPDATE_NAMES[update] if isinstance(update, str) else int(update)
+    o.max_iters, o.tol = max_iters, tol
+    o.equilibrate, o.fallback, o.nb = int(bool(equilibrate)), int(bool(fallback)), nb
+    return o
+
+
+def posv_refined(a, b, **kw):
+    """Solves A X = B (host numpy views; `a` read only, `b` overwritten with X)
+    by the low-precision factorisation plus FP64 refinement; returns the report."""
+    _writable(b)
+    if a.dtype != np.float64 or b.dtype != np.float64:
+        raise TypeError("the refined solve is f64")
+    o, r, e = refine_opts(**kw), RefineReport(), Error()
+    lib.lla_dposv_refined(*_view(a), *_view(b), ctypes.byref(o), ctypes.byref(r), ctypes.byref(e))
+    _raise(e)
+    return r.as_dict()
+
+
+def posv_refined_device(A, B, X, stream=None, **kw):
+    """Device form on column-major CUDA tensors (stride(0) == 1): A (n x n),
+    B (n x m) read, X (n x m) written.  Returns the report."""
+    n, m = A.shape[0], B.shape[1]
+    assert A.stride(0) == 1 and B.stride(0) == 1 and X.stride(0) == 1
+    o, r, e = refine_opts(**kw), RefineReport(), Error()
+    lib.lla_dposv_refined_device(ctypes.c_void_p(A.data_ptr()), n, max(1, A.stride(1)),
+                                 ctypes.c_void_p(B.data_ptr()), m, max(1, B.stride(1)),
+                                 ctypes.c_void_p(X.data_ptr()), max(1, X.stride(1)),
+                                 ctypes.byref(o), ctypes.byref(r), _stream_ptr(stream),
+                                 ctypes.byref(e))
+    _raise(e)
+    return r.as_dict()

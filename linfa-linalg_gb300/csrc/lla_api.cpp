@@ -622,6 +622,46 @@ int is_triangular_impl(const T *a, int64_t rows, int64_t cols, int64_t rs, int64
 
 }  // namespace
 
+// ---- mixed-precision refined solve on host views ---------------------------
+
+int lla_dposv_refined(const double *a, int64_t rows, int64_t cols, int64_t rs, int64_t cs, double *b,
+                      int64_t brows, int64_t bcols, int64_t brs, int64_t bcs,
+                      const lla_refine_opts *opts, lla_refine_report *report, lla_error *err) {
+    if (bad_view(a, rows, cols) || bad_view(b, brows, bcols))
+        return lla__set_status(err, LLA_ERR_INVALID_ARG);
+    if (rows != cols) return not_square(err, rows, cols);
+    const int64_t n = rows;
+    if (brows != n) return wrong_rows(err, n, brows);
+    lla__set_status(err, LLA_OK);
+    if (n == 0 || bcols == 0) {
+        return lla_dposv_refined_device(nullptr, 0, 1, nullptr, 0, 1, nullptr, 1, opts, report,
+                                        nullptr, err);
+    }
+    Ctx *c = get_ctx(err);
+    if (!c) return err ? err->code : LLA_ERR_NO_DEVICE;
+    View va{(char *)a, rows, cols, rs, cs, sizeof(double)};
+    int64_t ars, acs;
+    LLA_TRY_CUDA(upload(*c, va, c->raw_a, c->stage_a, ars, acs));
+    LLA_TRY_CUDA(c->work_a.ensure(sizeof(double) * n * n));
+    double *W = (double *)c->work_a.p;
+    LLA_TRY_CUDA(launch_status(
+        import_launch<double>((const double *)c->raw_a.p, ars, acs, n, n, W, n, c->stream)));
+    View vb{(char *)b, brows, bcols, brs, bcs, sizeof(double)};
+    int64_t drs, dcs;
+    LLA_TRY_CUDA(upload(*c, vb, c->raw_b, c->stage_b, drs, dcs));
+    LLA_TRY_CUDA(c->work_b.ensure(sizeof(double) * n * bcols));
+    LLA_TRY_CUDA(c->aux_x.ensure(sizeof(double) * n * bcols));
+    double *WB = (double *)c->work_b.p, *X = (double *)c->aux_x.p;
+    LLA_TRY_CUDA(launch_status(import_launch<double>((const double *)c->raw_b.p, drs, dcs, n, bcols,
+                                                     WB, n, c->stream)));
+    const int st = lla_dposv_refined_device(W, n, n, WB, bcols, n, X, n, opts, report, c->stream, err);
+    if (st != LLA_OK) return st;
+    LLA_TRY_CUDA(launch_status(export_launch<double>(X, n, (double *)c->raw_b.p, drs, dcs, n, bcols,
+                                                     EXPORT_FULL, -1, c->stream)));
+    LLA_TRY_CUDA(download(*c, vb, c->raw_b, c->stage_b));
+    return LLA_OK;
+}
+
 // ---- device-resident entry points -----------------------------------------
 
 template <typename T>

@@ -25,9 +25,19 @@ struct HostBuf {
     ~HostBuf();
 };
 
+// Workspace of the mixed-precision refined solve.
+struct MixedWs {
+    DevBuf L, s, rowsum, R, Y, diag0, words;  // FP32 factor, scaling, norms, residual, correction
+    DevBuf F, fdiag;                          // plain FP64 fallback
+    DevBuf opA, opB;                          // tensor-core operand planes of one panel
+    DevBuf maps;                              // TMA descriptors
+    HostBuf words_host;
+};
+
 // One per calling host thread: its own stream and buffers, so concurrent
 // callers never share scratch memory.
 struct Ctx {
+    MixedWs mixed;
     int device = 0;
     cudaStream_t stream = nullptr;
     DevBuf small_dev;                 // status words
@@ -35,6 +45,7 @@ struct Ctx {
     DevBuf raw_a, raw_b;              // host views as uploaded
     DevBuf work_a, work_b;            // column-major working copies
     DevBuf aux_s, aux_d, aux_diag;    // factor scratch (EXACT S/D, FAST diag0), diag override
+    DevBuf aux_x;                     // solution of the refined solve
     DevBuf ws;                        // triangular-solve tickets and flags
     DevBuf dev_s, dev_d, dev_ws;      // scratch of the device-resident entry points
     HostBuf stage_a, stage_b;         // pinned staging for strided views

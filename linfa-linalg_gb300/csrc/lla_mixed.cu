@@ -1,0 +1,507 @@
+// lla_mixed.cu -- mixed-precision SPD solve with FP64 iterative refinement.
+//
+//   1. Equilibrate symmetrically with exact powers of two: A^ = S A S,
+//      s_i = 2^-floor(log2(a_ii)/2), so diag(A^) lies in [1, 4) and every
+//      entry of A^ is exact in FP64.  (Only the lower triangle of A is read,
+//      as in the reference; the solved matrix is the symmetric matrix it
+//      defines.)
+//   2. Factor A^ ~= L L^T in low precision: FP32 diagonal blocks and panels,
+//      trailing updates on the tensor cores (BF16 or FP16 operand terms with
+//      FP32 accumulation, lla_tc_update.cu) or in FP32 SIMT.
+//   3. Refine in FP64: r = b - A x (FP64 tensor pipe), d = S L^-T L^-1 S r in
+//      FP32, x += d (FP64), until the normwise backward error
+//      max_j ||r_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf) <= tol.
+//   4. On a low-precision breakdown (non-positive pivot) or a stall, fall back
+//      to the plain FP64 factorisation, whose verdict (NotPositiveDefinite)
+//      stands.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "lla_api_internal.h"
+#include "lla_common.cuh"
+#include "lla_kernels.h"
+#include "lla_mixed.h"
+#include "lla_prof.h"
+
+namespace lla {
+
+__device__ __forceinline__ void atomic_max_nonneg(double *addr, double v) {
+    // non-negative doubles order like their bit patterns; NaN/inf map to the top
+    if (!(v >= 0.0)) v = __longlong_as_double(0x7ff0000000000000ll);  // NaN -> +inf
+    atomicMax((unsigned long long *)addr, (unsigned long long)__double_as_longlong(v));
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// s_i = 2^-floor(log2(a_ii)/2); a non-positive or non-finite diagonal marks
+// the matrix as not factorable in low precision (the FP64 path decides).
+__global__ void equil_scale_kernel(const double *A, int64_t lda, int64_t n, int scale, double *s,
+                                   int *bad) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double a = A[i + i * lda];
+    if (!(a > 0.0) || !isfinite(a)) {
+        s[i] = 1.0;
+        atomicExch(bad, 1);
+        return;
+    }
+    if (!scale) {
+        s[i] = 1.0;
+        return;
+    }
+    const int e = ilogb(a);
+    s[i] = ldexp(1.0, -(e >= 0 ? e / 2 : -((-e + 1) / 2)));
+}
+
+// W[i,j] = fp32(s_i a_ij s_j) for the lower triangle (i >= j), column-major.
+__global__ void equil_convert_kernel(const double *__restrict__ A, int64_t lda, int64_t n,
+                                     const double *__restrict__ s, float *W, int64_t ldw) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t j = blockIdx.y;
+    if (i >= n) return;
+    for (int64_t jj = j; jj < n; jj += gridDim.y)
+        if (i >= jj) W[i + jj * ldw] = (float)(s[i] * A[i + jj * lda] * s[jj]);
+}
+
+// Row sums of |A_sym| (A_sym from the lower triangle): one block per 32-column
+// strip; each element (i, k), i >= k, adds |a_ik| to row i and, off the
+// diagonal, to row k.
+__global__ void sym_rowsum_kernel(const double *__restrict__ A, int64_t lda, int64_t n,
+                                  double *rowsum) {
+    __shared__ double colacc[32];
+    const int64_t k0 = (int64_t)blockIdx.x * 32;
+    if (threadIdx.x < 32) colacc[threadIdx.x] = 0.0;
+    __syncthreads();
+    for (int64_t i = k0 + threadIdx.x; i < n; i += blockDim.x) {
+        double racc = 0.0;
+        for (int c = 0; c < 32; ++c) {
+            const int64_t k = k0 + c;
+            if (k >= n || k > i) break;
+            const double v = fabs(A[i + k * lda]);
+            racc += v;
+            if (k != i) atomicAdd(&colacc[c], v);
+        }
+        atomicAdd(&rowsum[i], racc);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32 && k0 + threadIdx.x < n) atomicAdd(&rowsum[k0 + threadIdx.x], colacc[threadIdx.x]);
+}
+
+__global__ void max_reduce_kernel(const double *v, int64_t n, double *out) {
+    double m = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = fmax(m, fabs(v[i]));
+    m = warp_max(m);
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(out, m);
+}
+
+// colmax[j] = max_i |M[i, j]|  (n x m column-major, leading dim ld)
+__global__ void colmax_kernel(const double *M, int64_t ld, int64_t n, int64_t m, double *colmax) {
+    const int64_t j = blockIdx.y;
+    double v = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v = fmax(v, fabs(M[i + j * ld]));
+    v = warp_max(v);
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&colmax[j], v);
+}
+
+// Y = fp32(s .* R)   (n x m, column-major; ld of Y = n)
+__global__ void scale_to_f32_kernel(const double *R, int64_t ldr, const double *s, int64_t n,
+                                    int64_t m, float *Y) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t j = blockIdx.y;
+    if (i < n && j < m) Y[i + j * n] = (float)(s[i] * R[i + j * ldr]);
+}
+
+// X += s .* Y (FP64), and colmax_x[j] = max_i |X[i,j]|
+__global__ void update_x_kernel(double *X, int64_t ldx, const double *s, const float *Y, int64_t n,
+                                int64_t m, double *colmax_x) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t j = blockIdx.y;
+    double v = 0.0;
+    if (i < n && j < m) {
+        const double x = X[i + j * ldx] + s[i] * (double)Y[i + j * n];
+        X[i + j * ldx] = x;
+        v = fabs(x);
+    }
+    v = warp_max(v);
+    if ((threadIdx.x & 31) == 0 && j < m) atomic_max_nonneg(&colmax_x[j], v);
+}
+
+// R = B - A_sym X on the FP64 tensor pipe (mma.sync m16n8k16 .f64).
+// CTA tile: 32 rows x 64 RHS columns, K chunks of 32; four warps, each 16 x 32
+// (four m16n8 MMAs per k16 step).  A_sym(i,k) reads the lower triangle:
+// A[i + k*lda] for k <= i, A[k + i*lda] otherwise.  Also colmax_r.
+constexpr int kResRows = 32, kResCols = 64, kResK = 32;
+
+__global__ void __launch_bounds__(128) residual_dmma_kernel(const double *__restrict__ A, int64_t lda,
+                                                            int64_t n, const double *__restrict__ X,
+                                                            int64_t ldx, const double *__restrict__ B,
+                                                            int64_t ldb, double *R, int64_t ldr,
+                                                            int64_t m, double *colmax_r) {
+    __shared__ double As[kResK][kResRows + 4];  // [k][row], stride 36 = 4 (mod 16)
+    __shared__ double Xs[kResK][kResCols + 4];  // [k][col], stride 68 = 4 (mod 16)
+    const int64_t i0 = (int64_t)blockIdx.x * kResRows;
+    const int64_t c0 = (int64_t)blockIdx.y * kResCols;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int g = lane >> 2, t = lane & 3;
+    const int wr = (warp & 1) * 16, wc = (warp >> 1) * 32;
+    double acc[4][4];
+#pragma unroll
+    for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[ni][q] = 0.0;
+    for (int64_t k0 = 0; k0 < n; k0 += kResK) {
+        const bool upper = k0 > i0 + kResRows - 1;  // whole tile above the diagonal
+        for (int e = tid; e < kResRows * kResK; e += 128) {
+            int r, c;
+            if (upper) {
+                r = e / kResK;
+                c = e % kResK;  // consecutive e -> consecutive k -> A[k + i*lda]
+            } else {
+                r = e % kResRows;
+                c = e / kResRows;  // consecutive e -> consecutive i -> A[i + k*lda]
+            }
+            const int64_t i = i0 + r, k = k0 + c;
+            double v = 0.0;
+            if (i < n && k < n) v = (k <= i) ? A[i + k * lda] : A[k + i * lda];
+            As[c][r] = v;
+        }
+        for (int e = tid; e < kResK * kResCols; e += 128) {
+            const int kk = e % kResK, cc = e / kResK;  // consecutive e -> consecutive k in column cc
+            const int64_t k = k0 + kk, col = c0 + cc;
+            Xs[kk][cc] = (k < n && col < m) ? X[k + col * ldx] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < kResK; kk += 16) {
+            double af[8], bf[4][4];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) af[q] = As[kk + t + 4 * (q >> 1)][wr + g + 8 * (q & 1)];
+#pragma unroll
+            for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) bf[ni][q] = Xs[kk + t + 4 * q][wc + ni * 8 + g];
+#pragma unroll
+            for (int ni = 0; ni < 4; ++ni)
+                asm volatile(
+                    "mma.sync.aligned.m16n8k16.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, "
+                    "{%4,%5,%6,%7,%8,%9,%10,%11}, {%12,%13,%14,%15}, {%0,%1,%2,%3};\n"
+                    : "+d"(acc[ni][0]), "+d"(acc[ni][1]), "+d"(acc[ni][2]), "+d"(acc[ni][3])
+                    : "d"(af[0]), "d"(af[1]), "d"(af[2]), "d"(af[3]), "d"(af[4]), "d"(af[5]),
+                      "d"(af[6]), "d"(af[7]), "d"(bf[ni][0]), "d"(bf[ni][1]), "d"(bf[ni][2]),
+                      "d"(bf[ni][3]));
+        }
+        __syncthreads();
+    }
+    // epilogue: R = B - acc, and column maxima of |R|
+#pragma unroll
+    for (int ni = 0; ni < 4; ++ni) {
+        double cm2[2] = {0.0, 0.0};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int64_t i = i0 + wr + g + 8 * (q >> 1);
+            const int64_t col = c0 + wc + ni * 8 + 2 * t + (q & 1);
+            if (i < n && col < m) {
+                const double r = B[i + col * ldb] - acc[ni][q];
+                R[i + col * ldr] = r;
+                cm2[q & 1] = fmax(cm2[q & 1], fabs(r));
+            }
+        }
+        // reduce over the 8 row groups g sharing a column (lanes with equal t)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            double v = cm2[h];
+            v = fmax(v, __shfl_xor_sync(0xffffffffu, v, 4));
+            v = fmax(v, __shfl_xor_sync(0xffffffffu, v, 8));
+            v = fmax(v, __shfl_xor_sync(0xffffffffu, v, 16));
+            const int64_t col = c0 + wc + ni * 8 + 2 * t + h;
+            if (g == 0 && col < m) atomic_max_nonneg(&colmax_r[col], v);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launch helpers
+
+static unsigned gx(int64_t n, int b) { return (unsigned)ceil_div(n, b); }
+
+int equilibrate_launch(const double *A, int64_t lda, int64_t n, bool scale, double *s, float *W,
+                       int64_t ldw, double *rowsum, double *anorm, int *bad, cudaStream_t st) {
+    {
+        LaunchScope ls(K_MIXED_CONVERT, st, 8.0 * n);
+        equil_scale_kernel<<<gx(n, 256), 256, 0, st>>>(A, lda, n, scale ? 1 : 0, s, bad);
+    }
+    {
+        LaunchScope ls(K_MIXED_CONVERT, st, 6.0 * n * (n + 1) / 2);
+        equil_convert_kernel<<<dim3(gx(n, 256), (unsigned)std::min<int64_t>(n, 4096)), 256, 0, st>>>(
+            A, lda, n, s, W, ldw);
+    }
+    if (cudaMemsetAsync(rowsum, 0, sizeof(double) * n, st) != cudaSuccess) return -1;
+    {
+        LaunchScope ls(K_MISC, st, 8.0 * n * (n + 1) / 2);
+        sym_rowsum_kernel<<<gx(n, 32), 256, 0, st>>>(A, lda, n, rowsum);
+    }
+    {
+        LaunchScope ls(K_MISC, st);
+        max_reduce_kernel<<<std::min<unsigned>(gx(n, 256), 1024), 256, 0, st>>>(rowsum, n, anorm);
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int colmax_launch(const double *M, int64_t ld, int64_t n, int64_t m, double *colmax, cudaStream_t st) {
+    LaunchScope ls(K_MISC, st);
+    colmax_kernel<<<dim3(std::min<unsigned>(gx(n, 256), 64), (unsigned)m), 256, 0, st>>>(M, ld, n, m,
+                                                                                        colmax);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int scale_to_f32_launch(const double *R, int64_t ldr, const double *s, int64_t n, int64_t m, float *Y,
+                        cudaStream_t st) {
+    LaunchScope ls(K_REFINE, st, 12.0 * n * m);
+    scale_to_f32_kernel<<<dim3(gx(n, 256), (unsigned)m), 256, 0, st>>>(R, ldr, s, n, m, Y);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int update_x_launch(double *X, int64_t ldx, const double *s, const float *Y, int64_t n, int64_t m,
+                    double *colmax_x, cudaStream_t st) {
+    LaunchScope ls(K_REFINE, st, 20.0 * n * m);
+    update_x_kernel<<<dim3(gx(n, 256), (unsigned)m), 256, 0, st>>>(X, ldx, s, Y, n, m, colmax_x);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int residual_launch(const double *A, int64_t lda, int64_t n, const double *X, int64_t ldx,
+                    const double *B, int64_t ldb, double *R, int64_t ldr, int64_t m, double *colmax_r,
+                    cudaStream_t st) {
+    // algorithmic work: 2 n^2 m flops
+    LaunchScope ls(K_RESIDUAL, st, 2.0 * n * n * m);
+    residual_dmma_kernel<<<dim3(gx(n, kResRows), gx(m, kResCols)), 128, 0, st>>>(
+        A, lda, n, X, ldx, B, ldb, R, ldr, m, colmax_r);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace lla
+
+// ---------------------------------------------------------------------------
+// host driver
+
+using namespace lla;
+
+namespace {
+
+cudaError_t last_err(int rc) {
+    if (rc == 0) return cudaSuccess;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? cudaErrorUnknown : e;
+}
+
+double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+extern "C" void lla_refine_opts_default(lla_refine_opts *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->update = LLA_UPDATE_FP16X3;
+    o->max_iters = 30;
+    o->tol = 1e-13;
+    o->equilibrate = 1;
+    o->fallback = 1;
+    o->nb = 0;
+}
+
+#define MX_TRY(expr)                                                \
+    do {                                                            \
+        cudaError_t e__ = (expr);                                   \
+        if (e__ != cudaSuccess) return lla__set_cuda_error(err, e__); \
+    } while (0)
+
+extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda, const double *dB,
+                                        int64_t m, int64_t ldb, double *dX, int64_t ldx,
+                                        const lla_refine_opts *opts_in, lla_refine_report *rep,
+                                        void *stream, lla_error *err) {
+    auto t_start = std::chrono::steady_clock::now();
+    if (n < 0 || m < 0 || lda < std::max<int64_t>(1, n) || ldb < std::max<int64_t>(1, n) ||
+        ldx < std::max<int64_t>(1, n) || (n > 0 && (!dA || (m > 0 && (!dB || !dX)))))
+        return lla__set_status(err, LLA_ERR_INVALID_ARG);
+    lla_refine_opts opts;
+    if (opts_in)
+        opts = *opts_in;
+    else
+        lla_refine_opts_default(&opts);
+    if (opts.max_iters <= 0) opts.max_iters = 30;
+    if (!(opts.tol > 0)) opts.tol = 1e-13;
+    lla_refine_report r;
+    std::memset(&r, 0, sizeof(r));
+    r.update = opts.update;
+    lla__set_status(err, LLA_OK);
+    if (n == 0 || m == 0) {
+        r.converged = 1;
+        if (rep) *rep = r;
+        return LLA_OK;
+    }
+    Ctx *c = get_ctx(err);
+    if (!c) return err ? err->code : LLA_ERR_NO_DEVICE;
+    cudaStream_t st = (cudaStream_t)stream;
+    MixedWs &w = c->mixed;
+    // workspace
+    MX_TRY(w.L.ensure(sizeof(float) * n * n));
+    MX_TRY(w.s.ensure(sizeof(double) * n));
+    MX_TRY(w.rowsum.ensure(sizeof(double) * n));
+    MX_TRY(w.R.ensure(sizeof(double) * n * m));
+    MX_TRY(w.Y.ensure(sizeof(float) * n * m));
+    MX_TRY(w.diag0.ensure(sizeof(float) * n));
+    MX_TRY(w.words.ensure(sizeof(double) * (8 + 3 * m)));
+    MX_TRY(c->ws.ensure(sizeof(int) * (trsm_ws_ints(n, m) + 1)));
+    MX_TRY(w.words_host.ensure(sizeof(double) * (8 + 3 * m)));
+    float *L = (float *)w.L.p;
+    double *s = (double *)w.s.p;
+    double *R = (double *)w.R.p;
+    float *Y = (float *)w.Y.p;
+    // words: [0] anorm, [1] min_ratio, [2] int64 info, [3] int bad | int err_word,
+    //        [8 ..) colmax_r[m], colmax_x[m], colmax_b[m]
+    double *words = (double *)w.words.p;
+    double *anorm = words + 0;
+    double *min_ratio = words + 1;
+    int64_t *info = (int64_t *)(words + 2);
+    int *bad = (int *)(words + 3);
+    int *err_word = bad + 1;
+    double *colmax_r = words + 8, *colmax_x = colmax_r + m, *colmax_b = colmax_x + m;
+    int *tws = (int *)c->ws.p;
+    double *hw = (double *)w.words_host.p;
+
+    auto read_words = [&](size_t count) -> cudaError_t {
+        cudaError_t e = cudaMemcpyAsync(hw, words, sizeof(double) * count, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        return e;
+    };
+    {
+        double init[8] = {0.0, 1e300, 0.0, 0.0, 0, 0, 0, 0};
+        int64_t minus1 = -1;
+        std::memcpy(&init[2], &minus1, sizeof(int64_t));
+        std::memcpy(hw, init, sizeof(init));
+        MX_TRY(cudaMemcpyAsync(words, hw, sizeof(init), cudaMemcpyHostToDevice, st));
+        MX_TRY(cudaMemsetAsync(colmax_r, 0, sizeof(double) * 3 * m, st));
+    }
+    // 1. equilibrate (and ||A||_inf, ||b_j||_inf)
+    auto t0 = std::chrono::steady_clock::now();
+    MX_TRY(last_err(equilibrate_launch(dA, lda, n, opts.equilibrate != 0, s, L, n,
+                                       (double *)w.rowsum.p, anorm, bad, st)));
+    MX_TRY(last_err(colmax_launch(dB, ldb, n, m, colmax_b, st)));
+    // 2. low-precision factorisation
+    bool lowp_ok = true;
+    MX_TRY(read_words(4));
+    if (((int *)(hw + 3))[0] != 0) lowp_ok = false;
+    if (lowp_ok) {
+        int rc = lowp_factor_launch(L, n, n, opts, info, (float *)w.diag0.p, min_ratio, c, st);
+        MX_TRY(last_err(rc));
+        MX_TRY(read_words(4));
+        int64_t finfo;
+        std::memcpy(&finfo, hw + 2, sizeof(int64_t));
+        if (finfo >= 0) lowp_ok = false;
+    }
+    r.ms_factor = ms_since(t0);
+    r.factor_failed = lowp_ok ? 0 : 1;
+    // 3. refinement
+    t0 = std::chrono::steady_clock::now();
+    double eta = INFINITY, eta_prev = INFINITY;
+    bool converged = false;
+    if (lowp_ok) {
+        for (int64_t j = 0; j < m; ++j)
+            MX_TRY(cudaMemsetAsync(dX + j * ldx, 0, sizeof(double) * n, st));
+        const double *rhs = dB;
+        int64_t ldrhs = ldb;
+        for (int it = 1; it <= opts.max_iters; ++it) {
+            // correction d = S L^-T L^-1 S r  (FP32), x += d
+            MX_TRY(last_err(scale_to_f32_launch(rhs, ldrhs, s, n, m, Y, st)));
+            MX_TRY(cudaMemsetAsync(err_word, 0, sizeof(int), st));
+            MX_TRY(last_err(trsm_launch<float>(L, n, n, 1, 0, nullptr, Y, n, m, false, tws, err_word, st)));
+            MX_TRY(last_err(trsm_launch<float>(L, n, n, 0, 1, nullptr, Y, n, m, false, tws, err_word, st)));
+            MX_TRY(cudaMemsetAsync(colmax_r, 0, sizeof(double) * 2 * m, st));
+            MX_TRY(last_err(update_x_launch(dX, ldx, s, Y, n, m, colmax_x, st)));
+            // r = b - A x  (FP64)
+            MX_TRY(last_err(residual_launch(dA, lda, n, dX, ldx, dB, ldb, R, n, m, colmax_r, st)));
+            rhs = R;
+            ldrhs = n;
+            MX_TRY(read_words(8 + 3 * m));
+            if (((int *)(hw + 3))[1] != 0) return lla__set_status(err, LLA_ERR_TIMEOUT);
+            const double an = hw[0];
+            double e = 0.0;
+            for (int64_t j = 0; j < m; ++j) {
+                const double den = an * hw[8 + m + j] + hw[8 + 2 * m + j];
+                const double ej = den > 0 ? hw[8 + j] / den : (hw[8 + j] > 0 ? INFINITY : 0.0);
+                e = std::isnan(ej) ? INFINITY : std::max(e, ej);
+            }
+            eta = e;
+            r.iterations = it;
+            if (it == 1) r.backward_error0 = eta;
+            if (eta <= opts.tol) {
+                converged = true;
+                break;
+            }
+            // stall: no halving of the backward error over an iteration (after two)
+            if (!std::isfinite(eta) || (it >= 3 && eta > 0.5 * eta_prev)) break;
+            eta_prev = eta;
+        }
+    }
+    r.ms_refine = ms_since(t0);
+    r.backward_error = eta;
+    r.converged = converged ? 1 : 0;
+    if (!converged) {
+        if (!opts.fallback) {
+            if (rep) *rep = r;
+            return lla__set_status(err, LLA_ERR_NOT_CONVERGED);
+        }
+        // 4. plain FP64 fallback
+        t0 = std::chrono::steady_clock::now();
+        r.fell_back = 1;
+        MX_TRY(w.F.ensure(sizeof(double) * n * n));
+        MX_TRY(w.fdiag.ensure(sizeof(double) * n));
+        double *F = (double *)w.F.p;
+        MX_TRY(cudaMemcpy2DAsync(F, sizeof(double) * n, dA, sizeof(double) * lda, sizeof(double) * n, n,
+                                 cudaMemcpyDeviceToDevice, st));
+        int64_t minus1 = -1;
+        MX_TRY(cudaMemcpyAsync(info, &minus1, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        MX_TRY(last_err(potrf_fast_launch<double>(F, n, n, info, (double *)w.fdiag.p, nullptr, st)));
+        MX_TRY(read_words(4));
+        int64_t finfo;
+        std::memcpy(&finfo, hw + 2, sizeof(int64_t));
+        if (finfo >= 0) {
+            r.ms_fallback = ms_since(t0);
+            if (rep) *rep = r;
+            lla__set_status(err, LLA_NOT_POSITIVE_DEFINITE);
+            if (err) err->index = finfo;
+            return LLA_NOT_POSITIVE_DEFINITE;
+        }
+        MX_TRY(cudaMemcpy2DAsync(dX, sizeof(double) * ldx, dB, sizeof(double) * ldb, sizeof(double) * n,
+                                 m, cudaMemcpyDeviceToDevice, st));
+        MX_TRY(cudaMemsetAsync(err_word, 0, sizeof(int), st));
+        MX_TRY(last_err(trsm_launch<double>(F, n, n, 1, 0, nullptr, dX, ldx, m, false, tws, err_word, st)));
+        MX_TRY(last_err(trsm_launch<double>(F, n, n, 0, 1, nullptr, dX, ldx, m, false, tws, err_word, st)));
+        MX_TRY(cudaMemsetAsync(colmax_r, 0, sizeof(double) * 2 * m, st));
+        MX_TRY(last_err(colmax_launch(dX, ldx, n, m, colmax_x, st)));
+        MX_TRY(last_err(residual_launch(dA, lda, n, dX, ldx, dB, ldb, R, n, m, colmax_r, st)));
+        MX_TRY(read_words(8 + 3 * m));
+        double e = 0.0;
+        for (int64_t j = 0; j < m; ++j) {
+            const double den = hw[0] * hw[8 + m + j] + hw[8 + 2 * m + j];
+            e = std::max(e, den > 0 ? hw[8 + j] / den : 0.0);
+        }
+        r.backward_error = e;
+        r.ms_fallback = ms_since(t0);
+    }
+    r.ms_total = ms_since(t_start);
+    if (rep) *rep = r;
+    return LLA_OK;
+}

@@ -1,0 +1,26 @@
+// lla_mixed.h -- internal declarations of the mixed-precision path.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/lla_gb300.h"
+
+namespace lla {
+
+struct Ctx;
+
+// Low-precision Cholesky of the equilibrated FP32 matrix L (lower triangle,
+// column-major, ld) in place, with the trailing-update form opts.update.
+// *info (device) receives the first non-positive pivot's row or stays -1.
+int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &opts, int64_t *info,
+                       float *diag0, double *min_ratio, Ctx *c, cudaStream_t st);
+
+int equilibrate_launch(const double *A, int64_t lda, int64_t n, bool scale, double *s, float *W,
+                       int64_t ldw, double *rowsum, double *anorm, int *bad, cudaStream_t st);
+int colmax_launch(const double *M, int64_t ld, int64_t n, int64_t m, double *colmax, cudaStream_t st);
+int residual_launch(const double *A, int64_t lda, int64_t n, const double *X, int64_t ldx,
+                    const double *B, int64_t ldb, double *R, int64_t ldr, int64_t m, double *colmax_r,
+                    cudaStream_t st);
+
+}  // namespace lla

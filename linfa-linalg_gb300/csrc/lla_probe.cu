@@ -11,29 +11,40 @@ namespace {
 
 constexpr int kIters = 2048;
 
+// Eight MMAs per step with two distinct A fragments and four distinct B
+// fragments, as a GEMM tile issues them.  (Issuing the same operand registers
+// back to back runs several times faster on GB300 -- operand reuse that no
+// GEMM can exploit -- so it would not be an honest roofline denominator.)
 __global__ void probe_dmma(double *out, double av, double bv) {
-    double a[8], b[4], c[2][4];
+    double a[2][8], b[4][4], c[8][4];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) a[j] = av + threadIdx.x + j;
+    for (int q = 0; q < 2; ++q)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) b[j] = bv + j;
+        for (int j = 0; j < 8; ++j) a[q][j] = (av + threadIdx.x + j + q) * 0.1234567891234567;
 #pragma unroll
-    for (int j = 0; j < 2; ++j)
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) b[q][j] = (bv + j + q) * 0.7654321987654321;
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
 #pragma unroll
         for (int q = 0; q < 4; ++q) c[j][q] = 0.0;
-    for (int i = 0; i < kIters / 16; ++i) {
+    for (int i = 0; i < kIters / 64; ++i) {
 #pragma unroll
-        for (int j = 0; j < 2; ++j)
+        for (int j = 0; j < 8; ++j) {
+            const int ia = j % 2, ib = j / 2;
             asm volatile(
                 "mma.sync.aligned.m16n8k16.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, "
                 "{%4,%5,%6,%7,%8,%9,%10,%11}, {%12,%13,%14,%15}, {%0,%1,%2,%3};"
                 : "+d"(c[j][0]), "+d"(c[j][1]), "+d"(c[j][2]), "+d"(c[j][3])
-                : "d"(a[0]), "d"(a[1]), "d"(a[2]), "d"(a[3]), "d"(a[4]), "d"(a[5]), "d"(a[6]),
-                  "d"(a[7]), "d"(b[0]), "d"(b[1]), "d"(b[2]), "d"(b[3]));
+                : "d"(a[ia][0]), "d"(a[ia][1]), "d"(a[ia][2]), "d"(a[ia][3]), "d"(a[ia][4]),
+                  "d"(a[ia][5]), "d"(a[ia][6]), "d"(a[ia][7]), "d"(b[ib][0]), "d"(b[ib][1]),
+                  "d"(b[ib][2]), "d"(b[ib][3]));
+        }
     }
     double s = 0.0;
 #pragma unroll
-    for (int j = 0; j < 2; ++j)
+    for (int j = 0; j < 8; ++j)
 #pragma unroll
         for (int q = 0; q < 4; ++q) s += c[j][q];
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
@@ -81,9 +92,9 @@ extern "C" double lla_measure_peak_tflops(int which) {
     for (int rep = 0; rep < 4; ++rep) {
         cudaEventRecord(e0);
         double flops = 0.0;
-        if (which == 0) {  // FP64 tensor pipe: 2 x m16n8k16 per iteration step
+        if (which == 0) {  // FP64 tensor pipe: 8 x m16n8k16 per step
             probe_dmma<<<blocks, threads>>>(out, 0.5, 0.25);
-            flops = 2.0 * 16 * 8 * 16 * 2 * (kIters / 16) * (double)(threads / 32) * blocks;
+            flops = 2.0 * 16 * 8 * 16 * 8 * (kIters / 64) * (double)(threads / 32) * blocks;
         } else if (which == 1) {
             probe_dfma<<<blocks, threads>>>(out, 0.999, 1e-3);
             flops = 2.0 * 8 * kIters * (double)threads * blocks;

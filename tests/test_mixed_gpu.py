@@ -1,0 +1,123 @@
+"""GPU tests of the mixed-precision refined solve (low-precision Cholesky of
+the equilibrated matrix + FP64 refinement + plain FP64 fallback).
+
+Every converged result must reach the target normwise backward error
+(1e-13 by default) measured here independently in FP64, and agree with the
+plain FP64 solution to the forward error the conditioning allows.  Failures
+are decided by the FP64 path: a non-SPD input raises NotPositiveDefinite.
+"""
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+UPDATES = ["fp32"]
+
+
+def qdq(rng, n, kappa, diag_scale=0.0):
+    """A = D Q diag(s) Q^T D, Q from QR of a Gaussian, s log-uniform in [1, kappa],
+    D = diag(10^U(-diag_scale, diag_scale))."""
+    q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = np.exp(rng.uniform(0, np.log(kappa), n))
+    s[0], s[-1] = 1.0, kappa
+    a = (q * s) @ q.T
+    a = (a + a.T) / 2
+    if diag_scale:
+        d = 10.0 ** rng.uniform(-diag_scale, diag_scale, n)
+        a = a * d[:, None] * d[None, :]
+    return a
+
+
+def backward_error(a, x, b):
+    r = b - a @ x
+    return (np.abs(r).max(0) / (np.abs(a).sum(1).max() * np.abs(x).max(0) + np.abs(b).max(0))).max()
+
+
+@pytest.mark.parametrize("update", UPDATES)
+@pytest.mark.parametrize("n,kappa", [(100, 1e2), (512, 1e6), (1000, 1e4), (1537, 1e6)])
+def test_refined_reaches_fp64_accuracy(gpu_lla, update, n, kappa):
+    lla = gpu_lla
+    rng = np.random.default_rng(n)
+    a = qdq(rng, n, kappa)
+    b = rng.standard_normal((n, 7))
+    x = b.copy()
+    rep = lla.posv_refined(a, x, update=update)
+    assert rep["converged"] == 1 and rep["fell_back"] == 0, rep
+    assert rep["backward_error"] <= 1e-13
+    be = backward_error(a, x, b)
+    assert be <= 2e-13, be
+    xr = np.linalg.solve(a, b)
+    fe = np.abs(x - xr).max() / np.abs(xr).max()
+    assert fe <= max(kappa * 1e-13, 1e-12), fe
+
+
+def test_equilibration_handles_badly_scaled_diagonal(gpu_lla):
+    lla = gpu_lla
+    rng = np.random.default_rng(3)
+    n = 700
+    a = qdq(rng, n, 1e4, diag_scale=3.0)
+    b = rng.standard_normal((n, 4))
+    x = b.copy()
+    rep = lla.posv_refined(a, x)
+    assert rep["backward_error"] <= 1e-13
+    assert backward_error(a, x, b) <= 2e-13
+
+
+def test_strided_views_and_lower_triangle_only(gpu_lla):
+    """Only the lower triangle is read (as in the reference's solvec)."""
+    lla = gpu_lla
+    rng = np.random.default_rng(4)
+    n = 300
+    a = cases.spd_gram(rng, n)
+    garbage = a.copy()
+    garbage[np.triu_indices(n, 1)] = 1e9
+    b = rng.standard_normal((n, 3))
+    x = cases.relayout(b.copy(), rng)
+    lla.posv_refined(cases.relayout(garbage, rng), x)
+    assert backward_error(a, x, b) <= 2e-13
+
+
+def test_not_positive_definite_decided_by_fp64_path(gpu_lla):
+    lla = gpu_lla
+    rng = np.random.default_rng(6)
+    n = 200
+    a = cases.spd_gram(rng, n)
+    a[50, 50] = -1.0
+    with pytest.raises(lla.NotPositiveDefinite) as e:
+        lla.posv_refined(a, np.ones((n, 2)))
+    assert e.value.index == 50
+
+
+def test_ill_conditioned_falls_back_or_converges(gpu_lla):
+    lla = gpu_lla
+    rng = np.random.default_rng(8)
+    n = 400
+    a = qdq(rng, n, 1e12)
+    b = rng.standard_normal((n, 2))
+    x = b.copy()
+    rep = lla.posv_refined(a, x)
+    assert rep["converged"] == 1 or rep["fell_back"] == 1
+    assert backward_error(a, x, b) <= 1e-13
+    x2 = b.copy()
+    with pytest.raises(lla.DeviceError) as e:
+        lla.posv_refined(a, x2, fallback=False, max_iters=2)
+    assert e.value.code == lla.ERR_NOT_CONVERGED
+
+
+def test_device_form_matches_host_form(gpu_lla):
+    torch = pytest.importorskip("torch")
+    lla = gpu_lla
+    rng = np.random.default_rng(10)
+    n, m = 640, 5
+    a = qdq(rng, n, 1e5)
+    b = rng.standard_normal((n, m))
+    A = torch.tensor(a, device="cuda").T.contiguous().T
+    B = torch.tensor(b, device="cuda").T.contiguous().T
+    X = torch.empty_like(B.T.contiguous()).T
+    rep = lla.posv_refined_device(A, B, X)
+    x = b.copy()
+    rep2 = lla.posv_refined(a, x)
+    assert rep["iterations"] == rep2["iterations"]
+    assert np.array_equal(X.cpu().numpy(), x)
