@@ -259,6 +259,15 @@ int lla_dposv_refined(const double *a, int64_t rows, int64_t cols, int64_t rs, i
                       double *b, int64_t brows, int64_t bcols, int64_t brs, int64_t bcs,
                       const lla_refine_opts *opts, lla_refine_report *report, lla_error *err);
 
+/* The low-precision factorisation on its own: in-place Cholesky of the lower
+ * triangle of an FP32 SPD matrix (column-major, ld) with FP32 diagonal blocks
+ * and panels and the trailing updates in the given lla_update form.  *d_info
+ * (device) receives -1, or the first row of the panel where a non-positive
+ * pivot appeared.  Synchronises `stream` for the tensor-core forms (their
+ * bounded waits report LLA_ERR_TIMEOUT). */
+int lla_spotrf_mixed_device(float *dA, int64_t n, int64_t ld, int update, int64_t *d_info,
+                            void *stream, lla_error *err);
+
 /* ---- diagnostics (no counterpart in the reference) ----------------------
  * Launch accounting and per-kernel CUDA-event timing used by the benchmark:
  * while profiling is on, every kernel launch is bracketed by an event pair on

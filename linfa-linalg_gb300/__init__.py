@@ -108,6 +108,8 @@ EXPORTS = {
                                   ctypes.c_void_p, _E], ctypes.c_int),
     "lla_dposv_refined": (_V + _V + [ctypes.POINTER(RefineOpts), ctypes.POINTER(RefineReport), _E],
                           ctypes.c_int),
+    "lla_spotrf_mixed_device": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
+                                 ctypes.c_void_p, ctypes.c_void_p, _E], ctypes.c_int),
 }
 for _p in "ds":
     EXPORTS.update({
@@ -457,3 +459,20 @@ def posv_refined_device(A, B, X, stream=None, **kw):
                                  ctypes.byref(e))
     _raise(e)
     return r.as_dict()
+
+
+def spotrf_mixed_device(A, update="fp16x3", info=None, stream=None):
+    """Low-precision Cholesky of a column-major FP32 CUDA tensor in place (FP32
+    diagonal blocks and panels, tensor-core trailing updates); returns the
+    device int64 info tensor."""
+    import torch
+    n = A.shape[0]
+    assert A.is_cuda and A.dtype == torch.float32 and A.stride(0) == 1
+    if info is None:
+        info = torch.empty(1, dtype=torch.int64, device=A.device)
+    u = UPDATE_NAMES[update] if isinstance(update, str) else int(update)
+    e = Error()
+    lib.lla_spotrf_mixed_device(ctypes.c_void_p(A.data_ptr()), n, max(1, A.stride(1)), u,
+                                ctypes.c_void_p(info.data_ptr()), _stream_ptr(stream), ctypes.byref(e))
+    _raise(e)
+    return info

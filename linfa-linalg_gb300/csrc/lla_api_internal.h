@@ -30,7 +30,7 @@ struct MixedWs {
     DevBuf L, s, rowsum, R, Y, diag0, words;  // FP32 factor, scaling, norms, residual, correction
     DevBuf F, fdiag;                          // plain FP64 fallback
     DevBuf opA, opB;                          // tensor-core operand planes of one panel
-    DevBuf maps;                              // TMA descriptors
+    DevBuf tcerr;                             // tensor-core update status word
     HostBuf words_host;
 };
 

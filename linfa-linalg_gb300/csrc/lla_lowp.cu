@@ -1,18 +1,322 @@
-// lla_lowp.cu -- low-precision Cholesky of the equilibrated FP32 matrix for
-// the mixed-precision solve: dispatch on the trailing-update form.
+// lla_lowp.cu -- low-precision Cholesky of the equilibrated FP32 matrix used
+// by the mixed-precision solve (lla_mixed.cu).
+//
+// Right-looking with panels of nb = 128 columns:
+//   diag   : one CTA factors the 128 x 128 diagonal block in FP32 (32-column
+//            sub-blocks: a one-warp shuffle Cholesky, a row-parallel solve of
+//            the rows below it, a shared-memory update of the rest);
+//   panel  : L21 = A21 L11^-T in FP32, one thread per row, and the operand
+//            planes of L21 for the tensor cores: a one-, two- or three-term
+//            split of every FP32 value into BF16 (or FP16) parts
+//            x ~= h0 + h1 + h2;
+//   update : A22 -= L21 L21^T on the 5th-generation tensor cores
+//            (lla_tc_update.cu): the products of the chosen term pairs
+//            (h0 h0^T, h0 h1^T + h1 h0^T, ...) accumulate in FP32 in tensor
+//            memory and are subtracted from the FP32 trailing matrix.
+// With two FP16 terms (11 + 11 significant bits) or three BF16 terms the
+// update is as accurate as an FP32 one; one BF16 term (8 bits) is the fastest
+// and the least accurate (refinement converges only for modest condition
+// numbers and otherwise falls back).
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstring>
+
 #include "lla_api_internal.h"
 #include "lla_common.cuh"
 #include "lla_kernels.h"
 #include "lla_mixed.h"
 #include "lla_prof.h"
+#include "lla_tc.h"
 
 namespace lla {
 
+constexpr int kLpNb = 128;  // panel width
+constexpr int kLpLd = kLpNb + 1;
+
+// ---------------------------------------------------------------------------
+// diagonal block: b <= 128, one CTA of 1024 threads, block in shared memory
+
+__global__ void __launch_bounds__(1024) lowp_diag_kernel(float *L, int64_t ld, int64_t p, int b,
+                                                         int64_t *info, double *min_ratio) {
+    extern __shared__ float sa[];  // [128][129]: sa[r * kLpLd + c] = L11[r][c]
+    __shared__ int failed;
+    if (*(volatile int64_t *)info >= 0) return;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int e = tid; e < kLpNb * kLpNb; e += 1024) {
+        const int r = e % kLpNb, c = e / kLpNb;
+        if (r < b && c <= r) sa[r * kLpLd + c] = L[(p + r) + (p + c) * ld];
+    }
+    if (tid == 0) failed = 0;
+    __syncthreads();
+    float ratio = 1e30f;
+    for (int kb = 0; kb < b; kb += 32) {
+        const int bs = min(32, b - kb);
+        // (1) one warp: Cholesky of the bs x bs block; lane i holds row kb+i
+        if (warp == 0) {
+            float v[32];
+#pragma unroll
+            for (int c = 0; c < 32; ++c)
+                v[c] = (lane < bs && c <= lane) ? sa[(kb + lane) * kLpLd + kb + c] : 0.f;
+            bool bad = false;
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+                if (c < bs) {
+                    const float piv = __shfl_sync(0xffffffffu, v[c], c);
+                    if (!(piv > 0.f)) bad = true;  // non-positive (or NaN) pivot: breakdown
+                    const float lcc = sqrtf(fmaxf(piv, 0.f));
+                    if (lane == c) {
+                        v[c] = lcc;
+                        ratio = fminf(ratio, piv);
+                    }
+                    if (lane > c) v[c] = v[c] / lcc;
+#pragma unroll
+                    for (int c2 = c + 1; c2 < 32; ++c2) {
+                        const float t = __shfl_sync(0xffffffffu, v[c], c2);
+                        if (c2 < bs && lane >= c2) v[c2] = fmaf(-v[c], t, v[c2]);
+                    }
+                }
+            }
+            if (lane == 0 && bad) failed = 1;
+            if (lane < bs) {
+#pragma unroll
+                for (int c = 0; c < 32; ++c)
+                    if (c <= lane) sa[(kb + lane) * kLpLd + kb + c] = v[c];
+            }
+        }
+        __syncthreads();
+        if (failed) break;
+        const int rest0 = kb + bs;
+        // (2) rows below inside the block: row r solves against the bs x bs factor
+        if (tid < b - rest0) {
+            const int r = rest0 + tid;
+            float v[32];
+#pragma unroll
+            for (int c = 0; c < 32; ++c) v[c] = (c < bs) ? sa[r * kLpLd + kb + c] : 0.f;
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+                if (c < bs) {
+                    v[c] = v[c] / sa[(kb + c) * kLpLd + kb + c];
+#pragma unroll
+                    for (int c2 = c + 1; c2 < 32; ++c2)
+                        if (c2 < bs) v[c2] = fmaf(-v[c], sa[(kb + c2) * kLpLd + kb + c], v[c2]);
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 32; ++c)
+                if (c < bs) sa[r * kLpLd + kb + c] = v[c];
+        }
+        __syncthreads();
+        // (3) trailing part of the block: a[r][c] -= sum_t a[r][kb+t] a[c][kb+t]
+        const int w = b - rest0;
+        for (int e = tid; e < w * w; e += 1024) {
+            const int r = rest0 + e % w, c = rest0 + e / w;
+            if (c <= r) {
+                float acc = sa[r * kLpLd + c];
+                for (int t = 0; t < bs; ++t)
+                    acc = fmaf(-sa[r * kLpLd + kb + t], sa[c * kLpLd + kb + t], acc);
+                sa[r * kLpLd + c] = acc;
+            }
+        }
+        __syncthreads();
+    }
+    if (failed) {
+        if (tid == 0) *info = p;  // the low-precision factorisation broke down in this panel
+        return;
+    }
+    if (warp == 0) {
+        // smallest pivot of this block relative to the unit-ish equilibrated diagonal
+        float rmin = ratio;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) rmin = fminf(rmin, __shfl_xor_sync(0xffffffffu, rmin, o));
+        if (lane == 0 && min_ratio) {
+            const double d = (double)rmin;
+            if (d >= 0.0)
+                atomicMin((unsigned long long *)min_ratio,
+                          (unsigned long long)__double_as_longlong(d));
+        }
+    }
+    for (int e = tid; e < kLpNb * kLpNb; e += 1024) {
+        const int r = e % kLpNb, c = e / kLpNb;
+        if (r < b && c <= r) L[(p + r) + (p + c) * ld] = sa[r * kLpLd + c];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// panel: rows [q, n), q = p + b.  L21 row j = A21 row j * L11^-T (FP32), then
+// the operand planes P_t[r][k] (r = j - q, k < kpad; zero for k >= b).
+
+template <typename H>
+__device__ __forceinline__ H to_half(float x);
+template <>
+__device__ __forceinline__ __nv_bfloat16 to_half<__nv_bfloat16>(float x) { return __float2bfloat16_rn(x); }
+template <>
+__device__ __forceinline__ __half to_half<__half>(float x) { return __float2half_rn(x); }
+__device__ __forceinline__ float from_half(__nv_bfloat16 h) { return __bfloat162float(h); }
+__device__ __forceinline__ float from_half(__half h) { return __half2float(h); }
+
+template <typename H>
+__global__ void __launch_bounds__(128) lowp_panel_kernel(float *L, int64_t ld, int64_t n, int64_t p,
+                                                         int b, H *planes, int64_t plane_stride,
+                                                         int kpad, int terms, const int64_t *info) {
+    extern __shared__ float sl[];  // L11: [128][129]
+    if (*(volatile const int64_t *)info >= 0) return;
+    for (int e = threadIdx.x; e < kLpNb * kLpNb; e += blockDim.x) {
+        const int r = e % kLpNb, c = e / kLpNb;
+        if (r < b && c <= r) sl[r * kLpLd + c] = L[(p + r) + (p + c) * ld];
+    }
+    __syncthreads();
+    const int64_t q = p + b;
+    const int64_t j = q + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    float v[kLpNb];
+#pragma unroll
+    for (int k = 0; k < kLpNb; ++k) v[k] = (k < b) ? L[j + (p + k) * ld] : 0.f;
+#pragma unroll
+    for (int k = 0; k < kLpNb; ++k) {
+        if (k < b) {
+            v[k] = v[k] / sl[k * kLpLd + k];
+#pragma unroll
+            for (int k2 = k + 1; k2 < kLpNb; ++k2)
+                if (k2 < b) v[k2] = fmaf(-v[k], sl[k2 * kLpLd + k], v[k2]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kLpNb; ++k)
+        if (k < b) L[j + (p + k) * ld] = v[k];
+    // operand planes, 16-byte stores of 8 halves (v[k] = 0 for k >= b)
+    const int64_t r = j - q;
+#pragma unroll
+    for (int k0 = 0; k0 < kLpNb; k0 += 8) {
+        if (k0 < kpad) {
+            H h[3][8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const float x = v[k0 + u];
+                const H a0 = to_half<H>(x);
+                const float r1 = x - from_half(a0);  // exact in FP32
+                const H a1 = to_half<H>(r1);
+                const float r2 = r1 - from_half(a1);
+                h[0][u] = a0;
+                h[1][u] = a1;
+                h[2][u] = to_half<H>(r2);
+            }
+            for (int t = 0; t < terms; ++t)
+                *(uint4 *)(planes + t * plane_stride + r * kpad + k0) = *(const uint4 *)h[t];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host loop
+
+static int64_t tri_tiles128(int64_t m) {
+    const int64_t t = ceil_div(m, 128);
+    return t * (t + 1) / 2;
+}
+
 int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &opts, int64_t *info,
                        float *diag0, double *min_ratio, Ctx *c, cudaStream_t st) {
-    (void)opts;
-    (void)c;
-    return potrf_fast_launch<float>(L, n, ld, info, diag0, min_ratio, st);
+    const int upd = opts.update;
+    if (upd == LLA_UPDATE_FP32) return potrf_fast_launch<float>(L, n, ld, info, diag0, min_ratio, st);
+    const bool fp16 = (upd == LLA_UPDATE_FP16 || upd == LLA_UPDATE_FP16X3);
+    const int terms = (upd == LLA_UPDATE_BF16 || upd == LLA_UPDATE_FP16) ? 1
+                      : (upd == LLA_UPDATE_BF16X6)                        ? 3
+                                                                          : 2;
+    TcPairs pairs;
+    if (terms == 1) {
+        pairs.n = 1;
+        pairs.pa[0] = 0; pairs.pb[0] = 0;
+    } else if (terms == 2) {  // small products first
+        pairs.n = 3;
+        const int pa[3] = {0, 1, 0}, pb[3] = {1, 0, 0};
+        for (int i = 0; i < 3; ++i) pairs.pa[i] = pa[i], pairs.pb[i] = pb[i];
+    } else {
+        pairs.n = 6;
+        const int pa[6] = {0, 1, 2, 0, 1, 0}, pb[6] = {2, 1, 0, 1, 0, 0};
+        for (int i = 0; i < 6; ++i) pairs.pa[i] = pa[i], pairs.pb[i] = pb[i];
+    }
+    const int kpad = kLpNb;
+    const int64_t plane_stride = n * kpad;  // elements per plane
+    if (c->mixed.opA.ensure(sizeof(uint16_t) * plane_stride * terms) != cudaSuccess) return -1;
+    void *planes = c->mixed.opA.p;
+    int *err_word = nullptr;
+    if (c->mixed.tcerr.ensure(sizeof(int)) != cudaSuccess) return -1;
+    err_word = (int *)c->mixed.tcerr.p;
+    if (cudaMemsetAsync(err_word, 0, sizeof(int), st) != cudaSuccess) return -1;
+    const size_t smem_l11 = sizeof(float) * kLpNb * kLpLd;
+    static bool attr_done = false;
+    if (!attr_done) {
+        cudaFuncSetAttribute(lowp_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_l11);
+        cudaFuncSetAttribute(lowp_panel_kernel<__nv_bfloat16>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_l11);
+        cudaFuncSetAttribute(lowp_panel_kernel<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_l11);
+        if (tc_update_prepare() != 0) return -1;
+        attr_done = true;
+    }
+    for (int64_t p = 0; p < n; p += kLpNb) {
+        const int b = (int)std::min<int64_t>(kLpNb, n - p);
+        {
+            LaunchScope ls(K_MIXED_DIAG, st, (double)b * b * b / 3.0);
+            lowp_diag_kernel<<<1, 1024, smem_l11, st>>>(L, ld, p, b, info, min_ratio);
+        }
+        const int64_t rest = n - p - b;
+        if (rest <= 0) break;
+        {
+            LaunchScope ls(K_MIXED_PANEL, st, (double)rest * b * b);
+            if (fp16)
+                lowp_panel_kernel<__half><<<(unsigned)ceil_div(rest, 128), 128, smem_l11, st>>>(
+                    L, ld, n, p, b, (__half *)planes, plane_stride, kpad, terms, info);
+            else
+                lowp_panel_kernel<__nv_bfloat16><<<(unsigned)ceil_div(rest, 128), 128, smem_l11, st>>>(
+                    L, ld, n, p, b, (__nv_bfloat16 *)planes, plane_stride, kpad, terms, info);
+        }
+        // algorithmic work of the update: rest(rest+1)/2 entries x b multiply-adds x 2
+        LaunchScope ls(K_MIXED_UPDATE, st, (double)rest * (rest + 1) * b);
+        if (tc_update_launch(L, ld, p + b, n, planes, plane_stride, rest, kpad, terms, fp16, pairs,
+                             info, err_word, tri_tiles128(rest), st) != 0)
+            return -1;
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 }  // namespace lla
+
+// ---------------------------------------------------------------------------
+// C ABI: the low-precision factorisation on its own
+
+extern "C" int lla_spotrf_mixed_device(float *dA, int64_t n, int64_t ld, int update, int64_t *d_info,
+                                       void *stream, lla_error *err) {
+    using namespace lla;
+    if (n < 0 || ld < std::max<int64_t>(1, n) || !d_info || (n > 0 && !dA) ||
+        !(update == LLA_UPDATE_FP32 || update == LLA_UPDATE_BF16 || update == LLA_UPDATE_BF16X3 ||
+          update == LLA_UPDATE_BF16X6 || update == LLA_UPDATE_FP16 || update == LLA_UPDATE_FP16X3))
+        return lla__set_status(err, LLA_ERR_INVALID_ARG);
+    lla__set_status(err, LLA_OK);
+    Ctx *c = get_ctx(err);
+    if (!c) return err ? err->code : LLA_ERR_NO_DEVICE;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(d_info, 0xff, sizeof(int64_t), st);
+    if (e != cudaSuccess) return lla__set_cuda_error(err, e);
+    if (n == 0) return LLA_OK;
+    if ((e = c->mixed.diag0.ensure(sizeof(float) * n)) != cudaSuccess) return lla__set_cuda_error(err, e);
+    lla_refine_opts o;
+    lla_refine_opts_default(&o);
+    o.update = update;
+    if (lowp_factor_launch(dA, n, ld, o, d_info, (float *)c->mixed.diag0.p, nullptr, c, st) != 0) {
+        e = cudaGetLastError();
+        return lla__set_cuda_error(err, e == cudaSuccess ? cudaErrorUnknown : e);
+    }
+    if (update != LLA_UPDATE_FP32) {
+        int flag = 0;
+        if ((e = cudaMemcpyAsync(&flag, c->mixed.tcerr.p, sizeof(int), cudaMemcpyDeviceToHost, st)) !=
+                cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            return lla__set_cuda_error(err, e);
+        if (flag) return lla__set_status(err, flag);
+    }
+    return LLA_OK;
+}

@@ -1,0 +1,31 @@
+// lla_tc.h -- tensor-core (tcgen05) trailing update of the mixed-precision
+// Cholesky.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lla {
+
+// Term pairs (a, b): the update subtracts sum_pairs P_a[I] P_b[J]^T.
+struct TcPairs {
+    int n;
+    int pa[6];
+    int pb[6];
+};
+
+// One-time set-up (dynamic shared memory limit, driver entry point for TMA
+// descriptors); 0 on success.
+int tc_update_prepare();
+
+// C[q + I*128 + r, q + J*128 + c] -= sum over pairs of planes[a][I*128 + r, :] .
+// planes[b][J*128 + c, :] for the lower tiles I >= J of the rows x rows
+// trailing matrix (FP32, column-major, leading dimension ld, global order n).
+// planes: `terms` planes of rows x kpad BF16 (or FP16) values, plane_stride
+// elements apart, row-major.  Skips all work when *info >= 0; bounded waits
+// record LLA_ERR_TIMEOUT in *err_word.
+int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, int64_t plane_stride,
+                     int64_t rows, int kpad, int terms, bool fp16, const TcPairs &pairs,
+                     const int64_t *info, int *err_word, int64_t tiles, cudaStream_t st);
+
+}  // namespace lla

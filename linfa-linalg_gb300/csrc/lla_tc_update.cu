@@ -1,0 +1,284 @@
+// lla_tc_update.cu -- trailing update A22 -= L21 L21^T of the mixed-precision
+// Cholesky on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// One CTA per 128 x 128 lower tile (I >= J) of the trailing matrix:
+//   * thread 0 streams 64-wide K chunks of the two operand row blocks with TMA
+//     (cp.async.bulk.tensor, 128-byte swizzle) into a 3-stage shared-memory
+//     ring, completion tracked by mbarriers;
+//   * thread 32 issues tcgen05.mma (kind::f16, M = 128, N = 128, K = 16, BF16
+//     or FP16 operands, FP32 accumulator in tensor memory) for every chunk of
+//     every term pair, releasing each stage with tcgen05.commit;
+//   * all four warps then read the accumulator from tensor memory
+//     (tcgen05.ld 32x32b, one 32-lane quarter per warp) and subtract it from the
+//     FP32 tile in HBM (coalesced: a warp covers 32 consecutive rows of a
+//     column-major column); diagonal tiles write their lower half only.
+// Every wait is bounded: on expiry the CTA records LLA_ERR_TIMEOUT, skips its
+// writes, frees its tensor memory and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include "lla_common.cuh"
+#include "lla_tc.h"
+
+namespace lla {
+
+constexpr int kTcM = 128, kTcN = 128, kTcK = 64;  // tile and K-chunk
+constexpr int kTcStages = 3;
+constexpr int kTcTileBytes = kTcM * kTcK * 2;  // 16 KiB per operand per stage
+constexpr int kTcSmem = 1024 + 2 * kTcStages * kTcTileBytes + 256;
+constexpr long long kTcSpin = 1ll << 22;  // polls per wait (well under a second of polling)
+constexpr uint32_t kTcCols = 128;  // tensor-memory columns (FP32 128 x 128 accumulator)
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n"
+        " .reg .pred p;\n"
+        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait on an mbarrier phase; false when the limit expired or another
+// CTA has already reported a failure.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, const int *err_word) {
+    for (long long i = 0; i < kTcSpin; ++i) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((i & 1023) == 1023 && *(volatile const int *)err_word != 0) return false;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y, int z,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major operand tile stored with the
+// 128-byte swizzle: rows of 128 bytes, 8-row (1024-byte) swizzle atoms
+// stacked along M (stride byte offset 1024); the leading byte offset is not
+// used by swizzled K-major layouts; bit 46 is the Blackwell descriptor version.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) |
+           ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+    asm volatile(
+        "{\n"
+        " .reg .pred p;\n"
+        " setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+        "}\n" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+          "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]),
+          "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]),
+          "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_tri_tile(int64_t t, int64_t &I, int64_t &J) {
+    int64_t i = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while ((i + 1) * (i + 2) / 2 <= t) ++i;
+    while (i * (i + 1) / 2 > t) --i;
+    I = i;
+    J = t - i * (i + 1) / 2;
+}
+
+__global__ void __launch_bounds__(128, 1) tc_update_kernel(const __grid_constant__ CUtensorMap tmap,
+                                                          float *C, int64_t ld, int64_t q, int64_t n,
+                                                          int kchunks, TcPairs pairs, uint32_t idesc,
+                                                          const int64_t *info, int *err_word) {
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ int s_abort;
+    if (*(volatile const int64_t *)info >= 0 || *(volatile const int *)err_word != 0) return;
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *sA = smem;
+    uint8_t *sB = smem + kTcStages * kTcTileBytes;
+    uint64_t *bars = (uint64_t *)(smem + 2 * kTcStages * kTcTileBytes);
+    uint32_t *tslot = (uint32_t *)(bars + 2 * kTcStages + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    int64_t I, J;
+    tc_tri_tile(blockIdx.x, I, J);
+    const int rowA = (int)(I * kTcM), rowB = (int)(J * kTcN);
+    const int total = pairs.n * kchunks;
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kTcStages);
+    const uint32_t done = smem_u32(bars + 2 * kTcStages);
+    if (tid == 0) {
+        for (int s = 0; s < kTcStages; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tslot)),
+                     "r"(kTcCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    if (tid == 0) {  // TMA producer
+        for (int it = 0; it < total; ++it) {
+            const int s = it % kTcStages;
+            if (it >= kTcStages && !mbar_wait(empty0 + 8 * s, ((it / kTcStages) - 1) & 1, err_word)) {
+                s_abort = 1;
+                break;
+            }
+            mbar_expect_tx(full0 + 8 * s, 2 * kTcTileBytes);
+            const int pr = it / kchunks, kc = it % kchunks;
+            tma_load_3d(smem_u32(sA + s * kTcTileBytes), &tmap, kc * kTcK, rowA, pairs.pa[pr],
+                        full0 + 8 * s);
+            tma_load_3d(smem_u32(sB + s * kTcTileBytes), &tmap, kc * kTcK, rowB, pairs.pb[pr],
+                        full0 + 8 * s);
+        }
+    } else if (tid == 32) {  // MMA issuer
+        for (int it = 0; it < total; ++it) {
+            const int s = it % kTcStages;
+            if (!mbar_wait(full0 + 8 * s, (it / kTcStages) & 1, err_word)) {
+                s_abort = 1;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t a0 = smem_u32(sA + s * kTcTileBytes), b0 = smem_u32(sB + s * kTcTileBytes);
+#pragma unroll
+            for (int k = 0; k < kTcK / 16; ++k)
+                tc_mma(tmem, sw128_desc(a0 + 32 * k), sw128_desc(b0 + 32 * k), idesc,
+                       (it > 0 || k > 0) ? 1u : 0u);
+            tc_commit(empty0 + 8 * s);  // frees the stage once these MMAs are done
+        }
+        tc_commit(done);  // arrives when every MMA issued above has completed
+    }
+    __syncwarp();
+    __syncthreads();
+    bool ok = mbar_wait(done, 0, err_word);
+    ok = __all_sync(0xffffffffu, ok) && !s_abort;
+    if (ok) {
+        tc_fence_after();
+        const int r = warp * 32 + lane;
+        const int64_t grow = q + rowA + r;
+#pragma unroll 1
+        for (int cb = 0; cb < kTcN / 32; ++cb) {
+            uint32_t v[32];
+            tc_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 32), v);
+            if (grow < n) {
+#pragma unroll
+                for (int c = 0; c < 32; ++c) {
+                    const int cc = cb * 32 + c;
+                    const int64_t gcol = q + rowB + cc;
+                    if (gcol < n && (I != J || cc <= r)) {
+                        float *p = C + grow + gcol * ld;
+                        *p = *p - __uint_as_float(v[c]);
+                    }
+                }
+            }
+        }
+    } else if (tid == 0) {
+        atomicCAS(err_word, 0, (int)LLA_ERR_TIMEOUT);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols)
+                     : "memory");
+}
+
+// ---------------------------------------------------------------------------
+
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+int tc_update_prepare() {
+    if (!g_encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult qres;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                             &qres) != cudaSuccess ||
+            qres != cudaDriverEntryPointSuccess || !fn)
+            return -1;
+        g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }
+    if (cudaFuncSetAttribute(tc_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) !=
+        cudaSuccess)
+        return -1;
+    return 0;
+}
+
+int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, int64_t plane_stride,
+                     int64_t rows, int kpad, int terms, bool fp16, const TcPairs &pairs,
+                     const int64_t *info, int *err_word, int64_t tiles, cudaStream_t st) {
+    if (!g_encode || rows <= 0 || kpad % kTcK != 0) return -1;
+    CUtensorMap map;
+    const cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rows, (cuuint64_t)terms};
+    const cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)plane_stride * 2};
+    const cuuint32_t box[3] = {(cuuint32_t)kTcK, (cuuint32_t)kTcM, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r =
+        g_encode(&map, fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
+                 planes, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                 CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return -1;
+    // instruction descriptor: D = F32 (bits 4-5), A/B = BF16 (1) or F16 (0) (bits 7-9, 10-12),
+    // both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+    const uint32_t ab = fp16 ? 0u : 1u;
+    const uint32_t idesc = (1u << 4) | (ab << 7) | (ab << 10) | ((uint32_t)(kTcN >> 3) << 17) |
+                           ((uint32_t)(kTcM >> 4) << 24);
+    tc_update_kernel<<<(unsigned)tiles, 128, kTcSmem, st>>>(map, C, ld, q, n, kpad / kTcK, pairs,
+                                                            idesc, info, err_word);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace lla

@@ -13,7 +13,7 @@ import cases
 
 pytestmark = pytest.mark.gpu
 
-UPDATES = ["fp32"]
+UPDATES = ["fp32", "fp16x3", "bf16x6", "bf16x3"]
 
 
 def qdq(rng, n, kappa, diag_scale=0.0):
@@ -121,3 +121,29 @@ def test_device_form_matches_host_form(gpu_lla):
     rep2 = lla.posv_refined(a, x)
     assert rep["iterations"] == rep2["iterations"]
     assert np.array_equal(X.cpu().numpy(), x)
+
+
+# accuracy of the low-precision factorisation alone: ||L L^T - A|| / ||A||
+# bounds per update form (FP32 panels; the split forms are FP32-accurate)
+FACTOR_TOL = {"fp32": 2e-6, "fp16x3": 4e-6, "bf16x6": 4e-6, "bf16x3": 3e-5, "fp16": 3e-3,
+              "bf16": 3e-2}
+
+
+@pytest.mark.parametrize("update", list(FACTOR_TOL))
+@pytest.mark.parametrize("n", [128, 200, 385, 1024])
+def test_lowp_factor_accuracy(gpu_lla, update, n):
+    """Checks the tensor-core trailing update (and the FP32 diagonal/panel
+    kernels) directly: partial tiles, several panels, every term form."""
+    torch = pytest.importorskip("torch")
+    lla = gpu_lla
+    rng = np.random.default_rng(1000 + n)
+    a = cases.spd_gram(rng, n)
+    d = 1.0 / np.sqrt(np.diag(a))
+    a = a * d[:, None] * d[None, :]  # unit diagonal, as after equilibration
+    A = torch.tensor(a, dtype=torch.float32, device="cuda").T.contiguous().T
+    info = lla.spotrf_mixed_device(A, update=update)
+    torch.cuda.synchronize()
+    assert int(info.item()) == -1
+    L = np.tril(A.cpu().numpy().astype(np.float64))
+    rel = np.linalg.norm(L @ L.T - a) / np.linalg.norm(a)
+    assert rel <= FACTOR_TOL[update], rel
