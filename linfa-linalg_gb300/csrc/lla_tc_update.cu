@@ -136,8 +136,12 @@ __global__ void __launch_bounds__(128, 1) tc_update_kernel(const __grid_constant
                                                           int kchunks, TcPairs pairs, uint32_t idesc,
                                                           const int64_t *info, int *err_word) {
     extern __shared__ uint8_t smem_raw[];
-    __shared__ int s_abort;
-    if (*(volatile const int64_t *)info >= 0 || *(volatile const int *)err_word != 0) return;
+    __shared__ int s_abort, s_skip;
+    // one reader decides for the whole CTA (another CTA may set err_word meanwhile)
+    if (threadIdx.x == 0)
+        s_skip = (*(volatile const int64_t *)info >= 0 || *(volatile const int *)err_word != 0);
+    __syncthreads();
+    if (s_skip) return;
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *sA = smem;
     uint8_t *sB = smem + kTcStages * kTcTileBytes;
