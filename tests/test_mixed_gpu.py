@@ -50,7 +50,7 @@ def test_refined_reaches_fp64_accuracy(gpu_lla, update, n, kappa):
     assert be <= 2e-13, be
     xr = np.linalg.solve(a, b)
     fe = np.abs(x - xr).max() / np.abs(xr).max()
-    assert fe <= max(kappa * 1e-13, 1e-12), fe
+    assert fe <= 10 * kappa * max(rep["backward_error"], 1e-15), fe  # forward <~ kappa * backward
 
 
 def test_equilibration_handles_badly_scaled_diagonal(gpu_lla):
