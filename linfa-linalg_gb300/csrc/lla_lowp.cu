@@ -161,51 +161,66 @@ template <typename H>
 __global__ void __launch_bounds__(128) lowp_panel_kernel(float *L, int64_t ld, int64_t n, int64_t p,
                                                          int b, H *planes, int64_t plane_stride,
                                                          int kpad, int terms, const int64_t *info) {
-    extern __shared__ float sl[];  // L11: [128][129]
+    // L11 [128][129], 1/diag [128], then one finished row per thread [128][129]
+    extern __shared__ float sm[];
+    float *sl = sm, *rinv = sm + kLpNb * kLpLd, *rows = rinv + kLpNb;
     if (*(volatile const int64_t *)info >= 0) return;
     for (int e = threadIdx.x; e < kLpNb * kLpNb; e += blockDim.x) {
         const int r = e % kLpNb, c = e / kLpNb;
         if (r < b && c <= r) sl[r * kLpLd + c] = L[(p + r) + (p + c) * ld];
     }
     __syncthreads();
+    if (threadIdx.x < b) rinv[threadIdx.x] = 1.0f / sl[threadIdx.x * kLpLd + threadIdx.x];
+    __syncthreads();
     const int64_t q = p + b;
     const int64_t j = q + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    float v[kLpNb];
+    float *my = rows + threadIdx.x * kLpLd;  // conflict-free: bank (tid + k) % 32
+    // forward substitution l L11^T = a, 32 columns at a time in registers; the
+    // finished part of the row stays in shared memory
+    for (int kb = 0; kb < b; kb += 32) {
+        float v[32];
 #pragma unroll
-    for (int k = 0; k < kLpNb; ++k) v[k] = (k < b) ? L[j + (p + k) * ld] : 0.f;
+        for (int c = 0; c < 32; ++c) v[c] = (kb + c < b) ? L[j + (p + kb + c) * ld] : 0.f;
+        for (int t = 0; t < kb; ++t) {
+            const float lt = my[t];
 #pragma unroll
-    for (int k = 0; k < kLpNb; ++k) {
-        if (k < b) {
-            v[k] = v[k] / sl[k * kLpLd + k];
+            for (int c = 0; c < 32; ++c) v[c] = fmaf(-lt, sl[(kb + c) * kLpLd + t], v[c]);
+        }
 #pragma unroll
-            for (int k2 = k + 1; k2 < kLpNb; ++k2)
-                if (k2 < b) v[k2] = fmaf(-v[k], sl[k2 * kLpLd + k], v[k2]);
+        for (int c = 0; c < 32; ++c) {
+            if (kb + c < b) {
+                v[c] *= rinv[kb + c];
+#pragma unroll
+                for (int c2 = c + 1; c2 < 32; ++c2)
+                    v[c2] = fmaf(-v[c], sl[(kb + c2) * kLpLd + kb + c], v[c2]);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 32; ++c) {
+            if (kb + c < b) {
+                my[kb + c] = v[c];
+                L[j + (p + kb + c) * ld] = v[c];
+            }
         }
     }
-#pragma unroll
-    for (int k = 0; k < kLpNb; ++k)
-        if (k < b) L[j + (p + k) * ld] = v[k];
-    // operand planes, 16-byte stores of 8 halves (v[k] = 0 for k >= b)
+    // operand planes, 16-byte stores of 8 halves (zero for k >= b)
     const int64_t r = j - q;
+    for (int k0 = 0; k0 < kpad; k0 += 8) {
+        H h[3][8];
 #pragma unroll
-    for (int k0 = 0; k0 < kLpNb; k0 += 8) {
-        if (k0 < kpad) {
-            H h[3][8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const float x = v[k0 + u];
-                const H a0 = to_half<H>(x);
-                const float r1 = x - from_half(a0);  // exact in FP32
-                const H a1 = to_half<H>(r1);
-                const float r2 = r1 - from_half(a1);
-                h[0][u] = a0;
-                h[1][u] = a1;
-                h[2][u] = to_half<H>(r2);
-            }
-            for (int t = 0; t < terms; ++t)
-                *(uint4 *)(planes + t * plane_stride + r * kpad + k0) = *(const uint4 *)h[t];
+        for (int u = 0; u < 8; ++u) {
+            const float x = (k0 + u < b) ? my[k0 + u] : 0.f;
+            const H a0 = to_half<H>(x);
+            const float r1 = x - from_half(a0);  // exact in FP32
+            const H a1 = to_half<H>(r1);
+            const float r2 = r1 - from_half(a1);
+            h[0][u] = a0;
+            h[1][u] = a1;
+            h[2][u] = to_half<H>(r2);
         }
+        for (int t = 0; t < terms; ++t)
+            *(uint4 *)(planes + t * plane_stride + r * kpad + k0) = *(const uint4 *)h[t];
     }
 }
 
@@ -247,13 +262,14 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
     err_word = (int *)c->mixed.tcerr.p;
     if (cudaMemsetAsync(err_word, 0, sizeof(int), st) != cudaSuccess) return -1;
     const size_t smem_l11 = sizeof(float) * kLpNb * kLpLd;
+    const size_t smem_panel = sizeof(float) * (2 * kLpNb * kLpLd + kLpNb);
     static bool attr_done = false;
     if (!attr_done) {
         cudaFuncSetAttribute(lowp_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_l11);
         cudaFuncSetAttribute(lowp_panel_kernel<__nv_bfloat16>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_l11);
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_panel);
         cudaFuncSetAttribute(lowp_panel_kernel<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem_l11);
+                             (int)smem_panel);
         if (tc_update_prepare() != 0) return -1;
         attr_done = true;
     }
@@ -268,10 +284,10 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
         {
             LaunchScope ls(K_MIXED_PANEL, st, (double)rest * b * b);
             if (fp16)
-                lowp_panel_kernel<__half><<<(unsigned)ceil_div(rest, 128), 128, smem_l11, st>>>(
+                lowp_panel_kernel<__half><<<(unsigned)ceil_div(rest, 128), 128, smem_panel, st>>>(
                     L, ld, n, p, b, (__half *)planes, plane_stride, kpad, terms, info);
             else
-                lowp_panel_kernel<__nv_bfloat16><<<(unsigned)ceil_div(rest, 128), 128, smem_l11, st>>>(
+                lowp_panel_kernel<__nv_bfloat16><<<(unsigned)ceil_div(rest, 128), 128, smem_panel, st>>>(
                     L, ld, n, p, b, (__nv_bfloat16 *)planes, plane_stride, kpad, terms, info);
         }
         // algorithmic work of the update: rest(rest+1)/2 entries x b multiply-adds x 2

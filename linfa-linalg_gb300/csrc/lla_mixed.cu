@@ -73,27 +73,43 @@ __global__ void equil_convert_kernel(const double *__restrict__ A, int64_t lda, 
 }
 
 // Row sums of |A_sym| (A_sym from the lower triangle): one block per 32-column
-// strip; each element (i, k), i >= k, adds |a_ik| to row i and, off the
-// diagonal, to row k.
-__global__ void sym_rowsum_kernel(const double *__restrict__ A, int64_t lda, int64_t n,
-                                  double *rowsum) {
-    __shared__ double colacc[32];
+// strip [k0, k0+32).  Element (i, k), i >= k, adds |a_ik| to row i (a per-row
+// partial, one atomic per strip) and, off the diagonal, to row k (per-thread
+// column partials, reduced across the block at the end).
+__global__ void __launch_bounds__(256) sym_rowsum_kernel(const double *__restrict__ A, int64_t lda,
+                                                         int64_t n, double *rowsum) {
+    __shared__ double red[8][32];
     const int64_t k0 = (int64_t)blockIdx.x * 32;
-    if (threadIdx.x < 32) colacc[threadIdx.x] = 0.0;
-    __syncthreads();
+    double colp[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) colp[c] = 0.0;
     for (int64_t i = k0 + threadIdx.x; i < n; i += blockDim.x) {
         double racc = 0.0;
+#pragma unroll
         for (int c = 0; c < 32; ++c) {
             const int64_t k = k0 + c;
-            if (k >= n || k > i) break;
-            const double v = fabs(A[i + k * lda]);
-            racc += v;
-            if (k != i) atomicAdd(&colacc[c], v);
+            if (k < n && k <= i) {
+                const double v = fabs(A[i + k * lda]);
+                racc += v;
+                if (k != i) colp[c] += v;
+            }
         }
         atomicAdd(&rowsum[i], racc);
     }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int c = 0; c < 32; ++c) {
+        double v = colp[c];
+#pragma unroll
+        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][c] = v;
+    }
     __syncthreads();
-    if (threadIdx.x < 32 && k0 + threadIdx.x < n) atomicAdd(&rowsum[k0 + threadIdx.x], colacc[threadIdx.x]);
+    if (threadIdx.x < 32 && k0 + threadIdx.x < n) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
+        atomicAdd(&rowsum[k0 + threadIdx.x], v);
+    }
 }
 
 __global__ void max_reduce_kernel(const double *v, int64_t n, double *out) {

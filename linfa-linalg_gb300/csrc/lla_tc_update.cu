@@ -1,17 +1,20 @@
 // lla_tc_update.cu -- trailing update A22 -= L21 L21^T of the mixed-precision
 // Cholesky on the 5th-generation tensor cores (tcgen05, sm_103a).
 //
-// One CTA per 128 x 128 lower tile (I >= J) of the trailing matrix:
-//   * thread 0 streams 64-wide K chunks of the two operand row blocks with TMA
-//     (cp.async.bulk.tensor, 128-byte swizzle) into a 3-stage shared-memory
-//     ring, completion tracked by mbarriers;
-//   * thread 32 issues tcgen05.mma (kind::f16, M = 128, N = 128, K = 16, BF16
+// Persistent CTAs (one per SM) walk the 128 x 128 lower tiles (I >= J) of the
+// trailing matrix:
+//   * one thread streams 64-wide K chunks of the two operand row blocks with
+//     TMA (cp.async.bulk.tensor, 128-byte swizzle) into a 6-stage
+//     shared-memory ring, completion tracked by mbarriers;
+//   * one thread issues tcgen05.mma (kind::f16, M = 128, N = 128, K = 16, BF16
 //     or FP16 operands, FP32 accumulator in tensor memory) for every chunk of
-//     every term pair, releasing each stage with tcgen05.commit;
-//   * all four warps then read the accumulator from tensor memory
+//     every term pair, releasing each stage with tcgen05.commit, alternating
+//     between two accumulators;
+//   * four epilogue warps read a finished accumulator from tensor memory
 //     (tcgen05.ld 32x32b, one 32-lane quarter per warp) and subtract it from the
 //     FP32 tile in HBM (coalesced: a warp covers 32 consecutive rows of a
-//     column-major column); diagonal tiles write their lower half only.
+//     column-major column) while the next tile's MMAs run; diagonal tiles write
+//     their lower half only.
 // Every wait is bounded: on expiry the CTA records LLA_ERR_TIMEOUT, skips its
 // writes, frees its tensor memory and returns.
 #include <cuda.h>
@@ -24,7 +27,7 @@
 namespace lla {
 
 constexpr int kTcM = 128, kTcN = 128, kTcK = 64;  // tile and K-chunk
-constexpr int kTcStages = 3;
+constexpr int kTcStages = 6;
 constexpr int kTcTileBytes = kTcM * kTcK * 2;  // 16 KiB per operand per stage
 constexpr int kTcSmem = 1024 + 2 * kTcStages * kTcTileBytes + 256;
 constexpr long long kTcSpin = 1ll << 22;  // polls per wait (well under a second of polling)
@@ -131,10 +134,15 @@ __device__ __forceinline__ void tc_tri_tile(int64_t t, int64_t &I, int64_t &J) {
     J = t - i * (i + 1) / 2;
 }
 
-__global__ void __launch_bounds__(128, 1) tc_update_kernel(const __grid_constant__ CUtensorMap tmap,
-                                                          float *C, int64_t ld, int64_t q, int64_t n,
-                                                          int kchunks, TcPairs pairs, uint32_t idesc,
-                                                          const int64_t *info, int *err_word) {
+// Persistent, warp-specialised: warps 0-3 drain accumulators (epilogue),
+// warp 4 lane 0 feeds the shared-memory ring with TMA, warp 5 lane 0 issues
+// the MMAs.  Two tensor-memory accumulators let the epilogue of one tile
+// overlap the MMAs of the next.
+constexpr int kTcThreads = 192;
+
+__global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
+    const __grid_constant__ CUtensorMap tmap, float *C, int64_t ld, int64_t q, int64_t n, int kchunks,
+    TcPairs pairs, uint32_t idesc, int64_t ntiles, const int64_t *info, int *err_word) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ int s_abort, s_skip;
     // one reader decides for the whole CTA (another CTA may set err_word meanwhile)
@@ -146,27 +154,28 @@ __global__ void __launch_bounds__(128, 1) tc_update_kernel(const __grid_constant
     uint8_t *sA = smem;
     uint8_t *sB = smem + kTcStages * kTcTileBytes;
     uint64_t *bars = (uint64_t *)(smem + 2 * kTcStages * kTcTileBytes);
-    uint32_t *tslot = (uint32_t *)(bars + 2 * kTcStages + 1);
+    // bars: full[S], empty[S], tmem_full[2], tmem_empty[2]
+    uint32_t *tslot = (uint32_t *)(bars + 2 * kTcStages + 4);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    int64_t I, J;
-    tc_tri_tile(blockIdx.x, I, J);
-    const int rowA = (int)(I * kTcM), rowB = (int)(J * kTcN);
-    const int total = pairs.n * kchunks;
     const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kTcStages);
-    const uint32_t done = smem_u32(bars + 2 * kTcStages);
+    const uint32_t tfull0 = smem_u32(bars + 2 * kTcStages), tempty0 = tfull0 + 16;
+    const int per_tile = pairs.n * kchunks;
     if (tid == 0) {
         for (int s = 0; s < kTcStages; ++s) {
             mbar_init(full0 + 8 * s, 1);
             mbar_init(empty0 + 8 * s, 1);
         }
-        mbar_init(done, 1);
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(tfull0 + 8 * a, 1);
+            mbar_init(tempty0 + 8 * a, 128);  // every epilogue thread releases
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(tslot)),
-                     "r"(kTcCols)
+                     "r"(2 * kTcCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -175,68 +184,108 @@ __global__ void __launch_bounds__(128, 1) tc_update_kernel(const __grid_constant
     tc_fence_after();
     const uint32_t tmem = *tslot;
 
-    if (tid == 0) {  // TMA producer
-        for (int it = 0; it < total; ++it) {
-            const int s = it % kTcStages;
-            if (it >= kTcStages && !mbar_wait(empty0 + 8 * s, ((it / kTcStages) - 1) & 1, err_word)) {
-                s_abort = 1;
-                break;
-            }
-            mbar_expect_tx(full0 + 8 * s, 2 * kTcTileBytes);
-            const int pr = it / kchunks, kc = it % kchunks;
-            tma_load_3d(smem_u32(sA + s * kTcTileBytes), &tmap, kc * kTcK, rowA, pairs.pa[pr],
-                        full0 + 8 * s);
-            tma_load_3d(smem_u32(sB + s * kTcTileBytes), &tmap, kc * kTcK, rowB, pairs.pb[pr],
-                        full0 + 8 * s);
-        }
-    } else if (tid == 32) {  // MMA issuer
-        for (int it = 0; it < total; ++it) {
-            const int s = it % kTcStages;
-            if (!mbar_wait(full0 + 8 * s, (it / kTcStages) & 1, err_word)) {
-                s_abort = 1;
-                break;
-            }
-            tc_fence_after();
-            const uint32_t a0 = smem_u32(sA + s * kTcTileBytes), b0 = smem_u32(sB + s * kTcTileBytes);
-#pragma unroll
-            for (int k = 0; k < kTcK / 16; ++k)
-                tc_mma(tmem, sw128_desc(a0 + 32 * k), sw128_desc(b0 + 32 * k), idesc,
-                       (it > 0 || k > 0) ? 1u : 0u);
-            tc_commit(empty0 + 8 * s);  // frees the stage once these MMAs are done
-        }
-        tc_commit(done);  // arrives when every MMA issued above has completed
-    }
-    __syncwarp();
-    __syncthreads();
-    bool ok = mbar_wait(done, 0, err_word);
-    ok = __all_sync(0xffffffffu, ok) && !s_abort;
-    if (ok) {
-        tc_fence_after();
-        const int r = warp * 32 + lane;
-        const int64_t grow = q + rowA + r;
-#pragma unroll 1
-        for (int cb = 0; cb < kTcN / 32; ++cb) {
-            uint32_t v[32];
-            tc_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 32), v);
-            if (grow < n) {
-#pragma unroll
-                for (int c = 0; c < 32; ++c) {
-                    const int cc = cb * 32 + c;
-                    const int64_t gcol = q + rowB + cc;
-                    if (gcol < n && (I != J || cc <= r)) {
-                        float *p = C + grow + gcol * ld;
-                        *p = *p - __uint_as_float(v[c]);
+    if (warp == 4) {
+        if (lane == 0) {  // TMA producer
+            int64_t g = 0;
+            for (int64_t t = blockIdx.x; t < ntiles && !*(volatile int *)&s_abort; t += gridDim.x) {
+                int64_t I, J;
+                tc_tri_tile(t, I, J);
+                for (int it = 0; it < per_tile; ++it, ++g) {
+                    const int s = (int)(g % kTcStages);
+                    const int64_t round = g / kTcStages;
+                    if (round > 0 && !mbar_wait(empty0 + 8 * s, (uint32_t)((round - 1) & 1), err_word)) {
+                        s_abort = 1;
+                        break;
                     }
+                    mbar_expect_tx(full0 + 8 * s, 2 * kTcTileBytes);
+                    const int pr = it / kchunks, kc = it % kchunks;
+                    tma_load_3d(smem_u32(sA + s * kTcTileBytes), &tmap, kc * kTcK, (int)(I * kTcM),
+                                pairs.pa[pr], full0 + 8 * s);
+                    tma_load_3d(smem_u32(sB + s * kTcTileBytes), &tmap, kc * kTcK, (int)(J * kTcN),
+                                pairs.pb[pr], full0 + 8 * s);
                 }
             }
         }
-    } else if (tid == 0) {
-        atomicCAS(err_word, 0, (int)LLA_ERR_TIMEOUT);
+    } else if (warp == 5) {
+        if (lane == 0) {  // MMA issuer
+            int64_t g = 0, lt = 0;
+            for (int64_t t = blockIdx.x; t < ntiles && !*(volatile int *)&s_abort; t += gridDim.x, ++lt) {
+                const int a = (int)(lt & 1);
+                const int64_t use = lt >> 1;
+                if (use > 0 && !mbar_wait(tempty0 + 8 * a, (uint32_t)((use - 1) & 1), err_word)) {
+                    s_abort = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t dt = tmem + (uint32_t)(a * kTcCols);
+                for (int it = 0; it < per_tile; ++it, ++g) {
+                    const int s = (int)(g % kTcStages);
+                    if (!mbar_wait(full0 + 8 * s, (uint32_t)((g / kTcStages) & 1), err_word)) {
+                        s_abort = 1;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a0 = smem_u32(sA + s * kTcTileBytes);
+                    const uint32_t b0 = smem_u32(sB + s * kTcTileBytes);
+#pragma unroll
+                    for (int k = 0; k < kTcK / 16; ++k)
+                        tc_mma(dt, sw128_desc(a0 + 32 * k), sw128_desc(b0 + 32 * k), idesc,
+                               (it > 0 || k > 0) ? 1u : 0u);
+                    tc_commit(empty0 + 8 * s);  // frees the stage once these MMAs are done
+                }
+                if (s_abort) break;
+                tc_commit(tfull0 + 8 * a);  // accumulator a is complete
+            }
+        }
+    } else {  // warps 0-3: epilogue
+        int64_t lt = 0;
+        const int r = warp * 32 + lane;
+        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
+            const int a = (int)(lt & 1);
+            const int64_t use = lt >> 1;
+            bool ok = mbar_wait(tfull0 + 8 * a, (uint32_t)(use & 1), err_word);
+            ok = __all_sync(0xffffffffu, ok) && !*(volatile int *)&s_abort;
+            if (!ok) {
+                if (lane == 0) s_abort = 1;
+                break;
+            }
+            tc_fence_after();
+            int64_t I, J;
+            tc_tri_tile(t, I, J);
+            const int64_t grow = q + I * kTcM + r;
+#pragma unroll 1
+            for (int cb = 0; cb < kTcN / 32; ++cb) {
+                uint32_t v[32];
+                tc_ld32(tmem + (uint32_t)(a * kTcCols) + ((uint32_t)(warp * 32) << 16) +
+                            (uint32_t)(cb * 32),
+                        v);
+                if (grow < n) {
+                    float *base = C + grow + (q + J * kTcN + cb * 32) * ld;
+                    const int64_t cmax = n - (q + J * kTcN + cb * 32);  // columns left in the matrix
+                    float old[32];
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) {
+                        const bool in = c < cmax && (I != J || cb * 32 + c <= r);
+                        old[c] = in ? base[c * ld] : 0.f;
+                    }
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) {
+                        const bool in = c < cmax && (I != J || cb * 32 + c <= r);
+                        if (in) base[c * ld] = old[c] - __uint_as_float(v[c]);
+                    }
+                }
+            }
+            tc_fence_before();
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tempty0 + 8 * a) : "memory");
+        }
     }
-    tc_fence_before();
+    __syncwarp();
     __syncthreads();
+    if (s_abort && tid == 0) atomicCAS(err_word, 0, (int)LLA_ERR_TIMEOUT);
+    tc_fence_after();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(2 * kTcCols)
                      : "memory");
 }
 
@@ -280,8 +329,16 @@ int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, i
     const uint32_t ab = fp16 ? 0u : 1u;
     const uint32_t idesc = (1u << 4) | (ab << 7) | (ab << 10) | ((uint32_t)(kTcN >> 3) << 17) |
                            ((uint32_t)(kTcM >> 4) << 24);
-    tc_update_kernel<<<(unsigned)tiles, 128, kTcSmem, st>>>(map, C, ld, q, n, kpad / kTcK, pairs,
-                                                            idesc, info, err_word);
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, sms);
+    tc_update_kernel<<<grid, kTcThreads, kTcSmem, st>>>(map, C, ld, q, n, kpad / kTcK, pairs, idesc,
+                                                        tiles, info, err_word);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
