@@ -184,11 +184,14 @@ __global__ void __launch_bounds__(256) trsm_lookback(const T *__restrict__ M, in
     if (tid == 0) st_release(flags + rb * n_chunks + cc, 1);
 }
 
-// Columns per CTA and per thread of the look-back solve.
+// Columns per CTA and per thread of the look-back solve.  Narrow column
+// chunks (one column per thread, up to 8 per CTA) measured fastest on GB300
+// for 64 right-hand sides in both precisions: more independent look-back
+// chains, each with a short per-tile step.
 static void trsm_shape(int64_t m, int &mc, int &ny, int &cpt) {
-    mc = (int)std::min<int64_t>(kTrsmMaxCols, m);
-    ny = std::min(kTrsmMaxMc, mc);
-    cpt = (mc + ny - 1) / ny;
+    mc = (int)std::min<int64_t>(kTrsmMaxMc, m);
+    ny = mc;
+    cpt = 1;
 }
 
 template <typename T>
