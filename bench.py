@@ -208,7 +208,7 @@ def main():
     ap.add_argument("--cpu-sample-n", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI leg")
-    ap.add_argument("--update", default="fp16x3",
+    ap.add_argument("--update", default="bf16x6",
                     help="trailing-update form of the mixed path: fp32|bf16|bf16x3|bf16x6|fp16|fp16x3")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed steps of the plain FP64 leg")
     args = ap.parse_args()

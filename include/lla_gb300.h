@@ -222,7 +222,7 @@ enum lla_update {
 };
 
 typedef struct lla_refine_opts {
-    int32_t update;      /* lla_update (default LLA_UPDATE_FP16X3) */
+    int32_t update;      /* lla_update (default LLA_UPDATE_BF16X6) */
     int32_t max_iters;   /* refinement iterations before giving up (default 30) */
     double tol;          /* target normwise backward error (default 1e-13) */
     int32_t equilibrate; /* 1: symmetric power-of-two scaling (default) */

@@ -425,7 +425,7 @@ def trsm_device(L, B, trans, algo=ALGO_FAST, stream=None):
 
 # ---- mixed-precision refined solve (no counterpart in the reference) --------
 
-def refine_opts(update="fp16x3", max_iters=30, tol=1e-13, equilibrate=True, fallback=True, nb=0):
+def refine_opts(update="bf16x6", max_iters=30, tol=1e-13, equilibrate=True, fallback=True, nb=0):
     o = RefineOpts()
     lib.lla_refine_opts_default(ctypes.byref(o))
     o.update = UPDATE_NAMES[update] if isinstance(update, str) else int(update)
@@ -461,7 +461,7 @@ def posv_refined_device(A, B, X, stream=None, **kw):
     return r.as_dict()
 
 
-def spotrf_mixed_device(A, update="fp16x3", info=None, stream=None):
+def spotrf_mixed_device(A, update="bf16x6", info=None, stream=None):
     """Low-precision Cholesky of a column-major FP32 CUDA tensor in place (FP32
     diagonal blocks and panels, tensor-core trailing updates); returns the
     device int64 info tensor."""

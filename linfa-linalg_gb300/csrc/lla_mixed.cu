@@ -329,7 +329,7 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 extern "C" void lla_refine_opts_default(lla_refine_opts *o) {
     if (!o) return;
     std::memset(o, 0, sizeof(*o));
-    o->update = LLA_UPDATE_FP16X3;
+    o->update = LLA_UPDATE_BF16X6;
     o->max_iters = 30;
     o->tol = 1e-13;
     o->equilibrate = 1;
