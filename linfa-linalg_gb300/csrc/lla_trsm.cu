@@ -42,23 +42,19 @@ __device__ __forceinline__ void st_release(int *p, int v) {
     asm volatile("st.release.gpu.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-constexpr int kTrsmMaxCols = 64;  // RHS columns per CTA
-
-// Block (32 rows) x (up to 64 RHS columns) per CTA: thread (tx, ty) owns row
-// tx and columns ty + u * blockDim.y, u < cpt.
 template <typename T, bool kExact>
 __global__ void __launch_bounds__(256) trsm_lookback(const T *__restrict__ M, int64_t ld, int64_t n,
                                                      int lower, int trans,
                                                      const T *__restrict__ diag, T *B, int64_t ldb,
-                                                     int64_t m, int mc, int cpt, int n_chunks, int *ws,
+                                                     int64_t m, int mc, int n_chunks, int *ws,
                                                      int *err_word) {
     using Ar = Arith<T>;
     __shared__ T ts[kTrsmNb][kTrsmNb + 1];
-    __shared__ T xs[kTrsmMaxCols][kTrsmNb];
+    __shared__ T xs[kTrsmMaxMc][kTrsmNb];
     __shared__ T dg[kTrsmNb];
     __shared__ int s_ticket, s_abort;
-    const int tx = threadIdx.x, ty = threadIdx.y, ny = blockDim.y;
-    const int tid = ty * kTrsmNb + tx, nthr = kTrsmNb * ny;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * kTrsmNb + tx, nthr = kTrsmNb * blockDim.y;
     int *counter = ws, *flags = ws + 1;
     if (tid == 0) {
         s_ticket = atomicAdd(counter, 1);
@@ -67,20 +63,14 @@ __global__ void __launch_bounds__(256) trsm_lookback(const T *__restrict__ M, in
     __syncthreads();
     const int64_t rb = s_ticket / n_chunks;
     const int cc = s_ticket % n_chunks;
+    const int64_t col = (int64_t)cc * mc + ty;
+    const bool col_ok = ty < mc && col < m;
     auto row_of = [&](int64_t t) -> int64_t { return lower ? t : n - 1 - t; };
     auto tval = [&](int64_t r, int64_t c) -> T { return trans ? M[c + r * ld] : M[r + c * ld]; };
     const int64_t t_own = rb * kTrsmNb + tx;
     const bool row_ok = t_own < n;
     const int64_t r_own = row_ok ? row_of(t_own) : 0;
-    T bv[kTrsmMaxMc];
-    bool cok[kTrsmMaxMc];
-#pragma unroll
-    for (int u = 0; u < kTrsmMaxMc; ++u) {
-        const int lc = ty + u * ny;
-        const int64_t col = (int64_t)cc * mc + lc;
-        cok[u] = u < cpt && lc < mc && col < m;
-        bv[u] = (row_ok && cok[u]) ? B[r_own + col * ldb] : T(0);
-    }
+    T bv = (row_ok && col_ok) ? B[r_own + col * ldb] : T(0);
 
     for (int64_t q = 0; q < rb; ++q) {
         if (tid == 0) {
@@ -114,20 +104,13 @@ __global__ void __launch_bounds__(256) trsm_lookback(const T *__restrict__ M, in
             ts[x][y] = (tr < n) ? tval(row_of(tr), row_of(q * kTrsmNb + y)) : T(0);
         }
         __syncthreads();
-        if (row_ok) {
-#pragma unroll 4
+        if (row_ok && col_ok) {
+#pragma unroll 8
             for (int y = 0; y < kTrsmNb; ++y) {
-                const T t = ts[tx][y];
-#pragma unroll
-                for (int u = 0; u < kTrsmMaxMc; ++u) {
-                    if (cok[u]) {
-                        const T x = xs[ty + u * ny][y];
-                        if (kExact)
-                            bv[u] = Ar::sub(bv[u], Ar::mul(x, t));
-                        else
-                            bv[u] = Ar::fma_(-x, t, bv[u]);
-                    }
-                }
+                if (kExact)
+                    bv = Ar::sub(bv, Ar::mul(xs[ty][y], ts[tx][y]));
+                else
+                    bv = Ar::fma_(-xs[ty][y], ts[tx][y], bv);
             }
         }
         __syncthreads();
@@ -149,77 +132,49 @@ __global__ void __launch_bounds__(256) trsm_lookback(const T *__restrict__ M, in
         __syncthreads();
         for (int y = 0; y < bs; ++y) {
             if (tx == y) {
-#pragma unroll
-                for (int u = 0; u < kTrsmMaxMc; ++u) {
-                    if (u < cpt) {
-                        const T xv = Ar::div(bv[u], dg[y]);  // coeff = b[i,k] / diag  (:117-119)
-                        bv[u] = xv;
-                        if (ty + u * ny < kTrsmMaxCols) xs[ty + u * ny][y] = xv;
-                    }
-                }
+                const T xv = Ar::div(bv, dg[y]);  // coeff = b[i,k] / diag  (:117-119)
+                bv = xv;
+                xs[ty][y] = xv;
             }
             __syncthreads();
             if (tx > y && tx < bs) {
-                const T t = ts[tx][y];
-#pragma unroll
-                for (int u = 0; u < kTrsmMaxMc; ++u) {
-                    if (cok[u]) {
-                        const T x = xs[ty + u * ny][y];
-                        if (kExact)
-                            bv[u] = Ar::sub(bv[u], Ar::mul(x, t));
-                        else
-                            bv[u] = Ar::fma_(-x, t, bv[u]);
-                    }
-                }
+                if (kExact)
+                    bv = Ar::sub(bv, Ar::mul(xs[ty][y], ts[tx][y]));
+                else
+                    bv = Ar::fma_(-xs[ty][y], ts[tx][y], bv);
             }
         }
     }
-    if (row_ok) {
-#pragma unroll
-        for (int u = 0; u < kTrsmMaxMc; ++u)
-            if (cok[u]) B[r_own + ((int64_t)cc * mc + ty + u * ny) * ldb] = bv[u];
-    }
+    if (row_ok && col_ok) B[r_own + col * ldb] = bv;
     __threadfence();
     __syncthreads();
     if (tid == 0) st_release(flags + rb * n_chunks + cc, 1);
-}
-
-// Columns per CTA and per thread of the look-back solve.  Narrow column
-// chunks (one column per thread, up to 8 per CTA) measured fastest on GB300
-// for 64 right-hand sides in both precisions: more independent look-back
-// chains, each with a short per-tile step.
-static void trsm_shape(int64_t m, int &mc, int &ny, int &cpt) {
-    mc = (int)std::min<int64_t>(kTrsmMaxMc, m);
-    ny = mc;
-    cpt = 1;
 }
 
 template <typename T>
 int trsm_launch(const T *M, int64_t ld, int64_t n, int lower, int trans, const T *diag, T *B,
                 int64_t ldb, int64_t m, bool exact, int *ws, int *err_word, cudaStream_t st) {
     if (n == 0 || m == 0) return 0;
-    int mc, ny, cpt;
-    trsm_shape(m, mc, ny, cpt);
+    const int mc = (int)std::min<int64_t>(kTrsmMaxMc, m);
     const int64_t chunks = ceil_div(m, mc);
     const int64_t R = ceil_div(n, kTrsmNb);
     if (cudaMemsetAsync(ws, 0, sizeof(int) * (1 + R * chunks), st) != cudaSuccess) return -1;
-    const dim3 block(kTrsmNb, ny);
+    const dim3 block(kTrsmNb, mc);
     const unsigned grid = (unsigned)(R * chunks);
     // algorithmic work: n^2 * m flops (n(n-1)/2 multiply-adds and n divisions per column)
     LaunchScope ls(K_TRSM, st, (double)n * n * m);
     if (exact)
         trsm_lookback<T, true><<<grid, block, 0, st>>>(M, ld, n, lower, trans, diag, B, ldb, m, mc,
-                                                       cpt, (int)chunks, ws, err_word);
+                                                       (int)chunks, ws, err_word);
     else
         trsm_lookback<T, false><<<grid, block, 0, st>>>(M, ld, n, lower, trans, diag, B, ldb, m,
-                                                        mc, cpt, (int)chunks, ws, err_word);
+                                                        mc, (int)chunks, ws, err_word);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 size_t trsm_ws_ints(int64_t n, int64_t m) {
     if (n == 0 || m == 0) return 1;
-    int mc, ny, cpt;
-    trsm_shape(m, mc, ny, cpt);
+    const int mc = (int)std::min<int64_t>(kTrsmMaxMc, m);
     return (size_t)(1 + ceil_div(n, kTrsmNb) * ceil_div(m, mc));
 }
 
@@ -311,11 +266,11 @@ extern "C" int lla_dtrsm_device_noalloc(const double *dL, int64_t n, int64_t ld,
     const int lower = trans ? 0 : 1;
     if (algo == LLA_ALGO_EXACT)
         trsm_lookback<double, true><<<grid, block, 0, st>>>(dL, ld, n, lower, trans ? 1 : 0,
-                                                            nullptr, dB, ldb, m, mc, 1, (int)chunks,
+                                                            nullptr, dB, ldb, m, mc, (int)chunks,
                                                             scratch, err_word);
     else
         trsm_lookback<double, false><<<grid, block, 0, st>>>(dL, ld, n, lower, trans ? 1 : 0,
-                                                             nullptr, dB, ldb, m, mc, 1, (int)chunks,
+                                                             nullptr, dB, ldb, m, mc, (int)chunks,
                                                              scratch, err_word);
     e = cudaGetLastError();
     if (e != cudaSuccess) return lla__set_cuda_error(err, e);
