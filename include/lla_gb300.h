@@ -268,6 +268,45 @@ int lla_dposv_refined(const double *a, int64_t rows, int64_t cols, int64_t rs, i
 int lla_spotrf_mixed_device(float *dA, int64_t n, int64_t ld, int update, int64_t *d_info,
                             void *stream, lla_error *err);
 
+/* ---- batched solves of many small SPD systems (no counterpart in the
+ * reference; one persistent launch for the whole batch) --------------------
+ * Systems of order n_i <= 256 with m_i <= 8 right-hand sides.  The plan fixes
+ * where each system lives in two device pools the caller fills: A_i
+ * (n_i x n_i, column-major, ld = n_i) at A-pool element offset a_off[i], B_i
+ * (n_i x m_i, ld = n_i) at b_off[i].  A solve factors every A_i in place (L in
+ * the lower triangle) and overwrites every B_i with X_i; d_info[i] (device
+ * int32) receives -1 or the first row with a non-positive pivot of system i.
+ * Plain FP64 (or FP32) arithmetic with FMA, as the single-matrix FAST path. */
+typedef struct lla_batch_plan lla_batch_plan;
+
+/* elem_bytes: 8 (f64) or 4 (f32).  LLA_ERR_TOO_LARGE for n_i > 256 or
+ * m_i > 8.  Picks up a cached launch shape for this batch's size histogram
+ * when the autotune cache has one. */
+int lla_batch_plan_create(int64_t count, const int32_t *n, const int32_t *m, int elem_bytes,
+                          lla_batch_plan **plan, lla_error *err);
+void lla_batch_plan_destroy(lla_batch_plan *plan);
+/* Pool sizes in elements, per-system offsets (arrays of `count`, may be NULL),
+ * the launch shape in use and the batch's flop count. */
+int lla_batch_plan_info(const lla_batch_plan *plan, int64_t *a_elems, int64_t *b_elems,
+                        int64_t *a_off, int64_t *b_off, int *ctas_per_sm, int *threads,
+                        double *flops);
+/* Overrides the launch shape (CTAs per SM 1..8, threads 128 or 256). */
+int lla_batch_set_shape(lla_batch_plan *plan, int ctas_per_sm, int threads);
+/* One persistent launch on `stream` (asynchronous). */
+int lla_dbatch_posv_device(lla_batch_plan *plan, double *dA, double *dB, int32_t *d_info,
+                           void *stream, lla_error *err);
+int lla_sbatch_posv_device(lla_batch_plan *plan, float *dA, float *dB, int32_t *d_info,
+                           void *stream, lla_error *err);
+/* The same launch replayed from a CUDA graph instantiated on first use for
+ * these pools and stream (either element type). */
+int lla_batch_posv_graph(lla_batch_plan *plan, void *dA, void *dB, int32_t *d_info, void *stream,
+                         lla_error *err);
+/* Times the launch shapes on this batch (restoring the pools between trials),
+ * keeps the fastest and records it in the autotune cache file
+ * (LLA_AUTOTUNE_CACHE or ~/.cache/lla_gb300_autotune.txt). */
+int lla_batch_autotune(lla_batch_plan *plan, void *dA, void *dB, int32_t *d_info, void *stream,
+                       double *best_ms, lla_error *err);
+
 /* ---- diagnostics (no counterpart in the reference) ----------------------
  * Launch accounting and per-kernel CUDA-event timing used by the benchmark:
  * while profiling is on, every kernel launch is bracketed by an event pair on

@@ -110,6 +110,19 @@ EXPORTS = {
                           ctypes.c_int),
     "lla_spotrf_mixed_device": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
                                  ctypes.c_void_p, ctypes.c_void_p, _E], ctypes.c_int),
+    "lla_batch_plan_create": ([ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                               ctypes.POINTER(ctypes.c_void_p), _E], ctypes.c_int),
+    "lla_batch_plan_destroy": ([ctypes.c_void_p], None),
+    "lla_batch_plan_info": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
+                             ctypes.POINTER(ctypes.c_int64), ctypes.c_void_p, ctypes.c_void_p,
+                             ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                             ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    "lla_batch_set_shape": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "lla_dbatch_posv_device": ([ctypes.c_void_p] * 5 + [_E], ctypes.c_int),
+    "lla_sbatch_posv_device": ([ctypes.c_void_p] * 5 + [_E], ctypes.c_int),
+    "lla_batch_posv_graph": ([ctypes.c_void_p] * 5 + [_E], ctypes.c_int),
+    "lla_batch_autotune": ([ctypes.c_void_p] * 5 + [ctypes.POINTER(ctypes.c_double), _E],
+                           ctypes.c_int),
 }
 for _p in "ds":
     EXPORTS.update({
@@ -476,3 +489,88 @@ def spotrf_mixed_device(A, update="bf16x6", info=None, stream=None):
                                 ctypes.c_void_p(info.data_ptr()), _stream_ptr(stream), ctypes.byref(e))
     _raise(e)
     return info
+
+
+# ---- batched solves of many small systems (no counterpart in the reference) --
+
+class BatchPlan:
+    """Packs `count` SPD systems (orders n[i] <= 256, m[i] <= 8 right-hand
+    sides) into two device pools and solves them all in one persistent launch.
+    Use pack() to copy host matrices into pools, solve() / solve_graph() to run,
+    unpack_x() to read the solutions."""
+
+    def __init__(self, n, m, dtype="f64"):
+        self.n = np.ascontiguousarray(n, dtype=np.int32)
+        self.m = np.ascontiguousarray(m, dtype=np.int32)
+        self.count = len(self.n)
+        self.elem = 8 if dtype in ("f64", np.float64) else 4
+        self.np_dtype = np.float64 if self.elem == 8 else np.float32
+        h = ctypes.c_void_p()
+        e = Error()
+        lib.lla_batch_plan_create(self.count, ctypes.c_void_p(self.n.ctypes.data),
+                                  ctypes.c_void_p(self.m.ctypes.data), self.elem, ctypes.byref(h),
+                                  ctypes.byref(e))
+        _raise(e)
+        self.h = h
+        ae, be = ctypes.c_int64(), ctypes.c_int64()
+        self.a_off = np.zeros(self.count, dtype=np.int64)
+        self.b_off = np.zeros(self.count, dtype=np.int64)
+        lib.lla_batch_plan_info(h, ctypes.byref(ae), ctypes.byref(be),
+                                ctypes.c_void_p(self.a_off.ctypes.data),
+                                ctypes.c_void_p(self.b_off.ctypes.data), None, None, None)
+        self.a_elems, self.b_elems = ae.value, be.value
+
+    def shape(self):
+        c, t, f = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        lib.lla_batch_plan_info(self.h, None, None, None, None, ctypes.byref(c), ctypes.byref(t),
+                                ctypes.byref(f))
+        return {"ctas_per_sm": c.value, "threads": t.value, "flops": f.value}
+
+    def set_shape(self, ctas_per_sm, threads):
+        if lib.lla_batch_set_shape(self.h, ctas_per_sm, threads):
+            raise ValueError((ctas_per_sm, threads))
+
+    def pack(self, As, Bs):
+        """Host pools (numpy) holding the column-major A_i and B_i."""
+        ap = np.zeros(self.a_elems, dtype=self.np_dtype)
+        bp = np.zeros(self.b_elems, dtype=self.np_dtype)
+        for i, (a, b) in enumerate(zip(As, Bs)):
+            n, m = self.n[i], self.m[i]
+            ap[self.a_off[i]:self.a_off[i] + n * n] = np.asarray(a, self.np_dtype).ravel(order="F")
+            bp[self.b_off[i]:self.b_off[i] + n * m] = np.asarray(b, self.np_dtype).ravel(order="F")
+        return ap, bp
+
+    def unpack_x(self, bp):
+        return [np.asarray(bp[self.b_off[i]:self.b_off[i] + self.n[i] * self.m[i]]).reshape(
+            (self.n[i], self.m[i]), order="F") for i in range(self.count)]
+
+    def _call(self, name, dA, dB, info, stream):
+        e = Error()
+        getattr(lib, name)(self.h, ctypes.c_void_p(dA.data_ptr()), ctypes.c_void_p(dB.data_ptr()),
+                           ctypes.c_void_p(info.data_ptr()), _stream_ptr(stream), ctypes.byref(e))
+        _raise(e)
+
+    def solve(self, dA, dB, info, stream=None):
+        """dA, dB: device tensors of the pools; info: int32 device tensor (count)."""
+        self._call("lla_dbatch_posv_device" if self.elem == 8 else "lla_sbatch_posv_device",
+                   dA, dB, info, stream)
+
+    def solve_graph(self, dA, dB, info, stream=None):
+        self._call("lla_batch_posv_graph", dA, dB, info, stream)
+
+    def autotune(self, dA, dB, info, stream=None):
+        e = Error()
+        ms = ctypes.c_double()
+        lib.lla_batch_autotune(self.h, ctypes.c_void_p(dA.data_ptr()), ctypes.c_void_p(dB.data_ptr()),
+                               ctypes.c_void_p(info.data_ptr()), _stream_ptr(stream),
+                               ctypes.byref(ms), ctypes.byref(e))
+        _raise(e)
+        return ms.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib.lla_batch_plan_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass

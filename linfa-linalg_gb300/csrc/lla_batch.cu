@@ -1,0 +1,562 @@
+// lla_batch.cu -- thousands of independent SPD systems of uneven order in one
+// persistent launch.
+//
+// Layout: the caller packs every system's A_i (n_i x n_i, column-major,
+// ld = n_i) into one "A pool" and every B_i (n_i x m_i, ld = n_i) into a "B
+// pool" at offsets chosen by the plan.  A plan sorts the systems by
+// decreasing cost (n^3/3 + 2 n^2 m) into a device work list; a persistent
+// kernel of (CTAs per SM) x (#SMs) blocks takes items from an atomic counter
+// (largest first, so the tail is short) and, inside one CTA per system:
+//   * factors A_i in place, right-looking with 32-column blocks: one warp
+//     factors the diagonal block with register shuffles, one thread per row
+//     solves the rows below it into a shared-memory panel, all threads update
+//     the trailing lower triangle from that panel (L2-resident);
+//   * solves L L^T X = B in place, 32-row blocks: one warp per right-hand side
+//     solves each diagonal block with shuffles, all threads update the rows
+//     below (above) from it.
+// A non-positive pivot stops that system only: info[i] = first failing row
+// (-1 when the system solved).  The (CTAs per SM, threads) shape is chosen per
+// batch by lla_batch_autotune and cached on disk.
+#include <cuda_runtime.h>
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/lla_gb300.h"
+#include "lla_common.cuh"
+#include "lla_prof.h"
+
+namespace lla {
+
+struct BatchItem {
+    int32_t n, m, idx, pad;
+    int64_t a_off, b_off;
+};
+
+constexpr int kBNb = 32;          // block width
+constexpr int kBMaxN = 256;       // largest order a batch system may have
+constexpr int kBMaxRhs = 8;       // right-hand sides per system
+
+template <typename T>
+__device__ __forceinline__ T shfl(T v, int src) {
+    return __shfl_sync(0xffffffffu, v, src);
+}
+
+// One warp: Cholesky of the bs x bs block at sD (row-major [32][33] in shared
+// memory); returns the first failing local row or -1.  Lane i holds row i.
+template <typename T>
+__device__ int warp_potrf32(T *sD, int bs, int lane) {
+    T v[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) v[c] = (lane < bs && c <= lane) ? sD[lane * 33 + c] : T(0);
+    int fail = -1;
+#pragma unroll
+    for (int c = 0; c < 32; ++c) {
+        if (c < bs && fail < 0) {
+            const T piv = shfl(v[c], c);
+            if (!(piv > T(0))) {
+                fail = c;  // non-positive pivot (NaN does not fail, as in the reference: `d <= 0`)
+                if (piv != piv) fail = -1;
+            }
+            if (fail < 0) {
+                const T lcc = sqrt(piv);
+                if (lane == c) v[c] = lcc;
+                if (lane > c) v[c] = v[c] / lcc;
+#pragma unroll
+                for (int c2 = c + 1; c2 < 32; ++c2) {
+                    const T t = shfl(v[c], c2);
+                    if (c2 < bs && lane >= c2) v[c2] = fma(-v[c], t, v[c2]);
+                }
+            }
+        }
+    }
+    if (lane < bs) {
+#pragma unroll
+        for (int c = 0; c < 32; ++c)
+            if (c <= lane) sD[lane * 33 + c] = v[c];
+    }
+    return fail;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256, 2) batch_posv_kernel(const BatchItem *__restrict__ items, int64_t count, T *Apool,
+                                  T *Bpool, int32_t *info, int *counter) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sD = (T *)smem_raw;  // [32][33] diagonal block
+    T *sP = sD + 32 * 33;   // [kBMaxN][33] panel / block rows (row r at sP[r * 33])
+    __shared__ int s_item, s_fail;
+    const int tid = threadIdx.x, nthr = blockDim.x, warp = tid >> 5, lane = tid & 31;
+    const int nwarps = nthr >> 5;
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(counter, 1);
+        __syncthreads();
+        const int64_t it = s_item;
+        if (it >= count) break;
+        const BatchItem w = items[it];
+        const int n = w.n, m = w.m;
+        T *A = Apool + w.a_off;
+        T *B = Bpool + w.b_off;
+        if (tid == 0) s_fail = -1;
+        // ---- factor: right-looking, 32-column blocks ----
+        for (int kb = 0; kb < n; kb += kBNb) {
+            const int bs = min(kBNb, n - kb);
+            for (int e = tid; e < 32 * 32; e += nthr) {
+                const int r = e % 32, c = e / 32;
+                if (r < bs && c <= r) sD[r * 33 + c] = A[(kb + r) + (int64_t)(kb + c) * n];
+            }
+            __syncthreads();
+            if (warp == 0) {
+                const int f = warp_potrf32(sD, bs, lane);
+                if (lane == 0 && f >= 0) s_fail = kb + f;
+            }
+            __syncthreads();
+            if (s_fail >= 0) break;
+            for (int e = tid; e < 32 * 32; e += nthr) {
+                const int r = e % 32, c = e / 32;
+                if (r < bs && c <= r) A[(kb + r) + (int64_t)(kb + c) * n] = sD[r * 33 + c];
+            }
+            // panel: each row below the block solves against L_kk
+            const int q = kb + bs, rows = n - q;
+            for (int rr = tid; rr < rows; rr += nthr) {
+                const int r = q + rr;
+                T v[32];
+#pragma unroll
+                for (int c = 0; c < 32; ++c) v[c] = (c < bs) ? A[r + (int64_t)(kb + c) * n] : T(0);
+#pragma unroll
+                for (int c = 0; c < 32; ++c) {
+                    if (c < bs) {
+                        v[c] = v[c] / sD[c * 33 + c];
+#pragma unroll
+                        for (int c2 = c + 1; c2 < 32; ++c2)
+                            if (c2 < bs) v[c2] = fma(-v[c], sD[c2 * 33 + c], v[c2]);
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 32; ++c) {
+                    if (c < bs) {
+                        sP[rr * 33 + c] = v[c];
+                        A[r + (int64_t)(kb + c) * n] = v[c];
+                    }
+                }
+            }
+            __syncthreads();
+            // trailing lower triangle, one column per warp, lanes over rows:
+            // A[i,j] -= sum_t P[i][t] P[j][t]
+            for (int j = warp; j < rows; j += nwarps) {
+                for (int i = j + lane; i < rows; i += 32) {
+                    T acc = A[(q + i) + (int64_t)(q + j) * n];
+#pragma unroll 8
+                    for (int t = 0; t < bs; ++t) acc = fma(-sP[i * 33 + t], sP[j * 33 + t], acc);
+                    A[(q + i) + (int64_t)(q + j) * n] = acc;
+                }
+            }
+            __syncthreads();
+        }
+        if (s_fail >= 0) {
+            if (tid == 0) info[w.idx] = s_fail;
+            __syncthreads();
+            continue;
+        }
+        // ---- solve L y = b (forward), then L^T x = y (backward), 32-row blocks ----
+        for (int pass = 0; pass < 2; ++pass) {
+            const bool fwd = pass == 0;
+            const int nblk = (n + kBNb - 1) / kBNb;
+            for (int bi = 0; bi < nblk; ++bi) {
+                const int kb = (fwd ? bi : nblk - 1 - bi) * kBNb;
+                const int bs = min(kBNb, n - kb);
+                for (int e = tid; e < 32 * 32; e += nthr) {
+                    const int r = e % 32, c = e / 32;
+                    if (r < bs && c <= r) sD[r * 33 + c] = A[(kb + r) + (int64_t)(kb + c) * n];
+                }
+                __syncthreads();
+                // warp k solves right-hand side k on this block (lane = row)
+                for (int k = warp; k < m; k += nwarps) {
+                    T x = (lane < bs) ? B[(kb + lane) + (int64_t)k * n] : T(0);
+                    if (fwd) {
+#pragma unroll
+                        for (int c = 0; c < 32; ++c) {
+                            if (c < bs) {
+                                const T xc = shfl(x, c) / sD[c * 33 + c];
+                                if (lane == c) x = xc;
+                                if (lane > c && lane < bs) x = fma(-xc, sD[lane * 33 + c], x);
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int cc = 31; cc >= 0; --cc) {
+                            if (cc < bs) {
+                                const T xc = shfl(x, cc) / sD[cc * 33 + cc];
+                                if (lane == cc) x = xc;
+                                if (lane < cc) x = fma(-xc, sD[cc * 33 + lane], x);
+                            }
+                        }
+                    }
+                    if (lane < bs) B[(kb + lane) + (int64_t)k * n] = x;
+                }
+                // stage the block's coupling to the remaining rows: forward needs
+                // L[r][kb+t] for r >= kb+bs, backward L[kb+t][r] for r < kb
+                const int q = fwd ? kb + bs : 0, rows = fwd ? n - kb - bs : kb;
+                for (int e = tid; e < rows * bs; e += nthr) {
+                    if (fwd) {
+                        const int rr = e % rows, t = e / rows;  // consecutive rr: contiguous column
+                        sP[rr * 33 + t] = A[(q + rr) + (int64_t)(kb + t) * n];
+                    } else {
+                        const int t = e % bs, rr = e / bs;  // consecutive t: contiguous column rr
+                        sP[rr * 33 + t] = A[(kb + t) + (int64_t)rr * n];
+                    }
+                }
+                __syncthreads();
+                for (int e = tid; e < rows * m; e += nthr) {
+                    const int rr = e % rows, k = e / rows;
+                    T acc = B[(q + rr) + (int64_t)k * n];
+#pragma unroll 8
+                    for (int t = 0; t < bs; ++t)
+                        acc = fma(-sP[rr * 33 + t], B[(kb + t) + (int64_t)k * n], acc);
+                    B[(q + rr) + (int64_t)k * n] = acc;
+                }
+                __syncthreads();
+            }
+        }
+        if (tid == 0) info[w.idx] = -1;
+        __syncthreads();
+    }
+}
+
+}  // namespace lla
+
+// ---------------------------------------------------------------------------
+// plan, autotune cache, launch
+
+using namespace lla;
+
+struct lla_batch_plan {
+    int64_t count = 0;
+    int dtype = 8;
+    std::vector<int32_t> n, m;
+    std::vector<int64_t> a_off, b_off;
+    int64_t a_elems = 0, b_elems = 0;
+    double flops = 0.0;
+    BatchItem *d_items = nullptr;
+    int *d_counter = nullptr;
+    int ctas_per_sm = 2, threads = 256;
+    bool tuned = false;
+    std::string key;
+    // graph replay cache
+    cudaGraphExec_t gexec = nullptr;
+    void *g_a = nullptr, *g_b = nullptr, *g_info = nullptr;
+    cudaStream_t g_stream = nullptr;
+};
+
+static size_t batch_smem(int dtype) { return (size_t)dtype * (32 * 33 + (size_t)kBMaxN * 33); }
+
+static std::string cache_path() {
+    const char *p = std::getenv("LLA_AUTOTUNE_CACHE");
+    if (p && *p) return p;
+    const char *h = std::getenv("HOME");
+    return std::string(h ? h : "/tmp") + "/.cache/lla_gb300_autotune.txt";
+}
+
+static std::mutex g_cache_mu;
+
+static bool cache_lookup(const std::string &key, int &cps, int &thr) {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    FILE *f = std::fopen(cache_path().c_str(), "r");
+    if (!f) return false;
+    char k[512];
+    int a, b;
+    bool found = false;
+    while (std::fscanf(f, "%511s %d %d", k, &a, &b) == 3)
+        if (key == k) {
+            cps = a;
+            thr = b;
+            found = true;
+        }
+    std::fclose(f);
+    return found;
+}
+
+static void cache_store(const std::string &key, int cps, int thr) {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    const std::string path = cache_path();
+    const size_t slash = path.rfind('/');
+    if (slash != std::string::npos) {
+        const std::string dir = path.substr(0, slash);
+        for (size_t i = 1; i <= dir.size(); ++i)
+            if (i == dir.size() || dir[i] == '/') (void)mkdir(dir.substr(0, i).c_str(), 0755);
+    }
+    FILE *f = std::fopen(path.c_str(), "a");
+    if (!f) return;
+    std::fprintf(f, "%s %d %d\n", key.c_str(), cps, thr);
+    std::fclose(f);
+}
+
+static int sm_count() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return sms;
+}
+
+template <typename T>
+static cudaError_t batch_launch(lla_batch_plan *p, T *dA, T *dB, int32_t *d_info, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(p->d_counter, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    const size_t smem = batch_smem(sizeof(T));
+    const unsigned grid = (unsigned)std::max<int64_t>(
+        1, std::min<int64_t>(p->count, (int64_t)p->ctas_per_sm * sm_count()));
+    LaunchScope ls(K_BATCH, st, p->flops);
+    batch_posv_kernel<T><<<grid, p->threads, smem, st>>>(p->d_items, p->count, dA, dB, d_info,
+                                                         p->d_counter);
+    return cudaGetLastError();
+}
+
+extern "C" {
+
+int lla_batch_plan_create(int64_t count, const int32_t *n, const int32_t *m, int elem_bytes,
+                          lla_batch_plan **out, lla_error *err) {
+    if (!out || count < 0 || (count > 0 && (!n || !m)) || (elem_bytes != 4 && elem_bytes != 8))
+        return lla__set_status(err, LLA_ERR_INVALID_ARG);
+    for (int64_t i = 0; i < count; ++i) {
+        if (n[i] < 0 || m[i] < 0) return lla__set_status(err, LLA_ERR_INVALID_ARG);
+        if (n[i] > kBMaxN || m[i] > kBMaxRhs) return lla__set_status(err, LLA_ERR_TOO_LARGE);
+    }
+    lla__set_status(err, LLA_OK);
+    lla_batch_plan *p = new lla_batch_plan();
+    p->count = count;
+    p->dtype = elem_bytes;
+    p->n.assign(n, n + count);
+    p->m.assign(m, m + count);
+    p->a_off.resize(count);
+    p->b_off.resize(count);
+    // pools in submission order, each system 16-byte aligned
+    const int64_t align = 16 / elem_bytes;
+    int64_t ao = 0, bo = 0;
+    int hist[9] = {0};
+    int maxm = 0;
+    for (int64_t i = 0; i < count; ++i) {
+        p->a_off[i] = ao;
+        p->b_off[i] = bo;
+        ao += ((int64_t)n[i] * n[i] + align - 1) / align * align;
+        bo += ((int64_t)n[i] * m[i] + align - 1) / align * align;
+        p->flops += (double)n[i] * n[i] * n[i] / 3.0 + 2.0 * n[i] * n[i] * m[i];
+        int b = 0;
+        while ((32 << b) < n[i] && b < 8) ++b;
+        hist[b]++;
+        maxm = std::max(maxm, (int)m[i]);
+    }
+    p->a_elems = ao;
+    p->b_elems = bo;
+    // work list: largest systems first
+    std::vector<BatchItem> items(count);
+    for (int64_t i = 0; i < count; ++i)
+        items[i] = BatchItem{n[i], m[i], (int32_t)i, 0, p->a_off[i], p->b_off[i]};
+    std::stable_sort(items.begin(), items.end(), [](const BatchItem &a, const BatchItem &b) {
+        const double ca = (double)a.n * a.n * (a.n + 6.0 * a.m), cb = (double)b.n * b.n * (b.n + 6.0 * b.m);
+        return ca > cb;
+    });
+    // autotune-cache key: element size, count, size-bucket histogram, widest RHS
+    char key[256];
+    std::snprintf(key, sizeof(key), "b%d:c%lld:h%d-%d-%d-%d-%d-%d-%d-%d-%d:m%d", elem_bytes,
+                  (long long)count, hist[0], hist[1], hist[2], hist[3], hist[4], hist[5], hist[6],
+                  hist[7], hist[8], maxm);
+    p->key = key;
+    int cps, thr;
+    if (cache_lookup(p->key, cps, thr)) {
+        p->ctas_per_sm = cps;
+        p->threads = thr;
+        p->tuned = true;
+    }
+    cudaError_t e = cudaMalloc(&p->d_items, sizeof(BatchItem) * std::max<int64_t>(1, count));
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_counter, sizeof(int));
+    if (e == cudaSuccess && count > 0)
+        e = cudaMemcpy(p->d_items, items.data(), sizeof(BatchItem) * count, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        const size_t smem = batch_smem(elem_bytes);
+        e = elem_bytes == 8 ? cudaFuncSetAttribute(batch_posv_kernel<double>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                            : cudaFuncSetAttribute(batch_posv_kernel<float>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
+    if (e != cudaSuccess) {
+        cudaFree(p->d_items);
+        cudaFree(p->d_counter);
+        delete p;
+        return lla__set_cuda_error(err, e);
+    }
+    *out = p;
+    return LLA_OK;
+}
+
+void lla_batch_plan_destroy(lla_batch_plan *p) {
+    if (!p) return;
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    cudaFree(p->d_items);
+    cudaFree(p->d_counter);
+    delete p;
+}
+
+int lla_batch_plan_info(const lla_batch_plan *p, int64_t *a_elems, int64_t *b_elems, int64_t *a_off,
+                        int64_t *b_off, int *ctas_per_sm, int *threads, double *flops) {
+    if (!p) return LLA_ERR_INVALID_ARG;
+    if (a_elems) *a_elems = p->a_elems;
+    if (b_elems) *b_elems = p->b_elems;
+    if (a_off) std::memcpy(a_off, p->a_off.data(), sizeof(int64_t) * p->count);
+    if (b_off) std::memcpy(b_off, p->b_off.data(), sizeof(int64_t) * p->count);
+    if (ctas_per_sm) *ctas_per_sm = p->ctas_per_sm;
+    if (threads) *threads = p->threads;
+    if (flops) *flops = p->flops;
+    return LLA_OK;
+}
+
+int lla_batch_set_shape(lla_batch_plan *p, int ctas_per_sm, int threads) {
+    if (!p || ctas_per_sm < 1 || ctas_per_sm > 8 || (threads != 128 && threads != 256))
+        return LLA_ERR_INVALID_ARG;
+    if (p->ctas_per_sm != ctas_per_sm || p->threads != threads) {
+        p->ctas_per_sm = ctas_per_sm;
+        p->threads = threads;
+        if (p->gexec) {
+            cudaGraphExecDestroy(p->gexec);
+            p->gexec = nullptr;
+        }
+    }
+    return LLA_OK;
+}
+
+static int batch_posv(lla_batch_plan *p, void *dA, void *dB, int32_t *d_info, void *stream,
+                      lla_error *err, int elem_bytes) {
+    if (!p || p->dtype != elem_bytes || (p->count > 0 && (!dA || !dB || !d_info)))
+        return lla__set_status(err, LLA_ERR_INVALID_ARG);
+    lla__set_status(err, LLA_OK);
+    if (p->count == 0) return LLA_OK;
+    cudaError_t e = elem_bytes == 8
+                        ? batch_launch<double>(p, (double *)dA, (double *)dB, d_info, (cudaStream_t)stream)
+                        : batch_launch<float>(p, (float *)dA, (float *)dB, d_info, (cudaStream_t)stream);
+    return e == cudaSuccess ? LLA_OK : lla__set_cuda_error(err, e);
+}
+
+int lla_dbatch_posv_device(lla_batch_plan *p, double *dA, double *dB, int32_t *d_info, void *stream,
+                           lla_error *err) {
+    return batch_posv(p, dA, dB, d_info, stream, err, 8);
+}
+
+int lla_sbatch_posv_device(lla_batch_plan *p, float *dA, float *dB, int32_t *d_info, void *stream,
+                           lla_error *err) {
+    return batch_posv(p, dA, dB, d_info, stream, err, 4);
+}
+
+// Same work as lla_?batch_posv_device, replayed from a CUDA graph: the first
+// call for a given (pools, info, stream) captures [counter reset, persistent
+// kernel] and instantiates it; later calls launch the executable graph.
+int lla_batch_posv_graph(lla_batch_plan *p, void *dA, void *dB, int32_t *d_info, void *stream,
+                         lla_error *err) {
+    if (!p || (p->count > 0 && (!dA || !dB || !d_info))) return lla__set_status(err, LLA_ERR_INVALID_ARG);
+    lla__set_status(err, LLA_OK);
+    if (p->count == 0) return LLA_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e;
+    if (!p->gexec || p->g_a != dA || p->g_b != dB || p->g_info != d_info || p->g_stream != st) {
+        if (p->gexec) {
+            cudaGraphExecDestroy(p->gexec);
+            p->gexec = nullptr;
+        }
+        cudaStream_t cap = nullptr;
+        if ((e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking)) != cudaSuccess)
+            return lla__set_cuda_error(err, e);
+        cudaGraph_t g = nullptr;
+        e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            const cudaError_t le = p->dtype == 8
+                                       ? batch_launch<double>(p, (double *)dA, (double *)dB, d_info, cap)
+                                       : batch_launch<float>(p, (float *)dA, (float *)dB, d_info, cap);
+            e = cudaStreamEndCapture(cap, &g);
+            if (le != cudaSuccess) e = le;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&p->gexec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        cudaStreamDestroy(cap);
+        if (e != cudaSuccess) return lla__set_cuda_error(err, e);
+        p->g_a = dA;
+        p->g_b = dB;
+        p->g_info = d_info;
+        p->g_stream = st;
+    }
+    e = cudaGraphLaunch(p->gexec, st);
+    return e == cudaSuccess ? LLA_OK : lla__set_cuda_error(err, e);
+}
+
+// Times every (CTAs per SM, threads) candidate on the caller's batch (A and B
+// are restored from copies between trials, so the pools keep their inputs),
+// keeps the fastest and appends it to the autotune cache file
+// (LLA_AUTOTUNE_CACHE, default ~/.cache/lla_gb300_autotune.txt) under the
+// batch's shape key.  best_ms (optional) receives the winner's time.
+int lla_batch_autotune(lla_batch_plan *p, void *dA, void *dB, int32_t *d_info, void *stream,
+                       double *best_ms, lla_error *err) {
+    if (!p || (p->count > 0 && (!dA || !dB || !d_info))) return lla__set_status(err, LLA_ERR_INVALID_ARG);
+    lla__set_status(err, LLA_OK);
+    if (p->count == 0) return LLA_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t abytes = (size_t)p->a_elems * p->dtype, bbytes = (size_t)p->b_elems * p->dtype;
+    void *a0 = nullptr, *b0 = nullptr;
+    cudaError_t e = cudaMalloc(&a0, abytes);
+    if (e == cudaSuccess) e = cudaMalloc(&b0, bbytes);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(a0, dA, abytes, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b0, dB, bbytes, cudaMemcpyDeviceToDevice, st);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    const int cands[][2] = {{1, 256}, {2, 256}, {3, 256}, {2, 128}, {3, 128}, {4, 128}};
+    int best_c = p->ctas_per_sm, best_t = p->threads;
+    float best = 1e30f;
+    const size_t smem = batch_smem(p->dtype);
+    for (const auto &c : cands) {
+        if (e != cudaSuccess) break;
+        if (smem * c[0] > 227 * 1024) continue;  // does not fit on one SM
+        p->ctas_per_sm = c[0];
+        p->threads = c[1];
+        float tbest = 1e30f;
+        for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {
+            e = cudaMemcpyAsync(dA, a0, abytes, cudaMemcpyDeviceToDevice, st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(dB, b0, bbytes, cudaMemcpyDeviceToDevice, st);
+            if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+            if (e == cudaSuccess)
+                e = p->dtype == 8 ? batch_launch<double>(p, (double *)dA, (double *)dB, d_info, st)
+                                  : batch_launch<float>(p, (float *)dA, (float *)dB, d_info, st);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e == cudaSuccess) tbest = std::min(tbest, ms);
+        }
+        if (e == cudaSuccess && tbest < best) {
+            best = tbest;
+            best_c = c[0];
+            best_t = c[1];
+        }
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dA, a0, abytes, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dB, b0, bbytes, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(a0);
+    cudaFree(b0);
+    lla_batch_set_shape(p, best_c, best_t);
+    if (e != cudaSuccess) return lla__set_cuda_error(err, e);
+    p->tuned = true;
+    cache_store(p->key, best_c, best_t);
+    if (best_ms) *best_ms = best;
+    return LLA_OK;
+}
+
+}  // extern "C"
