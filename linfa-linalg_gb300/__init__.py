@@ -123,6 +123,15 @@ EXPORTS = {
     "lla_batch_posv_graph": ([ctypes.c_void_p] * 5 + [_E], ctypes.c_int),
     "lla_batch_autotune": ([ctypes.c_void_p] * 5 + [ctypes.POINTER(ctypes.c_double), _E],
                            ctypes.c_int),
+    "lla_serve_opts_default": ([ctypes.c_void_p], None),
+    "lla_server_create": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), _E], ctypes.c_int),
+    "lla_server_submit": ([ctypes.c_void_p, ctypes.c_void_p, _E], ctypes.c_int),
+    "lla_server_poll": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                         ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+    "lla_server_drain": ([ctypes.c_void_p, ctypes.c_double], ctypes.c_int),
+    "lla_server_release_factor": ([ctypes.c_void_p, ctypes.c_int64], ctypes.c_int),
+    "lla_server_get_stats": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "lla_server_destroy": ([ctypes.c_void_p], None),
 }
 for _p in "ds":
     EXPORTS.update({
@@ -572,5 +581,111 @@ class BatchPlan:
             if getattr(self, "h", None):
                 lib.lla_batch_plan_destroy(self.h)
                 self.h = None
+        except Exception:
+            pass
+
+
+# ---- serving loop (no counterpart in the reference) --------------------------
+
+REQ_SOLVE, REQ_RESOLVE, REQ_TRSM = 0, 1, 2
+PATH_NAMES = {1: "batched", 2: "mixed", 3: "fp64", 4: "kept_factor"}
+
+
+class ServeOpts(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_double), ("slots", ctypes.c_int32),
+                ("small_n", ctypes.c_int32), ("batch_max", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("batch_window_us", ctypes.c_double)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("dtype", ctypes.c_int32), ("n", ctypes.c_int64),
+                ("m", ctypes.c_int64), ("A", ctypes.c_void_p), ("lda", ctypes.c_int64),
+                ("B", ctypes.c_void_p), ("ldb", ctypes.c_int64), ("tol", ctypes.c_double),
+                ("factor_handle", ctypes.c_int64), ("keep_factor", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("user_tag", ctypes.c_uint64)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("user_tag", ctypes.c_uint64), ("status", ctypes.c_int32), ("path", ctypes.c_int32),
+                ("factor_handle", ctypes.c_int64), ("backward_error", ctypes.c_double),
+                ("iterations", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("t_submit_us", ctypes.c_double), ("t_admit_us", ctypes.c_double),
+                ("t_start_us", ctypes.c_double), ("t_done_us", ctypes.c_double)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        d["path"] = PATH_NAMES.get(self.path, self.path)
+        return d
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("bytes_in_use", ctypes.c_double), ("bytes_peak", ctypes.c_double),
+                ("queued", ctypes.c_int64), ("running", ctypes.c_int64),
+                ("submitted", ctypes.c_int64), ("completed", ctypes.c_int64),
+                ("kept_factors", ctypes.c_int64)]
+
+
+class Server:
+    """Continuous-batching solve server over device-resident (column-major)
+    CUDA tensors.  submit() returns immediately; poll()/drain() collect results."""
+
+    def __init__(self, hbm_budget_bytes=40e9, slots=6, small_n=256, batch_max=512,
+                 batch_window_us=200.0):
+        o = ServeOpts()
+        lib.lla_serve_opts_default(ctypes.byref(o))
+        o.hbm_budget_bytes, o.slots, o.small_n = hbm_budget_bytes, slots, small_n
+        o.batch_max, o.batch_window_us = batch_max, batch_window_us
+        h, e = ctypes.c_void_p(), Error()
+        lib.lla_server_create(ctypes.byref(o), ctypes.byref(h), ctypes.byref(e))
+        _raise(e)
+        self.h = h
+        self._keep = {}
+
+    def submit(self, kind, A, B, tol=0.0, keep_factor=False, handle=0, tag=0):
+        import torch
+        assert A.stride(0) == 1 and B.stride(0) == 1
+        r = Request()
+        r.kind, r.dtype = kind, 8 if A.dtype == torch.float64 else 4
+        r.n, r.m = A.shape[0], B.shape[1]
+        r.A, r.lda = A.data_ptr(), max(1, A.stride(1))
+        r.B, r.ldb = B.data_ptr(), max(1, B.stride(1))
+        r.tol, r.factor_handle, r.keep_factor, r.user_tag = tol, handle, int(keep_factor), tag
+        self._keep[tag] = (A, B)  # keep the tensors alive until the result is polled
+        e = Error()
+        lib.lla_server_submit(self.h, ctypes.byref(r), ctypes.byref(e))
+        _raise(e)
+
+    def poll(self, max_results=4096):
+        buf = (Result * max_results)()
+        got = ctypes.c_int()
+        lib.lla_server_poll(self.h, buf, max_results, ctypes.byref(got))
+        out = [buf[i].as_dict() for i in range(got.value)]
+        for r in out:
+            self._keep.pop(r["user_tag"], None)
+        return out
+
+    def drain(self, timeout_s=600.0):
+        rc = lib.lla_server_drain(self.h, timeout_s)
+        if rc:
+            raise DeviceError(rc)
+
+    def release(self, handle):
+        rc = lib.lla_server_release_factor(self.h, handle)
+        if rc:
+            raise DeviceError(rc)
+
+    def stats(self):
+        st = ServerStats()
+        lib.lla_server_get_stats(self.h, ctypes.byref(st))
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib.lla_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass

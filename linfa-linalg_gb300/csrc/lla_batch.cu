@@ -31,18 +31,14 @@
 
 #include "../../include/lla_gb300.h"
 #include "lla_common.cuh"
+#include "lla_kernels.h"
 #include "lla_prof.h"
 
 namespace lla {
 
-struct BatchItem {
-    int32_t n, m, idx, pad;
-    int64_t a_off, b_off;
-};
-
-constexpr int kBNb = 32;          // block width
-constexpr int kBMaxN = 256;       // largest order a batch system may have
-constexpr int kBMaxRhs = 8;       // right-hand sides per system
+constexpr int kBNb = 32;                // block width
+constexpr int kBMaxN = kBatchMaxN;      // largest order a batch system may have
+constexpr int kBMaxRhs = kBatchMaxRhs;  // right-hand sides per system
 
 template <typename T>
 __device__ __forceinline__ T shfl(T v, int src) {
@@ -308,17 +304,42 @@ static int sm_count() {
     return sms;
 }
 
+namespace lla {
+
+template <typename T>
+int batch_launch_raw(const BatchItem *d_items, int64_t count, T *dA, T *dB, int32_t *d_info,
+                     int *d_counter, int ctas_per_sm, int threads, double flops, cudaStream_t st) {
+    if (count <= 0) return 0;
+    if (cudaMemsetAsync(d_counter, 0, sizeof(int), st) != cudaSuccess) return -1;
+    static bool attr[2] = {false, false};
+    const size_t smem = batch_smem(sizeof(T));
+    if (!attr[sizeof(T) == 8]) {
+        if (cudaFuncSetAttribute(batch_posv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return -1;
+        attr[sizeof(T) == 8] = true;
+    }
+    const unsigned grid =
+        (unsigned)std::max<int64_t>(1, std::min<int64_t>(count, (int64_t)ctas_per_sm * sm_count()));
+    LaunchScope ls(K_BATCH, st, flops);
+    batch_posv_kernel<T><<<grid, threads, smem, st>>>(d_items, count, dA, dB, d_info, d_counter);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template int batch_launch_raw<double>(const BatchItem *, int64_t, double *, double *, int32_t *, int *,
+                                      int, int, double, cudaStream_t);
+template int batch_launch_raw<float>(const BatchItem *, int64_t, float *, float *, int32_t *, int *, int,
+                                     int, double, cudaStream_t);
+
+}  // namespace lla
+
 template <typename T>
 static cudaError_t batch_launch(lla_batch_plan *p, T *dA, T *dB, int32_t *d_info, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(p->d_counter, 0, sizeof(int), st);
-    if (e != cudaSuccess) return e;
-    const size_t smem = batch_smem(sizeof(T));
-    const unsigned grid = (unsigned)std::max<int64_t>(
-        1, std::min<int64_t>(p->count, (int64_t)p->ctas_per_sm * sm_count()));
-    LaunchScope ls(K_BATCH, st, p->flops);
-    batch_posv_kernel<T><<<grid, p->threads, smem, st>>>(p->d_items, p->count, dA, dB, d_info,
-                                                         p->d_counter);
-    return cudaGetLastError();
+    if (batch_launch_raw<T>(p->d_items, p->count, dA, dB, d_info, p->d_counter, p->ctas_per_sm,
+                            p->threads, p->flops, st) == 0)
+        return cudaSuccess;
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? cudaErrorUnknown : e;
 }
 
 extern "C" {

@@ -28,6 +28,19 @@ int trsm_launch(const T *M, int64_t ld, int64_t n, int lower, int trans, const T
                 int64_t ldb, int64_t m, bool exact, int *ws, int *err_word, cudaStream_t st);
 size_t trsm_ws_ints(int64_t n, int64_t m);
 
+// One system of a batched solve: order n, m right-hand sides, caller index,
+// element offsets of A (n x n) and B (n x m) in the pools (column-major, ld n).
+struct BatchItem {
+    int32_t n, m, idx, pad;
+    int64_t a_off, b_off;
+};
+constexpr int kBatchMaxN = 256, kBatchMaxRhs = 8;
+// The persistent batched factor-and-solve over `count` items already on the
+// device (largest first); *d_counter is reset on `st` before the launch.
+template <typename T>
+int batch_launch_raw(const BatchItem *d_items, int64_t count, T *dA, T *dB, int32_t *d_info,
+                     int *d_counter, int ctas_per_sm, int threads, double flops, cudaStream_t st);
+
 // Layout kernels (lla_layout.cu).
 enum ExportMode { EXPORT_FULL = 0, EXPORT_LOWER = 1, EXPORT_LOWER_ZERO_UPPER = 2, EXPORT_FAIL = 3 };
 // W[i + j*ld] = R[i*rs + j*cs] for i < rows, j < cols.
