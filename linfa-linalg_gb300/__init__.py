@@ -411,6 +411,12 @@ def _stream_ptr(stream):
     return ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
 
 
+def _ld(T):
+    """Leading dimension of a column-major (stride(0) == 1) tensor; a single
+    column's stride is arbitrary in torch, so its leading dimension is n."""
+    return T.stride(1) if T.shape[1] > 1 else max(1, T.shape[0])
+
+
 def potrf_device(A, algo=ALGO_FAST, info=None, stream=None):
     """Cholesky of a column-major CUDA tensor in place.  `A` is a torch tensor
     whose transpose is contiguous (A.T.is_contiguous(), i.e. Fortran order);
@@ -422,7 +428,7 @@ def potrf_device(A, algo=ALGO_FAST, info=None, stream=None):
         info = torch.empty(1, dtype=torch.int64, device=A.device)
     e = Error()
     p = "d" if A.dtype == torch.float64 else "s"
-    getattr(lib, f"lla_{p}potrf_device")(ctypes.c_void_p(A.data_ptr()), n, A.stride(1), algo,
+    getattr(lib, f"lla_{p}potrf_device")(ctypes.c_void_p(A.data_ptr()), n, _ld(A), algo,
                                          ctypes.c_void_p(info.data_ptr()), _stream_ptr(stream),
                                          ctypes.byref(e))
     _raise(e)
@@ -437,10 +443,9 @@ def trsm_device(L, B, trans, algo=ALGO_FAST, stream=None):
     assert L.stride(0) == 1 and B.stride(0) == 1 and B.shape[0] == n
     e = Error()
     p = "d" if L.dtype == torch.float64 else "s"
-    getattr(lib, f"lla_{p}trsm_device")(ctypes.c_void_p(L.data_ptr()), n, L.stride(1), trans,
-                                        ctypes.c_void_p(B.data_ptr()), B.shape[1],
-                                        max(1, B.stride(1)), algo, _stream_ptr(stream),
-                                        ctypes.byref(e))
+    getattr(lib, f"lla_{p}trsm_device")(ctypes.c_void_p(L.data_ptr()), n, _ld(L), trans,
+                                        ctypes.c_void_p(B.data_ptr()), B.shape[1], _ld(B), algo,
+                                        _stream_ptr(stream), ctypes.byref(e))
     _raise(e)
     return B
 
@@ -474,9 +479,9 @@ def posv_refined_device(A, B, X, stream=None, **kw):
     n, m = A.shape[0], B.shape[1]
     assert A.stride(0) == 1 and B.stride(0) == 1 and X.stride(0) == 1
     o, r, e = refine_opts(**kw), RefineReport(), Error()
-    lib.lla_dposv_refined_device(ctypes.c_void_p(A.data_ptr()), n, max(1, A.stride(1)),
-                                 ctypes.c_void_p(B.data_ptr()), m, max(1, B.stride(1)),
-                                 ctypes.c_void_p(X.data_ptr()), max(1, X.stride(1)),
+    lib.lla_dposv_refined_device(ctypes.c_void_p(A.data_ptr()), n, _ld(A),
+                                 ctypes.c_void_p(B.data_ptr()), m, _ld(B),
+                                 ctypes.c_void_p(X.data_ptr()), _ld(X),
                                  ctypes.byref(o), ctypes.byref(r), _stream_ptr(stream),
                                  ctypes.byref(e))
     _raise(e)
@@ -494,7 +499,7 @@ def spotrf_mixed_device(A, update="bf16x6", info=None, stream=None):
         info = torch.empty(1, dtype=torch.int64, device=A.device)
     u = UPDATE_NAMES[update] if isinstance(update, str) else int(update)
     e = Error()
-    lib.lla_spotrf_mixed_device(ctypes.c_void_p(A.data_ptr()), n, max(1, A.stride(1)), u,
+    lib.lla_spotrf_mixed_device(ctypes.c_void_p(A.data_ptr()), n, _ld(A), u,
                                 ctypes.c_void_p(info.data_ptr()), _stream_ptr(stream), ctypes.byref(e))
     _raise(e)
     return info
@@ -647,8 +652,8 @@ class Server:
         r = Request()
         r.kind, r.dtype = kind, 8 if A.dtype == torch.float64 else 4
         r.n, r.m = A.shape[0], B.shape[1]
-        r.A, r.lda = A.data_ptr(), max(1, A.stride(1))
-        r.B, r.ldb = B.data_ptr(), max(1, B.stride(1))
+        r.A, r.lda = A.data_ptr(), _ld(A)
+        r.B, r.ldb = B.data_ptr(), _ld(B)
         r.tol, r.factor_handle, r.keep_factor, r.user_tag = tol, handle, int(keep_factor), tag
         self._keep[tag] = (A, B)  # keep the tensors alive until the result is polled
         e = Error()
