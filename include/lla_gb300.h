@@ -322,7 +322,8 @@ enum lla_request_kind {
     LLA_REQ_TRSM = 2     /* L X = B with the lower-triangular L given in A */
 };
 enum lla_result_path {
-    LLA_PATH_BATCHED = 1, LLA_PATH_MIXED = 2, LLA_PATH_FP64 = 3, LLA_PATH_KEPT_FACTOR = 4
+    LLA_PATH_BATCHED = 1, LLA_PATH_MIXED = 2, LLA_PATH_FP64 = 3, LLA_PATH_KEPT_FACTOR = 4,
+    LLA_PATH_TRSM = 5
 };
 
 typedef struct lla_serve_opts {

@@ -593,7 +593,7 @@ class BatchPlan:
 # ---- serving loop (no counterpart in the reference) --------------------------
 
 REQ_SOLVE, REQ_RESOLVE, REQ_TRSM = 0, 1, 2
-PATH_NAMES = {1: "batched", 2: "mixed", 3: "fp64", 4: "kept_factor"}
+PATH_NAMES = {1: "batched", 2: "mixed", 3: "fp64", 4: "kept_factor", 5: "trsm"}
 
 
 class ServeOpts(ctypes.Structure):

@@ -138,6 +138,7 @@ int run_big(lla_server *s, Pending *p, cudaStream_t st, std::vector<void *> &scr
         return scratch[slot];
     };
     if (r.kind == LLA_REQ_TRSM) {  // L X = B with the lower factor given in A
+        p->res.path = LLA_PATH_TRSM;
         if (r.dtype == 4)
             return lla_strsm_device((const float *)r.A, n, r.lda, 0, (float *)r.B, m, r.ldb,
                                     LLA_ALGO_FAST, st, &err) ||
