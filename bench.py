@@ -336,9 +336,17 @@ def main():
         bound, peak, src = "fp64-tensor", fp64_peak, \
             "measured live: 8 independent mma.sync m16n8k16 f64 per step on all SMs " \
             "(the measured peak table has HBM and bf16 only)"
+    traffic, traffic_src = None, None
+    tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tpath):
+        t = json.load(open(tpath)).get(dom)
+        if t:  # ncu capture of a smaller case, scaled by the units one launch processes
+            traffic = t["dram_bytes"] * (n / t["n_captured"]) ** t["exponent"]
+            traffic_src = f"{t['source']}, scaled from n={t['n_captured']} by (n/{t['n_captured']})^{t['exponent']}"
     roofline = {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak if peak and peak > 0 else None,
-                "traffic": None, "share_of_step": dom_ms / ms_mixed, "avg_launch_ms": dom_ms / dom_n,
+                "traffic": traffic, "traffic_source": traffic_src,
+                "share_of_step": dom_ms / ms_mixed, "avg_launch_ms": dom_ms / dom_n,
                 "peak_source": src}
 
     # end to end through the C ABI with host (pinned) buffers: lla_dposv_refined reads A
