@@ -66,12 +66,12 @@ __global__ void __launch_bounds__(1024) lowp_diag_kernel(float *L, int64_t ld, i
                 if (c < bs) {
                     const float piv = __shfl_sync(0xffffffffu, v[c], c);
                     if (!(piv > 0.f)) bad = true;  // non-positive (or NaN) pivot: breakdown
-                    const float lcc = sqrtf(fmaxf(piv, 0.f));
+                    const float rl = rsqrtf(fmaxf(piv, 1e-30f));  // 1 / L[c][c]
                     if (lane == c) {
-                        v[c] = lcc;
+                        v[c] = piv * rl;  // sqrt(piv)
                         ratio = fminf(ratio, piv);
                     }
-                    if (lane > c) v[c] = v[c] / lcc;
+                    if (lane > c) v[c] = v[c] * rl;
 #pragma unroll
                     for (int c2 = c + 1; c2 < 32; ++c2) {
                         const float t = __shfl_sync(0xffffffffu, v[c], c2);
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(1024) lowp_diag_kernel(float *L, int64_t ld, i
 #pragma unroll
             for (int c = 0; c < 32; ++c) {
                 if (c < bs) {
-                    v[c] = v[c] / sa[(kb + c) * kLpLd + kb + c];
+                    v[c] = __fdividef(v[c], sa[(kb + c) * kLpLd + kb + c]);
 #pragma unroll
                     for (int c2 = c + 1; c2 < 32; ++c2)
                         if (c2 < bs) v[c2] = fmaf(-v[c], sa[(kb + c2) * kLpLd + kb + c], v[c2]);

@@ -10,9 +10,9 @@
 //     or FP16 operands, FP32 accumulator in tensor memory) for every chunk of
 //     every term pair, releasing each stage with tcgen05.commit, alternating
 //     between two accumulators;
-//   * four epilogue warps read a finished accumulator from tensor memory
-//     (tcgen05.ld 32x32b, one 32-lane quarter per warp) and subtract it from the
-//     FP32 tile in HBM (coalesced: a warp covers 32 consecutive rows of a
+//   * eight epilogue warps read a finished accumulator from tensor memory
+//     (tcgen05.ld 32x32b, two warps per 32-lane quarter) and subtract it from
+//     the FP32 tile in HBM (coalesced: a warp covers 32 consecutive rows of a
 //     column-major column) while the next tile's MMAs run; diagonal tiles write
 //     their lower half only.
 // Every wait is bounded: on expiry the CTA records LLA_ERR_TIMEOUT, skips its
@@ -134,11 +134,14 @@ __device__ __forceinline__ void tc_tri_tile(int64_t t, int64_t &I, int64_t &J) {
     J = t - i * (i + 1) / 2;
 }
 
-// Persistent, warp-specialised: warps 0-3 drain accumulators (epilogue),
-// warp 4 lane 0 feeds the shared-memory ring with TMA, warp 5 lane 0 issues
-// the MMAs.  Two tensor-memory accumulators let the epilogue of one tile
-// overlap the MMAs of the next.
-constexpr int kTcThreads = 192;
+// Persistent, warp-specialised: warps 0-7 drain accumulators (epilogue, two
+// warps per 32-lane quarter of tensor memory, 64 columns each), warp 8 lane 0
+// feeds the shared-memory ring with TMA, warp 9 lane 0 issues the MMAs.  Two
+// tensor-memory accumulators let the epilogue of one tile overlap the MMAs of
+// the next, and the epilogue fetches its FP32 tile before the accumulator is
+// ready.
+constexpr int kTcThreads = 320;  // 8 epilogue warps, 1 producer warp, 1 MMA warp
+constexpr int kTcEpiThreads = 256;
 
 __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     const __grid_constant__ CUtensorMap tmap, float *C, int64_t ld, int64_t q, int64_t n, int kchunks,
@@ -167,7 +170,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
         }
         for (int a = 0; a < 2; ++a) {
             mbar_init(tfull0 + 8 * a, 1);
-            mbar_init(tempty0 + 8 * a, 128);  // every epilogue thread releases
+            mbar_init(tempty0 + 8 * a, kTcEpiThreads);  // every epilogue thread releases
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
@@ -184,7 +187,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     tc_fence_after();
     const uint32_t tmem = *tslot;
 
-    if (warp == 4) {
+    if (warp == 8) {
         if (lane == 0) {  // TMA producer
             int64_t g = 0;
             for (int64_t t = blockIdx.x; t < ntiles && !*(volatile int *)&s_abort; t += gridDim.x) {
@@ -206,7 +209,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
                 }
             }
         }
-    } else if (warp == 5) {
+    } else if (warp == 9) {
         if (lane == 0) {  // MMA issuer
             int64_t g = 0, lt = 0;
             for (int64_t t = blockIdx.x; t < ntiles && !*(volatile int *)&s_abort; t += gridDim.x, ++lt) {
@@ -237,12 +240,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
                 tc_commit(tfull0 + 8 * a);  // accumulator a is complete
             }
         }
-    } else {  // warps 0-3: epilogue
+    } else {  // warps 0-7: epilogue; warp w drains lane quarter w % 4, columns 64 (w / 4) ..
         int64_t lt = 0;
-        const int r = warp * 32 + lane;
+        const int qw = warp & 3, half = warp >> 2;
+        const int r = qw * 32 + lane;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
             const int a = (int)(lt & 1);
             const int64_t use = lt >> 1;
+            int64_t I, J;
+            tc_tri_tile(t, I, J);
+            const int64_t grow = q + I * kTcM + r;
+            const int64_t gcol0 = q + J * kTcN + half * 64;
+            const int64_t cmax = n - gcol0;  // columns left in the matrix
+            // the FP32 tile does not depend on the MMAs: fetch its first 32 columns
+            // while they run, the next 32 while the first are written back
+            float *base = C + grow + gcol0 * ld;
+            const bool row_in = grow < n;
+            float cur[32];
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+                const bool in = row_in && c < cmax && (I != J || half * 64 + c <= r);
+                cur[c] = in ? base[c * ld] : 0.f;
+            }
             bool ok = mbar_wait(tfull0 + 8 * a, (uint32_t)(use & 1), err_word);
             ok = __all_sync(0xffffffffu, ok) && !*(volatile int *)&s_abort;
             if (!ok) {
@@ -250,29 +269,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
                 break;
             }
             tc_fence_after();
-            int64_t I, J;
-            tc_tri_tile(t, I, J);
-            const int64_t grow = q + I * kTcM + r;
-#pragma unroll 1
-            for (int cb = 0; cb < kTcN / 32; ++cb) {
+#pragma unroll
+            for (int cb = 0; cb < 2; ++cb) {
                 uint32_t v[32];
-                tc_ld32(tmem + (uint32_t)(a * kTcCols) + ((uint32_t)(warp * 32) << 16) +
-                            (uint32_t)(cb * 32),
+                tc_ld32(tmem + (uint32_t)(a * kTcCols) + ((uint32_t)(qw * 32) << 16) +
+                            (uint32_t)(half * 64 + cb * 32),
                         v);
-                if (grow < n) {
-                    float *base = C + grow + (q + J * kTcN + cb * 32) * ld;
-                    const int64_t cmax = n - (q + J * kTcN + cb * 32);  // columns left in the matrix
-                    float old[32];
 #pragma unroll
-                    for (int c = 0; c < 32; ++c) {
-                        const bool in = c < cmax && (I != J || cb * 32 + c <= r);
-                        old[c] = in ? base[c * ld] : 0.f;
+                for (int c = 0; c < 32; ++c) {
+                    const int cc = cb * 32 + c;
+                    const bool in = row_in && cc < cmax && (I != J || half * 64 + cc <= r);
+                    const float x = cur[c] - __uint_as_float(v[c]);
+                    if (cb == 0) {  // fetch the second half before storing the first
+                        const int c2 = 32 + c;
+                        const bool in2 = row_in && c2 < cmax && (I != J || half * 64 + c2 <= r);
+                        cur[c] = in2 ? base[c2 * ld] : 0.f;
                     }
-#pragma unroll
-                    for (int c = 0; c < 32; ++c) {
-                        const bool in = c < cmax && (I != J || cb * 32 + c <= r);
-                        if (in) base[c * ld] = old[c] - __uint_as_float(v[c]);
-                    }
+                    if (in) base[cc * ld] = x;
                 }
             }
             tc_fence_before();
