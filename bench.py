@@ -211,7 +211,7 @@ def main():
     ap.add_argument("--update", default="bf16x6",
                     help="trailing-update form of the mixed path: fp32|bf16|bf16x3|bf16x6|fp16|fp16x3")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed steps of the plain FP64 leg")
-    ap.add_argument("--workload", default="single", choices=["single", "batch", "serve"],
+    ap.add_argument("--workload", default="single", choices=["single", "batch", "serve", "sweep"],
                     help="single: the n=16384 system (the headline); batch: 10,000 uneven small systems")
     ap.add_argument("--batch-count", type=int, default=10000)
     ap.add_argument("--batch-dtype", default="f64", choices=["f64", "f32"])
@@ -226,6 +226,9 @@ def main():
         return
     if args.workload == "serve":
         run_serve(args)
+        return
+    if args.workload == "sweep":
+        run_sweep(args)
         return
 
     import torch
@@ -506,6 +509,52 @@ def run_batch(args):
         "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
     }
     print(json.dumps(out))
+
+
+def run_sweep(args):
+    """Precision sweep: n=8192, 16 RHS, A = D Q diag(s) Q^T D with kappa(Q diag(s) Q^T) in
+    {1e2, 1e4, 1e6, 1e8} (log-uniform spectra) and D = diag(10^U(-3,3)); every update form;
+    reports iterations to converge, backward error, fallback and time."""
+    import torch
+    import __graft_entry__
+    lla = __graft_entry__.load_package()
+    dev = torch.device("cuda", 0)
+    n, m = 8192, 16
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED)
+    G = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+    import ctypes
+    libp = os.path.join(os.path.dirname(torch.__file__), "lib", "libtorch_cuda_linalg.so")
+    if os.path.exists(libp):
+        ctypes.CDLL(libp, mode=ctypes.RTLD_GLOBAL)
+    Q, _ = torch.linalg.qr(G)
+    del G
+    d = 10.0 ** (torch.rand(n, dtype=torch.float64, device=dev, generator=g) * 6 - 3)
+    B = torch.randn(n, m, dtype=torch.float64, device=dev, generator=g).T.contiguous().T
+    X = torch.empty_like(B.T.contiguous()).T
+    rows = []
+    for kappa in (1e2, 1e4, 1e6, 1e8):
+        u = torch.rand(n, dtype=torch.float64, device=dev, generator=g)
+        sv = torch.exp(u * np.log(kappa))
+        sv[0], sv[-1] = 1.0, kappa
+        A = (Q * sv) @ Q.T
+        A = (A + A.T) * 0.5
+        A = A * d[:, None] * d[None, :]
+        for form in ("bf16", "bf16x3", "bf16x6", "fp16", "fp16x3", "fp32"):
+            lla.posv_refined_device(A.T, B, X, update=form)  # warm
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rep = lla.posv_refined_device(A.T, B, X, update=form)
+            torch.cuda.synchronize()
+            ms = (time.perf_counter() - t0) * 1e3
+            be = backward_error(torch, A, X, B)
+            rows.append({"kappa": kappa, "update": form, "iterations": rep["iterations"],
+                         "converged": rep["converged"], "fell_back": rep["fell_back"],
+                         "factor_failed": rep["factor_failed"],
+                         "backward_error0": rep["backward_error0"], "backward_error": be, "ms": ms})
+    print(json.dumps({"metric": "precision sweep n=8192 nrhs=16 (iterations, fallback)",
+                      "dtype": "f64", "data": "synthetic (seeded D Q diag(s) Q^T D, D = 10^U(-3,3))",
+                      "rows": rows}))
 
 
 def run_serve(args):
