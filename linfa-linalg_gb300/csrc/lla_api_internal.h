@@ -28,6 +28,7 @@ struct HostBuf {
 // Workspace of the mixed-precision refined solve.
 struct MixedWs {
     DevBuf L, s, rowsum, R, Y, diag0, words;  // FP32 factor, scaling, norms, residual, correction
+    DevBuf P;                                 // split-K partial products of the residual
     DevBuf F, fdiag;                          // plain FP64 fallback
     DevBuf opA, opB;                          // tensor-core operand planes of one panel
     DevBuf tcerr;                             // tensor-core update status word

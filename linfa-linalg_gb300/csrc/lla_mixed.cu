@@ -159,11 +159,16 @@ __global__ void update_x_kernel(double *X, int64_t ldx, const double *s, const f
 // A[i + k*lda] for k <= i, A[k + i*lda] otherwise.  Also colmax_r.
 constexpr int kResRows = 32, kResCols = 64, kResK = 32;
 
+// K is split into `splits` contiguous ranges (blockIdx.z) so that the grid
+// covers the SMs in several full waves; with splits > 1 each range writes its
+// partial A_sym X into P[z] and residual_combine_kernel forms R = B - sum_z P[z]
+// in a fixed order (deterministic, no atomics).
 __global__ void __launch_bounds__(128) residual_dmma_kernel(const double *__restrict__ A, int64_t lda,
                                                             int64_t n, const double *__restrict__ X,
                                                             int64_t ldx, const double *__restrict__ B,
                                                             int64_t ldb, double *R, int64_t ldr,
-                                                            int64_t m, double *colmax_r) {
+                                                            int64_t m, double *colmax_r, int splits,
+                                                            double *P) {
     __shared__ double As[kResK][kResRows + 4];  // [k][row], stride 36 = 4 (mod 16)
     __shared__ double Xs[kResK][kResCols + 4];  // [k][col], stride 68 = 4 (mod 16)
     const int64_t i0 = (int64_t)blockIdx.x * kResRows;
@@ -176,7 +181,11 @@ __global__ void __launch_bounds__(128) residual_dmma_kernel(const double *__rest
     for (int ni = 0; ni < 4; ++ni)
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[ni][q] = 0.0;
-    for (int64_t k0 = 0; k0 < n; k0 += kResK) {
+    const int64_t kchunks = (n + kResK - 1) / kResK;
+    const int64_t kc_per = (kchunks + splits - 1) / splits;
+    const int64_t kbeg = (int64_t)blockIdx.z * kc_per * kResK;
+    const int64_t kend = min(n, kbeg + kc_per * kResK);
+    for (int64_t k0 = kbeg; k0 < kend; k0 += kResK) {
         const bool upper = k0 > i0 + kResRows - 1;  // whole tile above the diagonal
         for (int e = tid; e < kResRows * kResK; e += 128) {
             int r, c;
@@ -219,6 +228,18 @@ __global__ void __launch_bounds__(128) residual_dmma_kernel(const double *__rest
         }
         __syncthreads();
     }
+    if (splits > 1) {  // partial product of this K range
+        double *Pz = P + (int64_t)blockIdx.z * n * m;
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int64_t i = i0 + wr + g + 8 * (q >> 1);
+                const int64_t col = c0 + wc + ni * 8 + 2 * t + (q & 1);
+                if (i < n && col < m) Pz[i + col * n] = acc[ni][q];
+            }
+        return;
+    }
     // epilogue: R = B - acc, and column maxima of |R|
 #pragma unroll
     for (int ni = 0; ni < 4; ++ni) {
@@ -244,6 +265,24 @@ __global__ void __launch_bounds__(128) residual_dmma_kernel(const double *__rest
             if (g == 0 && col < m) atomic_max_nonneg(&colmax_r[col], v);
         }
     }
+}
+
+// R = B - (P[0] + P[1] + ...), summed in split order; and column maxima of |R|.
+__global__ void residual_combine_kernel(const double *__restrict__ P, int splits, const double *B,
+                                        int64_t ldb, double *R, int64_t ldr, int64_t n, int64_t m,
+                                        double *colmax_r) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t j = blockIdx.y;
+    double v = 0.0;
+    if (i < n) {
+        double s = P[i + j * n];
+        for (int z = 1; z < splits; ++z) s += P[(int64_t)z * n * m + i + j * n];
+        const double r = B[i + j * ldb] - s;
+        R[i + j * ldr] = r;
+        v = fabs(r);
+    }
+    v = warp_max(v);
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&colmax_r[j], v);
 }
 
 // ---------------------------------------------------------------------------
@@ -295,13 +334,36 @@ int update_x_launch(double *X, int64_t ldx, const double *s, const float *Y, int
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+int residual_splits(int64_t n, int64_t m) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    const int64_t tiles = (int64_t)gx(n, kResRows) * gx(m, kResCols);
+    // smallest split giving at least four waves of CTAs (at most 8)
+    int s = 1;
+    while (s < 8 && tiles * s < 4 * (int64_t)sms && n / (kResK * (s + 1)) >= 4) ++s;
+    return s;
+}
+
 int residual_launch(const double *A, int64_t lda, int64_t n, const double *X, int64_t ldx,
                     const double *B, int64_t ldb, double *R, int64_t ldr, int64_t m, double *colmax_r,
-                    cudaStream_t st) {
-    // algorithmic work: 2 n^2 m flops
-    LaunchScope ls(K_RESIDUAL, st, 2.0 * n * n * m);
-    residual_dmma_kernel<<<dim3(gx(n, kResRows), gx(m, kResCols)), 128, 0, st>>>(
-        A, lda, n, X, ldx, B, ldb, R, ldr, m, colmax_r);
+                    double *P, cudaStream_t st) {
+    const int splits = P ? residual_splits(n, m) : 1;
+    {
+        // algorithmic work: 2 n^2 m flops
+        LaunchScope ls(K_RESIDUAL, st, 2.0 * n * n * m);
+        residual_dmma_kernel<<<dim3(gx(n, kResRows), gx(m, kResCols), splits), 128, 0, st>>>(
+            A, lda, n, X, ldx, B, ldb, R, ldr, m, colmax_r, splits, P);
+    }
+    if (splits > 1) {
+        LaunchScope ls(K_REFINE, st, 8.0 * n * m * (splits + 2));
+        residual_combine_kernel<<<dim3(gx(n, 256), (unsigned)m), 256, 0, st>>>(P, splits, B, ldb, R, ldr,
+                                                                             n, m, colmax_r);
+    }
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -376,6 +438,7 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
     MX_TRY(w.s.ensure(sizeof(double) * n));
     MX_TRY(w.rowsum.ensure(sizeof(double) * n));
     MX_TRY(w.R.ensure(sizeof(double) * n * m));
+    MX_TRY(w.P.ensure(sizeof(double) * n * m * residual_splits(n, m)));
     MX_TRY(w.Y.ensure(sizeof(float) * n * m));
     MX_TRY(w.diag0.ensure(sizeof(float) * n));
     MX_TRY(w.words.ensure(sizeof(double) * (8 + 3 * m)));
@@ -447,7 +510,8 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
             MX_TRY(cudaMemsetAsync(colmax_r, 0, sizeof(double) * 2 * m, st));
             MX_TRY(last_err(update_x_launch(dX, ldx, s, Y, n, m, colmax_x, st)));
             // r = b - A x  (FP64)
-            MX_TRY(last_err(residual_launch(dA, lda, n, dX, ldx, dB, ldb, R, n, m, colmax_r, st)));
+            MX_TRY(last_err(residual_launch(dA, lda, n, dX, ldx, dB, ldb, R, n, m, colmax_r,
+                                            (double *)w.P.p, st)));
             rhs = R;
             ldrhs = n;
             MX_TRY(read_words(8 + 3 * m));
@@ -507,7 +571,8 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
         MX_TRY(last_err(trsm_launch<double>(F, n, n, 0, 1, nullptr, dX, ldx, m, false, tws, err_word, st)));
         MX_TRY(cudaMemsetAsync(colmax_r, 0, sizeof(double) * 2 * m, st));
         MX_TRY(last_err(colmax_launch(dX, ldx, n, m, colmax_x, st)));
-        MX_TRY(last_err(residual_launch(dA, lda, n, dX, ldx, dB, ldb, R, n, m, colmax_r, st)));
+        MX_TRY(last_err(residual_launch(dA, lda, n, dX, ldx, dB, ldb, R, n, m, colmax_r,
+                                        (double *)w.P.p, st)));
         MX_TRY(read_words(8 + 3 * m));
         double e = 0.0;
         for (int64_t j = 0; j < m; ++j) {

@@ -19,8 +19,11 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
 int equilibrate_launch(const double *A, int64_t lda, int64_t n, bool scale, double *s, float *W,
                        int64_t ldw, double *rowsum, double *anorm, int *bad, cudaStream_t st);
 int colmax_launch(const double *M, int64_t ld, int64_t n, int64_t m, double *colmax, cudaStream_t st);
+// R = B - A_sym X in FP64; P: workspace of residual_splits(n, m) * n * m
+// doubles for the split-K partials (NULL: no split).
+int residual_splits(int64_t n, int64_t m);
 int residual_launch(const double *A, int64_t lda, int64_t n, const double *X, int64_t ldx,
                     const double *B, int64_t ldb, double *R, int64_t ldr, int64_t m, double *colmax_r,
-                    cudaStream_t st);
+                    double *P, cudaStream_t st);
 
 }  // namespace lla
