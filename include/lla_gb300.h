@@ -221,6 +221,16 @@ enum lla_update {
     LLA_UPDATE_FP16X3 = 13  /* tcgen05: hi/lo FP16 split, three products */
 };
 
+/* How the refinement computes r = b - A x:
+ *  LLA_RESIDUAL_FP64          FP64 arithmetic on the FP64 MMA pipe (default);
+ *  LLA_RESIDUAL_EXACT_SLICES  the same quantity on the BF16 tensor cores: A and x
+ *                             are cut into 8 exact 7-bit integer slices with
+ *                             power-of-two row / column scales, the slice
+ *                             products are summed exactly (integers below 2^24 in
+ *                             FP32, drained into 64-bit integers) and combined in
+ *                             FP64 -- an error bound like an FP64 product's. */
+enum lla_residual { LLA_RESIDUAL_FP64 = 0, LLA_RESIDUAL_EXACT_SLICES = 1 };
+
 typedef struct lla_refine_opts {
     int32_t update;      /* lla_update (default LLA_UPDATE_BF16X6) */
     int32_t max_iters;   /* refinement iterations before giving up (default 30) */
@@ -228,7 +238,8 @@ typedef struct lla_refine_opts {
     int32_t equilibrate; /* 1: symmetric power-of-two scaling (default) */
     int32_t fallback;    /* 1: plain FP64 on breakdown or stall (default); 0: LLA_ERR_NOT_CONVERGED */
     int32_t nb;          /* panel width (0: default) */
-    int32_t reserved[3];
+    int32_t residual;    /* lla_residual (default LLA_RESIDUAL_FP64) */
+    int32_t reserved[2];
 } lla_refine_opts;
 
 typedef struct lla_refine_report {
@@ -251,6 +262,13 @@ void lla_refine_opts_default(lla_refine_opts *opts);
 int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda, const double *dB, int64_t m,
                              int64_t ldb, double *dX, int64_t ldx, const lla_refine_opts *opts,
                              lla_refine_report *report, void *stream, lla_error *err);
+
+/* R = B - A_sym X (A_sym: the symmetric matrix defined by the lower triangle
+ * of dA), column-major device arrays, by the given lla_residual method;
+ * synchronous on `stream`. */
+int lla_dresidual_device(const double *dA, int64_t n, int64_t lda, const double *dX, int64_t ldx,
+                         const double *dB, int64_t ldb, double *dR, int64_t ldr, int64_t m,
+                         int method, void *stream, lla_error *err);
 
 /* Host-view form (SolveC-like): `a` is read only; `b` (n x m) is overwritten
  * with X.  Errors: NotSquare(a), WrongRows(b), NotPositiveDefinite (decided by

@@ -66,7 +66,7 @@ class Error(ctypes.Structure):
 class RefineOpts(ctypes.Structure):
     _fields_ = [("update", ctypes.c_int32), ("max_iters", ctypes.c_int32), ("tol", ctypes.c_double),
                 ("equilibrate", ctypes.c_int32), ("fallback", ctypes.c_int32), ("nb", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 3)]
+                ("residual", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
 
 
 class RefineReport(ctypes.Structure):
@@ -83,6 +83,7 @@ class RefineReport(ctypes.Structure):
 
 UPDATE_FP32, UPDATE_BF16, UPDATE_BF16X3, UPDATE_BF16X6, UPDATE_FP16, UPDATE_FP16X3 = 0, 1, 3, 6, 11, 13
 UPDATE_NAMES = {"fp32": 0, "bf16": 1, "bf16x3": 3, "bf16x6": 6, "fp16": 11, "fp16x3": 13}
+RESIDUAL_NAMES = {"fp64": 0, "slices": 1}
 
 _V = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64]
 _E = ctypes.POINTER(Error)
@@ -110,6 +111,10 @@ EXPORTS = {
                           ctypes.c_int),
     "lla_spotrf_mixed_device": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
                                  ctypes.c_void_p, ctypes.c_void_p, _E], ctypes.c_int),
+    "lla_dresidual_device": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+                              ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                              ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, _E],
+                             ctypes.c_int),
     "lla_batch_plan_create": ([ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                ctypes.POINTER(ctypes.c_void_p), _E], ctypes.c_int),
     "lla_batch_plan_destroy": ([ctypes.c_void_p], None),
@@ -452,10 +457,12 @@ def trsm_device(L, B, trans, algo=ALGO_FAST, stream=None):
 
 # ---- mixed-precision refined solve (no counterpart in the reference) --------
 
-def refine_opts(update="bf16x6", max_iters=30, tol=1e-13, equilibrate=True, fallback=True, nb=0):
+def refine_opts(update="bf16x6", max_iters=30, tol=1e-13, equilibrate=True, fallback=True, nb=0,
+                residual="fp64"):
     o = RefineOpts()
     lib.lla_refine_opts_default(ctypes.byref(o))
     o.update = UPDATE_NAMES[update] if isinstance(update, str) else int(update)
+    o.residual = RESIDUAL_NAMES[residual] if isinstance(residual, str) else int(residual)
     o.max_iters, o.tol = max_iters, tol
     o.equilibrate, o.fallback, o.nb = int(bool(equilibrate)), int(bool(fallback)), nb
     return o
@@ -694,3 +701,16 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def residual_device(A, X, B, R, method="fp64", stream=None):
+    """R = B - A_sym X on column-major CUDA tensors (A_sym from A's lower triangle)."""
+    n, m = A.shape[0], X.shape[1]
+    e = Error()
+    lib.lla_dresidual_device(ctypes.c_void_p(A.data_ptr()), n, _ld(A), ctypes.c_void_p(X.data_ptr()),
+                             _ld(X), ctypes.c_void_p(B.data_ptr()), _ld(B),
+                             ctypes.c_void_p(R.data_ptr()), _ld(R), m,
+                             RESIDUAL_NAMES[method] if isinstance(method, str) else int(method),
+                             _stream_ptr(stream), ctypes.byref(e))
+    _raise(e)
+    return R

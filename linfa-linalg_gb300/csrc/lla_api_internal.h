@@ -29,6 +29,7 @@ struct HostBuf {
 struct MixedWs {
     DevBuf L, s, rowsum, R, Y, diag0, words;  // FP32 factor, scaling, norms, residual, correction
     DevBuf P;                                 // split-K partial products of the residual
+    DevBuf oz;                                // exact-slice residual: slices of A and X
     DevBuf F, fdiag;                          // plain FP64 fallback
     DevBuf opA, opB;                          // tensor-core operand planes of one panel
     DevBuf tcerr;                             // tensor-core update status word

@@ -397,6 +397,7 @@ extern "C" void lla_refine_opts_default(lla_refine_opts *o) {
     o->equilibrate = 1;
     o->fallback = 1;
     o->nb = 0;
+    o->residual = LLA_RESIDUAL_FP64;
 }
 
 #define MX_TRY(expr)                                                \
@@ -490,6 +491,11 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
         std::memcpy(&finfo, hw + 2, sizeof(int64_t));
         if (finfo >= 0) lowp_ok = false;
     }
+    const bool slices = opts.residual == LLA_RESIDUAL_EXACT_SLICES;
+    if (lowp_ok && slices) {  // slices of A, once per solve
+        MX_TRY(w.oz.ensure(oz_workspace_bytes(n, m)));
+        MX_TRY(last_err(oz_prepare(dA, lda, n, m, w.oz.p, st)));
+    }
     r.ms_factor = ms_since(t0);
     r.factor_failed = lowp_ok ? 0 : 1;
     // 3. refinement
@@ -510,8 +516,12 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
             MX_TRY(cudaMemsetAsync(colmax_r, 0, sizeof(double) * 2 * m, st));
             MX_TRY(last_err(update_x_launch(dX, ldx, s, Y, n, m, colmax_x, st)));
             // r = b - A x  (FP64)
-            MX_TRY(last_err(residual_launch(dA, lda, n, dX, ldx, dB, ldb, R, n, m, colmax_r,
-                                            (double *)w.P.p, st)));
+            if (slices)
+                MX_TRY(last_err(oz_residual_launch(dX, ldx, dB, ldb, R, n, n, m, colmax_x, colmax_r,
+                                                   w.oz.p, err_word, st)));
+            else
+                MX_TRY(last_err(residual_launch(dA, lda, n, dX, ldx, dB, ldb, R, n, m, colmax_r,
+                                                (double *)w.P.p, st)));
             rhs = R;
             ldrhs = n;
             MX_TRY(read_words(8 + 3 * m));
@@ -584,5 +594,41 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
     }
     r.ms_total = ms_since(t_start);
     if (rep) *rep = r;
+    return LLA_OK;
+}
+
+extern "C" int lla_dresidual_device(const double *dA, int64_t n, int64_t lda, const double *dX, int64_t ldx,
+                                    const double *dB, int64_t ldb, double *dR, int64_t ldr, int64_t m,
+                                    int method, void *stream, lla_error *err) {
+    if (n < 0 || m < 0 || lda < std::max<int64_t>(1, n) || ldx < std::max<int64_t>(1, n) ||
+        ldb < std::max<int64_t>(1, n) || ldr < std::max<int64_t>(1, n) ||
+        (n > 0 && m > 0 && (!dA || !dX || !dB || !dR)) ||
+        (method != LLA_RESIDUAL_FP64 && method != LLA_RESIDUAL_EXACT_SLICES))
+        return lla__set_status(err, LLA_ERR_INVALID_ARG);
+    lla__set_status(err, LLA_OK);
+    if (n == 0 || m == 0) return LLA_OK;
+    Ctx *c = get_ctx(err);
+    if (!c) return err ? err->code : LLA_ERR_NO_DEVICE;
+    cudaStream_t st = (cudaStream_t)stream;
+    MixedWs &w = c->mixed;
+    MX_TRY(w.words.ensure(sizeof(double) * (8 + 3 * m)));
+    double *colmax_r = (double *)w.words.p + 8, *colmax_x = colmax_r + m;
+    int *err_word = (int *)((double *)w.words.p + 3) + 1;
+    MX_TRY(cudaMemsetAsync(w.words.p, 0, sizeof(double) * (8 + 3 * m), st));
+    if (method == LLA_RESIDUAL_FP64) {
+        MX_TRY(w.P.ensure(sizeof(double) * n * m * residual_splits(n, m)));
+        MX_TRY(last_err(residual_launch(dA, lda, n, dX, ldx, dB, ldb, dR, ldr, m, colmax_r,
+                                        (double *)w.P.p, st)));
+    } else {
+        MX_TRY(w.oz.ensure(oz_workspace_bytes(n, m)));
+        MX_TRY(last_err(oz_prepare(dA, lda, n, m, w.oz.p, st)));
+        MX_TRY(last_err(colmax_launch(dX, ldx, n, m, colmax_x, st)));
+        MX_TRY(last_err(oz_residual_launch(dX, ldx, dB, ldb, dR, ldr, n, m, colmax_x, colmax_r, w.oz.p,
+                                           err_word, st)));
+    }
+    int flag = 0;
+    MX_TRY(cudaMemcpyAsync(&flag, err_word, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MX_TRY(cudaStreamSynchronize(st));
+    if (flag) return lla__set_status(err, flag);
     return LLA_OK;
 }

@@ -26,4 +26,12 @@ int residual_launch(const double *A, int64_t lda, int64_t n, const double *X, in
                     const double *B, int64_t ldb, double *R, int64_t ldr, int64_t m, double *colmax_r,
                     double *P, cudaStream_t st);
 
+// Exact-slice (tensor-core) residual: workspace size, once-per-solve slicing
+// of A, and the per-iteration residual (colmax_x: column maxima of |X|).
+size_t oz_workspace_bytes(int64_t n, int64_t m);
+int oz_prepare(const double *A, int64_t lda, int64_t n, int64_t m, void *ws, cudaStream_t st);
+int oz_residual_launch(const double *X, int64_t ldx, const double *B, int64_t ldb, double *R, int64_t ldr,
+                       int64_t n, int64_t m, const double *colmax_x, double *colmax_r, void *ws,
+                       int *err_word, cudaStream_t st);
+
 }  // namespace lla

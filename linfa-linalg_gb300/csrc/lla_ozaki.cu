@@ -1,0 +1,473 @@
+// lla_ozaki.cu -- FP64-accurate refinement residual R = B - A_sym X on the
+// BF16 tensor cores by exact integer slices (the Ozaki scheme).
+//
+// Each row of A_sym is scaled by a power of two 2^e_i (e_i above its largest
+// magnitude) and cut into S = 8 slices of 7 bits:
+//     a_ik = 2^e_i * sum_{p<S} alpha_p[i,k] 2^-7(p+1)  (+ a remainder below 2^-57),
+// with integer alpha_p in [-128, 128], exactly representable in BF16.  Each
+// column of X is sliced the same way with its own exponent f_j.  Then
+//     (A X)_ij = 2^(e_i + f_j) sum_d 2^-7(d+2) sum_{p+q=d} sum_k alpha_p[i,k] xi_q[j,k]
+// and the terms with d = p + q < S are kept (the dropped ones lie below
+// 2^-56 of 2^(e_i+f_j) per product).  Every product alpha*xi is an integer of
+// at most 14 bits; the tensor core sums them in FP32, which is exact as long
+// as a partial sum stays below 2^24: the kernel drains the tensor-memory
+// accumulator every G_d = 16 / (d+1) K-chunks of 64 (at most 16 x 64 terms of
+// 2^14), converts the drained integer exactly and accumulates it in a 64-bit
+// integer per level d; the levels are combined in FP64 at the end.  So the only
+// rounding errors are those of the final FP64 combination and subtraction,
+// like an FP64 GEMM's epilogue -- the residual is as accurate as an FP64 one,
+// computed on the BF16 pipe.
+//
+// Slices of A are built once per solve (A does not change during the
+// refinement); slices of X once per iteration.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "lla_common.cuh"
+#include "lla_mixed.h"
+#include "lla_prof.h"
+#include "lla_tcgen05.cuh"
+
+namespace lla {
+
+constexpr int kOzS = 8;                      // slices
+constexpr int kOzM = 128, kOzN = 64, kOzK = 64;
+constexpr int kOzStages = 4;
+constexpr int kOzATile = kOzM * kOzK * 2;    // 16 KiB
+constexpr int kOzBTile = kOzN * kOzK * 2;    // 8 KiB
+constexpr int kOzSmem = 1024 + kOzStages * (kOzATile + kOzBTile) + 256;
+constexpr int kOzThreads = 320;              // 8 epilogue warps + producer + MMA
+constexpr uint32_t kOzCols = 2 * kOzN;       // two FP32 accumulators of 64 columns
+
+__device__ __forceinline__ int oz_group(int d) { return max(1, 16 / (d + 1)); }
+
+// ---- slicing ---------------------------------------------------------------
+
+__device__ __forceinline__ void atomic_max_bits(double *addr, double v) {
+    if (!(v >= 0.0)) v = __longlong_as_double(0x7ff0000000000000ll);  // NaN -> +inf
+    atomicMax((unsigned long long *)addr, (unsigned long long)__double_as_longlong(v));
+}
+
+// rowmax[i] = max_k |A_sym(i, k)| from the lower triangle (one block per
+// 32-column strip, as the symmetric row sums).
+__global__ void __launch_bounds__(256) oz_rowmax_kernel(const double *__restrict__ A, int64_t lda,
+                                                        int64_t n, double *rowmax) {
+    __shared__ double red[8][32];
+    const int64_t k0 = (int64_t)blockIdx.x * 32;
+    double colp[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) colp[c] = 0.0;
+    for (int64_t i = k0 + threadIdx.x; i < n; i += blockDim.x) {
+        double racc = 0.0;
+#pragma unroll
+        for (int c = 0; c < 32; ++c) {
+            const int64_t k = k0 + c;
+            if (k < n && k <= i) {
+                const double v = fabs(A[i + k * lda]);
+                racc = fmax(racc, v);
+                if (k != i) colp[c] = fmax(colp[c], v);
+            }
+        }
+        atomic_max_bits(&rowmax[i], racc);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int c = 0; c < 32; ++c) {
+        double v = colp[c];
+#pragma unroll
+        for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0) red[warp][c] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32 && k0 + threadIdx.x < n) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v = fmax(v, red[w][threadIdx.x]);
+        atomic_max_bits(&rowmax[k0 + threadIdx.x], v);
+    }
+}
+
+// Exponent with |v| < 2^e (0 for v == 0); non-finite -> a flag value.
+__device__ __forceinline__ int oz_exponent(double v) { return v > 0.0 ? ilogb(v) + 1 : 0; }
+
+__device__ __forceinline__ void oz_slices(double t, __nv_bfloat16 (&q)[kOzS]) {
+#pragma unroll
+    for (int p = 0; p < kOzS; ++p) {
+        t *= 128.0;            // exact
+        const double r = rint(t);  // |r| <= 128
+        q[p] = __double2bfloat16(r);  // exact: an integer of at most 8 bits
+        t -= r;                // exact
+    }
+}
+
+// Slices of A_sym, planes [p][i][k] (row-major, row stride ldp >= n, zero for
+// k >= n).  32 x 32 tiles through shared memory: lower tiles read column-major
+// A coalesced along i, upper tiles (mirrored) along k.
+__global__ void __launch_bounds__(256) oz_slice_a_kernel(const double *__restrict__ A, int64_t lda,
+                                                         int64_t n, int64_t ldp,
+                                                         const double *__restrict__ rowmax,
+                                                         __nv_bfloat16 *planes, int64_t plane_stride) {
+    __shared__ double tile[32][33];
+    const int64_t i0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
+    const bool upper = k0 > i0;  // strictly above the diagonal block: mirror of a lower tile
+    for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
+        int r, c;
+        if (upper) {
+            c = e % 32;
+            r = e / 32;  // consecutive e -> consecutive k -> A[k + i*lda]
+        } else {
+            r = e % 32;
+            c = e / 32;  // consecutive e -> consecutive i -> A[i + k*lda]
+        }
+        const int64_t i = i0 + r, k = k0 + c;
+        double v = 0.0;
+        if (i < n && k < n) v = (k <= i) ? A[i + k * lda] : A[k + i * lda];
+        tile[r][c] = v;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
+        const int r = e / 32, c = e % 32;  // consecutive e -> consecutive k in the output row
+        const int64_t i = i0 + r, k = k0 + c;
+        if (i >= n || k >= ldp) continue;
+        const double rm = rowmax[i];
+        __nv_bfloat16 q[kOzS];
+        oz_slices(isfinite(rm) ? ldexp(tile[r][c], -oz_exponent(rm)) : 0.0, q);
+#pragma unroll
+        for (int p = 0; p < kOzS; ++p) planes[p * plane_stride + i * ldp + k] = q[p];
+    }
+}
+
+// Slices of X^T, planes [q][j][k] (m_pad = 64 rows, zero for j >= m or k >= n).
+__global__ void oz_slice_x_kernel(const double *__restrict__ X, int64_t ldx, int64_t n, int64_t m,
+                                  int64_t ldp, const double *__restrict__ colmax,
+                                  __nv_bfloat16 *planes, int64_t plane_stride) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t j = blockIdx.y;
+    if (k >= ldp) return;
+    double t = 0.0;
+    if (j < m && k < n) {
+        const double cm = colmax[j];
+        t = isfinite(cm) ? ldexp(X[k + j * ldx], -oz_exponent(cm)) : 0.0;
+    }
+    __nv_bfloat16 q[kOzS];
+    oz_slices(t, q);
+#pragma unroll
+    for (int p = 0; p < kOzS; ++p) planes[p * plane_stride + j * ldp + k] = q[p];
+}
+
+// ---- the tensor-core kernel ------------------------------------------------
+
+// Stage schedule shared by the three roles: level d, groups of G_d K-chunks,
+// pairs (p, d - p).
+__global__ void __launch_bounds__(kOzThreads, 1) oz_residual_kernel(
+    const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmX, int64_t n,
+    int64_t m, int kchunks, int splits, double *F, int *err_word) {
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ int s_abort;
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *sA = smem;
+    uint8_t *sB = smem + kOzStages * kOzATile;
+    uint64_t *bars = (uint64_t *)(sB + kOzStages * kOzBTile);
+    uint32_t *tslot = (uint32_t *)(bars + 2 * kOzStages + 4);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kOzStages);
+    const uint32_t tfull0 = smem_u32(bars + 2 * kOzStages), tempty0 = tfull0 + 16;
+    const int row0 = (int)blockIdx.x * kOzM;
+    const int z = blockIdx.y;
+    const int cps = (kchunks + splits - 1) / splits;
+    const int kc_beg = z * cps, kc_end = min(kchunks, kc_beg + cps);
+    if (tid == 0) {
+        for (int s = 0; s < kOzStages; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(tfull0 + 8 * a, 1);
+            mbar_init(tempty0 + 8 * a, 256);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tslot)),
+                     "r"(kOzCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    // instruction descriptor: D F32, A/B BF16, K-major, N = 64, M = 128
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kOzN >> 3) << 17) |
+                           ((uint32_t)(kOzM >> 4) << 24);
+
+    if (warp == 8) {
+        if (lane == 0) {  // TMA producer
+            int64_t g = 0;
+            for (int d = 0; d < kOzS && !*(volatile int *)&s_abort; ++d) {
+                const int plo = max(0, d - (kOzS - 1)), phi = min(d, kOzS - 1);
+                for (int kc = kc_beg; kc < kc_end; ++kc) {
+                    for (int p = plo; p <= phi; ++p, ++g) {
+                        const int s = (int)(g % kOzStages);
+                        const int64_t round = g / kOzStages;
+                        if (round > 0 &&
+                            !mbar_wait(empty0 + 8 * s, (uint32_t)((round - 1) & 1), err_word)) {
+                            s_abort = 1;
+                            break;
+                        }
+                        mbar_expect_tx(full0 + 8 * s, kOzATile + kOzBTile);
+                        tma_load_3d(smem_u32(sA + s * kOzATile), &tmA, kc * kOzK, row0, p, full0 + 8 * s);
+                        tma_load_3d(smem_u32(sB + s * kOzBTile), &tmX, kc * kOzK, 0, d - p, full0 + 8 * s);
+                    }
+                    if (*(volatile int *)&s_abort) break;
+                }
+            }
+        }
+    } else if (warp == 9) {
+        if (lane == 0) {  // MMA issuer
+            int64_t g = 0, grp = 0;
+            for (int d = 0; d < kOzS && !*(volatile int *)&s_abort; ++d) {
+                const int plo = max(0, d - (kOzS - 1)), phi = min(d, kOzS - 1);
+                const int G = oz_group(d);
+                for (int kg = kc_beg; kg < kc_end; kg += G, ++grp) {
+                    const int a = (int)(grp & 1);
+                    const int64_t use = grp >> 1;
+                    if (use > 0 && !mbar_wait(tempty0 + 8 * a, (uint32_t)((use - 1) & 1), err_word)) {
+                        s_abort = 1;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t dt = tmem + (uint32_t)(a * kOzN);
+                    bool first = true;
+                    for (int kc = kg; kc < min(kc_end, kg + G); ++kc) {
+                        for (int p = plo; p <= phi; ++p, ++g) {
+                            const int s = (int)(g % kOzStages);
+                            if (!mbar_wait(full0 + 8 * s, (uint32_t)((g / kOzStages) & 1), err_word)) {
+                                s_abort = 1;
+                                break;
+                            }
+                            tc_fence_after();
+                            const uint32_t a0 = smem_u32(sA + s * kOzATile);
+                            const uint32_t b0 = smem_u32(sB + s * kOzBTile);
+#pragma unroll
+                            for (int k = 0; k < kOzK / 16; ++k) {
+                                tc_mma(dt, sw128_desc(a0 + 32 * k), sw128_desc(b0 + 32 * k), idesc,
+                                       first ? 0u : 1u);
+                                first = false;
+                            }
+                            tc_commit(empty0 + 8 * s);
+                        }
+                        if (*(volatile int *)&s_abort) break;
+                    }
+                    if (*(volatile int *)&s_abort) break;
+                    tc_commit(tfull0 + 8 * a);
+                }
+            }
+        }
+    } else {  // epilogue: warp w drains lane quarter w % 4, columns 32 (w / 4) ..
+        const int qw = warp & 3, half = warp >> 2;
+        const int r = qw * 32 + lane;
+        long long I[32];
+        double acc[32];
+#pragma unroll
+        for (int c = 0; c < 32; ++c) acc[c] = 0.0;
+        int64_t grp = 0;
+        bool ok = true;
+        for (int d = 0; d < kOzS && ok; ++d) {
+            const int G = oz_group(d);
+#pragma unroll
+            for (int c = 0; c < 32; ++c) I[c] = 0;
+            for (int kg = kc_beg; kg < kc_end; kg += G, ++grp) {
+                const int a = (int)(grp & 1);
+                const int64_t use = grp >> 1;
+                bool w = mbar_wait(tfull0 + 8 * a, (uint32_t)(use & 1), err_word);
+                w = __all_sync(0xffffffffu, w) && !*(volatile int *)&s_abort;
+                if (!w) {
+                    if (lane == 0) s_abort = 1;
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                uint32_t v[32];
+                tc_ld32(tmem + (uint32_t)(a * kOzN) + ((uint32_t)(qw * 32) << 16) + (uint32_t)(half * 32), v);
+#pragma unroll
+                for (int c = 0; c < 32; ++c) I[c] += (long long)__float2int_rn(__uint_as_float(v[c]));
+                tc_fence_before();
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tempty0 + 8 * a) : "memory");
+            }
+            const double w = ldexp(1.0, -7 * (d + 2));
+#pragma unroll
+            for (int c = 0; c < 32; ++c) acc[c] = fma((double)I[c], w, acc[c]);
+        }
+        const int64_t i = row0 + r;
+        if (ok && i < n) {
+            double *Fz = F + (int64_t)z * n * m;
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+                const int64_t j = half * 32 + c;
+                if (j < m) Fz[i + j * n] = acc[c];
+            }
+        }
+    }
+    __syncwarp();
+    __syncthreads();
+    if (s_abort && tid == 0) atomicCAS(err_word, 0, (int)LLA_ERR_TIMEOUT);
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kOzCols)
+                     : "memory");
+}
+
+// R = B - 2^(e_i + f_j) (F_0 + F_1 + ...), column maxima of |R|; a non-finite
+// row or column scale (non-finite data) yields NaN, which the refinement treats
+// as a stall.
+__global__ void oz_combine_kernel(const double *__restrict__ F, int splits, const double *B, int64_t ldb,
+                                  const double *__restrict__ rowmax, const double *__restrict__ colmax_x,
+                                  double *R, int64_t ldr, int64_t n, int64_t m, double *colmax_r) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t j = blockIdx.y;
+    double v = 0.0;
+    if (i < n) {
+        double s = F[i + j * n];
+        for (int zz = 1; zz < splits; ++zz) s += F[(int64_t)zz * n * m + i + j * n];
+        const double rm = rowmax[i], cm = colmax_x[j];
+        double r;
+        if (!isfinite(rm) || !isfinite(cm))
+            r = __longlong_as_double(0x7ff8000000000000ll);
+        else
+            r = B[i + j * ldb] - ldexp(s, oz_exponent(rm) + oz_exponent(cm));
+        R[i + j * ldr] = r;
+        v = fabs(r);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) atomic_max_bits(&colmax_r[j], v);
+}
+
+// ---- host side -------------------------------------------------------------
+
+static int64_t oz_ldp(int64_t n) { return (n + kOzK - 1) / kOzK * kOzK; }
+
+size_t oz_workspace_bytes(int64_t n, int64_t m) {
+    const int64_t ldp = oz_ldp(n);
+    return (size_t)kOzS * n * ldp * 2        // A slices
+           + (size_t)kOzS * kOzN * ldp * 2   // X slices (one 64-column group)
+           + (size_t)n * 8                   // row maxima
+           + (size_t)4 * n * std::min<int64_t>(m, kOzN) * 8 + 4096;  // split partials
+}
+
+struct OzState {
+    __nv_bfloat16 *A, *X;
+    double *rowmax, *F;
+    int64_t ldp;
+    CUtensorMap tmA, tmX;
+    int splits;
+};
+
+static int oz_splits(int64_t n) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    const int64_t tiles = (n + kOzM - 1) / kOzM;
+    int s = 1;
+    while (s < 4 && tiles * s < (int64_t)sms && (oz_ldp(n) / kOzK) / (s + 1) >= 8) ++s;
+    return s;
+}
+
+static void oz_carve(void *ws, int64_t n, int64_t m, OzState &o) {
+    o.ldp = oz_ldp(n);
+    char *p = (char *)ws;
+    o.A = (__nv_bfloat16 *)p;
+    p += (size_t)kOzS * n * o.ldp * 2;
+    o.X = (__nv_bfloat16 *)p;
+    p += (size_t)kOzS * kOzN * o.ldp * 2;
+    o.rowmax = (double *)p;
+    p += (size_t)n * 8;
+    o.F = (double *)p;
+    o.splits = oz_splits(n);
+}
+
+// Once per solve: row maxima and slices of A.
+int oz_prepare(const double *A, int64_t lda, int64_t n, int64_t m, void *ws, cudaStream_t st) {
+    OzState o;
+    oz_carve(ws, n, m, o);
+    if (cudaMemsetAsync(o.rowmax, 0, sizeof(double) * n, st) != cudaSuccess) return -1;
+    {
+        LaunchScope ls(K_OZ_SLICE, st, 8.0 * n * n);
+        oz_rowmax_kernel<<<(unsigned)((n + 31) / 32), 256, 0, st>>>(A, lda, n, o.rowmax);
+    }
+    {
+        LaunchScope ls(K_OZ_SLICE, st, 8.0 * n * n + 2.0 * kOzS * n * o.ldp);
+        oz_slice_a_kernel<<<dim3((unsigned)((o.ldp + 31) / 32), (unsigned)((n + 31) / 32)), 256, 0, st>>>(
+            A, lda, n, o.ldp, o.rowmax, o.A, n * o.ldp);
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+// Every iteration: R = B - A_sym X for up to 64 columns at a time.
+int oz_residual_launch(const double *X, int64_t ldx, const double *B, int64_t ldb, double *R, int64_t ldr,
+                       int64_t n, int64_t m, const double *colmax_x, double *colmax_r, void *ws,
+                       int *err_word, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(oz_residual_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kOzSmem) !=
+            cudaSuccess)
+            return -1;
+        attr = true;
+    }
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tma_encoder();
+    if (!enc) return -1;
+    OzState o;
+    oz_carve(ws, n, m, o);
+    const cuuint32_t estr[3] = {1, 1, 1};
+    {
+        const cuuint64_t dims[3] = {(cuuint64_t)o.ldp, (cuuint64_t)n, (cuuint64_t)kOzS};
+        const cuuint64_t strides[2] = {(cuuint64_t)o.ldp * 2, (cuuint64_t)n * o.ldp * 2};
+        const cuuint32_t box[3] = {(cuuint32_t)kOzK, (cuuint32_t)kOzM, 1};
+        if (enc(&o.tmA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, o.A, dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return -1;
+    }
+    {
+        const cuuint64_t dims[3] = {(cuuint64_t)o.ldp, (cuuint64_t)kOzN, (cuuint64_t)kOzS};
+        const cuuint64_t strides[2] = {(cuuint64_t)o.ldp * 2, (cuuint64_t)kOzN * o.ldp * 2};
+        const cuuint32_t box[3] = {(cuuint32_t)kOzK, (cuuint32_t)kOzN, 1};
+        if (enc(&o.tmX, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, o.X, dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return -1;
+    }
+    const int kchunks = (int)(o.ldp / kOzK);
+    for (int64_t c0 = 0; c0 < m; c0 += kOzN) {
+        const int64_t mc = std::min<int64_t>(kOzN, m - c0);
+        {
+            LaunchScope ls(K_OZ_SLICE, st, 8.0 * n * mc + 2.0 * kOzS * kOzN * o.ldp);
+            oz_slice_x_kernel<<<dim3((unsigned)((o.ldp + 255) / 256), kOzN), 256, 0, st>>>(
+                X + c0 * ldx, ldx, n, mc, o.ldp, colmax_x + c0, o.X, kOzN * o.ldp);
+        }
+        {
+            // algorithmic work: 2 n^2 mc flops of the FP64 product it replaces
+            LaunchScope ls(K_RESIDUAL, st, 2.0 * n * n * mc);
+            oz_residual_kernel<<<dim3((unsigned)((n + kOzM - 1) / kOzM), (unsigned)o.splits), kOzThreads,
+                                 kOzSmem, st>>>(o.tmA, o.tmX, n, mc, kchunks, o.splits, o.F, err_word);
+        }
+        {
+            LaunchScope ls(K_REFINE, st, 8.0 * n * mc * (o.splits + 2));
+            oz_combine_kernel<<<dim3((unsigned)((n + 255) / 256), (unsigned)mc), 256, 0, st>>>(
+                o.F, o.splits, B + c0 * ldb, ldb, o.rowmax, colmax_x + c0, R + c0 * ldr, ldr, n, mc,
+                colmax_r + c0);
+        }
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace lla

@@ -15,7 +15,7 @@ static const char *kNames[K_COUNT] = {
     "potrf_fast_panel", "potrf_fast_update", "trsm",              "layout",
     "mixed_diag",       "mixed_panel",       "mixed_update",      "mixed_convert",
     "residual",         "refine",            "mixed_trsm",        "batch",
-    "misc"};
+    "oz_slice",         "misc"};
 
 const char *kernel_name(int id) { return (id >= 0 && id < K_COUNT) ? kNames[id] : "?"; }
 

@@ -30,6 +30,7 @@ enum KernelId {
     K_REFINE,
     K_MIXED_TRSM,
     K_BATCH,
+    K_OZ_SLICE,
     K_MISC,
     K_COUNT
 };

@@ -23,6 +23,7 @@
 
 #include "lla_common.cuh"
 #include "lla_tc.h"
+#include "lla_tcgen05.cuh"
 
 namespace lla {
 
@@ -30,101 +31,7 @@ constexpr int kTcM = 128, kTcN = 128, kTcK = 64;  // tile and K-chunk
 constexpr int kTcStages = 6;
 constexpr int kTcTileBytes = kTcM * kTcK * 2;  // 16 KiB per operand per stage
 constexpr int kTcSmem = 1024 + 2 * kTcStages * kTcTileBytes + 256;
-constexpr long long kTcSpin = 1ll << 22;  // polls per wait (well under a second of polling)
 constexpr uint32_t kTcCols = 128;  // tensor-memory columns (FP32 128 x 128 accumulator)
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n"
-        " .reg .pred p;\n"
-        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n"
-        "}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait on an mbarrier phase; false when the limit expired or another
-// CTA has already reported a failure.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, const int *err_word) {
-    for (long long i = 0; i < kTcSpin; ++i) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if ((i & 1023) == 1023 && *(volatile const int *)err_word != 0) return false;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y, int z,
-                                            uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
-        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(bar)
-        : "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() {
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-
-// Shared-memory matrix descriptor of a K-major operand tile stored with the
-// 128-byte swizzle: rows of 128 bytes, 8-row (1024-byte) swizzle atoms
-// stacked along M (stride byte offset 1024); the leading byte offset is not
-// used by swizzled K-major layouts; bit 46 is the Blackwell descriptor version.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
-    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) |
-           ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
-}
-
-__device__ __forceinline__ void tc_mma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                       uint32_t accumulate) {
-    asm volatile(
-        "{\n"
-        " .reg .pred p;\n"
-        " setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
-        "}\n" ::"r"(dtmem),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-        : "memory");
-}
-
-__device__ __forceinline__ void tc_commit(uint32_t bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-                 : "memory");
-}
-
-__device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-          "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]),
-          "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]),
-          "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
 
 __device__ __forceinline__ void tc_tri_tile(int64_t t, int64_t &I, int64_t &J) {
     int64_t i = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
@@ -306,16 +213,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
 
 static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
-int tc_update_prepare() {
+PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
     if (!g_encode) {
         void *fn = nullptr;
         cudaDriverEntryPointQueryResult qres;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
-                                             &qres) != cudaSuccess ||
-            qres != cudaDriverEntryPointSuccess || !fn)
-            return -1;
-        g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+                                             &qres) == cudaSuccess &&
+            qres == cudaDriverEntryPointSuccess && fn)
+            g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
     }
+    return g_encode;
+}
+
+int tc_update_prepare() {
+    if (!tma_encoder()) return -1;
     if (cudaFuncSetAttribute(tc_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) !=
         cudaSuccess)
         return -1;

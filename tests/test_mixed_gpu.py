@@ -147,3 +147,45 @@ def test_lowp_factor_accuracy(gpu_lla, update, n):
     L = np.tril(A.cpu().numpy().astype(np.float64))
     rel = np.linalg.norm(L @ L.T - a) / np.linalg.norm(a)
     assert rel <= FACTOR_TOL[update], rel
+
+
+@pytest.mark.parametrize("n,m", [(200, 3), (1000, 64), (4099, 17)])
+def test_exact_slice_residual_matches_fp64(gpu_lla, n, m):
+    """The tensor-core exact-slice residual against an extended-precision
+    reference: both it and the FP64 residual must be within ~FP64 rounding of
+    the exact B - A X (relative to |A| |x|, the scale of the cancellation)."""
+    torch = pytest.importorskip("torch")
+    lla = gpu_lla
+    rng = np.random.default_rng(n)
+    a = qdq(rng, n, 1e6) * 10.0 ** rng.uniform(-3, 3)
+    x = rng.standard_normal((n, m)) * 10.0 ** rng.uniform(-2, 2, m)
+    b = a @ x + 1e-9 * rng.standard_normal((n, m))  # residual ~1e-9: heavy cancellation
+    A = torch.tensor(a, device="cuda").T.contiguous().T
+    X = torch.tensor(x, device="cuda").T.contiguous().T
+    B = torch.tensor(b, device="cuda").T.contiguous().T
+    R1 = torch.empty_like(B.T.contiguous()).T
+    R2 = torch.empty_like(B.T.contiguous()).T
+    lla.residual_device(A, X, B, R1, "fp64")
+    lla.residual_device(A, X, B, R2, "slices")
+    torch.cuda.synchronize()
+    # extended-precision reference with numpy longdouble where available
+    ref = (b.astype(np.longdouble) - a.astype(np.longdouble) @ x.astype(np.longdouble)).astype(np.float64)
+    scale = (np.abs(a) @ np.abs(x))
+    e1 = (np.abs(R1.cpu().numpy() - ref) / scale).max()
+    e2 = (np.abs(R2.cpu().numpy() - ref) / scale).max()
+    assert e1 <= 1e-14, e1
+    assert e2 <= 1e-14, e2
+
+
+def test_refined_with_exact_slice_residual(gpu_lla):
+    lla = gpu_lla
+    rng = np.random.default_rng(31)
+    n = 1500
+    a = qdq(rng, n, 1e6)
+    b = rng.standard_normal((n, 8))
+    x1, x2 = b.copy(), b.copy()
+    r1 = lla.posv_refined(a, x1)
+    r2 = lla.posv_refined(a, x2, residual="slices")
+    assert r2["converged"] == 1 and r2["fell_back"] == 0
+    assert backward_error(a, x2, b) <= 2e-13
+    assert abs(r1["iterations"] - r2["iterations"]) <= 1
