@@ -211,6 +211,9 @@ def main():
     ap.add_argument("--update", default="bf16x6",
                     help="trailing-update form of the mixed path: fp32|bf16|bf16x3|bf16x6|fp16|fp16x3")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed steps of the plain FP64 leg")
+    ap.add_argument("--residual", default="fp64", choices=["fp64", "slices"],
+                    help="refinement residual of the headline: FP64 MMA pipe, or exact BF16 slices")
+    ap.add_argument("--no-alt", action="store_true", help="skip timing the other residual method")
     ap.add_argument("--workload", default="single", choices=["single", "batch", "serve", "sweep"],
                     help="single: the n=16384 system (the headline); batch: 10,000 uneven small systems")
     ap.add_argument("--batch-count", type=int, default=10000)
@@ -273,8 +276,9 @@ def main():
 
     reports = []
 
-    def mixed_step():
-        reports.append(lla.posv_refined_device(A0c, B0c, Xm, stream=stream, update=args.update))
+    def mixed_step(residual=args.residual):
+        reports.append(lla.posv_refined_device(A0c, B0c, Xm, stream=stream, update=args.update,
+                                               residual=residual))
 
     # correctness gates (outside the timed regions)
     plain_step()
@@ -324,6 +328,20 @@ def main():
     timed_reports = reports[-args.steps:]
     mixed_sps = world * args.steps / (ms_mixed / 1e3)
     assert all(r["backward_error"] <= BE_TARGET for r in timed_reports), timed_reports
+    # the other residual method, timed the same way (reported beside the headline)
+    alt = None
+    if not args.no_alt:
+        other = "slices" if args.residual == "fp64" else "fp64"
+        reports.clear()
+        ms_alt, _, prof_alt, _ = timed(lambda: mixed_step(other), args.steps, 1, profile=True)
+        torch.cuda.synchronize()
+        be_alt = backward_error(torch, A0, Xm, B0)
+        assert be_alt <= BE_TARGET and all(r["backward_error"] <= BE_TARGET for r in reports), be_alt
+        alt = {"residual": other, "value": world * args.steps / (ms_alt / 1e3), "unit": "solves/s",
+               "ms_per_step": ms_alt / args.steps, "iterations": reports[-1]["iterations"],
+               "backward_error": be_alt,
+               "kernels": {k: {"ms": v[0] / args.steps, "launches": v[1] // args.steps}
+                           for k, v in prof_alt.items()}}
 
     # roofline of the dominant kernel of the headline (mixed) step
     fp64_peak = lla.measure_peak_tflops(0)
@@ -364,7 +382,7 @@ def main():
         for it in range(k_e2e + 1):
             Bh.copy_(B0_cpu)
             t0 = time.perf_counter()
-            lla.posv_refined(Ah.numpy(), Bh.numpy(), update=args.update)
+            lla.posv_refined(Ah.numpy(), Bh.numpy(), update=args.update, residual=args.residual)
             dt = time.perf_counter() - t0
             if it > 0:
                 tot += dt
@@ -383,7 +401,7 @@ def main():
             "data": "synthetic (seeded Q diag(s) Q^T, built on the device)",
             "config": {"workload": f"single SPD solve n={n} nrhs={m} kappa=1e6",
                        "path": f"mixed: equilibrated low-precision Cholesky ({args.update} trailing "
-                               f"updates) + FP64 refinement, FP64 fallback",
+                               f"updates) + FP64 refinement ({args.residual} residual), FP64 fallback",
                        "l2": "inputs larger than L2 (A = %.2f GB)" % (n * n * 8 / 1e9),
                        "parallelism": "replicas" if world > 1 else "single"},
             "backward_error": max(r["backward_error"] for r in timed_reports),
@@ -395,6 +413,7 @@ def main():
                            "ms_per_step": ms_plain / k_plain, "backward_error": be_plain,
                            "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof_plain.items()}},
             "mixed_over_plain": mixed_sps / plain_sps,
+            "other_residual": alt,
             "gflops": flops_solve(n, m) * mixed_sps / 1e9,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": launches,
