@@ -3,8 +3,9 @@
 //
 // Each row of A_sym is scaled by a power of two 2^e_i (e_i above its largest
 // magnitude) and cut into S = 8 slices of 7 bits:
-//     a_ik = 2^e_i * sum_{p<S} alpha_p[i,k] 2^-7(p+1)  (+ a remainder below 2^-57),
-// with integer alpha_p in [-128, 128], exactly representable in BF16.  Each
+//     a_ik = 2^e_i * sum_{p<S} alpha_p[i,k] 2^-7(p+1)  (+ a remainder below 2^-56),
+// with integer alpha_p in [-127, 127] (the digits of |a|, carrying a's sign),
+// exactly representable in BF16.  Each
 // column of X is sliced the same way with its own exponent f_j.  Then
 //     (A X)_ij = 2^(e_i + f_j) sum_d 2^-7(d+2) sum_{p+q=d} sum_k alpha_p[i,k] xi_q[j,k]
 // and the terms with d = p + q < S are kept (the dropped ones lie below
@@ -92,13 +93,34 @@ __global__ void __launch_bounds__(256) oz_rowmax_kernel(const double *__restrict
 // Exponent with |v| < 2^e (0 for v == 0); non-finite -> a flag value.
 __device__ __forceinline__ int oz_exponent(double v) { return v > 0.0 ? ilogb(v) + 1 : 0; }
 
-__device__ __forceinline__ void oz_slices(double t, __nv_bfloat16 (&q)[kOzS]) {
+// Digits of a with respect to the scale 2^e (|a| < 2^e): the magnitude
+// |a| 2^(56 - e) as a 56-bit integer T (low bits truncated -- below 2^-56 of
+// the scale), cut into eight 7-bit digits T = sum_p alpha_p 2^(7 (7 - p)), each
+// carrying the sign of a.  Integer operations only (the FP64 pipe is slow).
+__device__ __forceinline__ void oz_digits(double a, int e, __nv_bfloat16 (&q)[kOzS]) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(a);
+    const int eb = (int)((bits >> 52) & 0x7ff);
+    unsigned long long mant = bits & ((1ull << 52) - 1);
+    int ea;  // a = mant * 2^ea
+    if (eb == 0) {
+        ea = -1074;
+    } else {
+        mant |= 1ull << 52;
+        ea = eb - 1075;
+    }
+    const int shift = ea + 56 - e;  // <= 3 since |a| < 2^e
+    unsigned long long T = 0;
+    if (mant != 0 && eb != 0x7ff) {
+        if (shift >= 0)
+            T = mant << shift;
+        else if (shift > -64)
+            T = mant >> (-shift);
+    }
+    const bool neg = (bits >> 63) != 0;
 #pragma unroll
     for (int p = 0; p < kOzS; ++p) {
-        t *= 128.0;            // exact
-        const double r = rint(t);  // |r| <= 128
-        q[p] = __double2bfloat16(r);  // exact: an integer of at most 8 bits
-        t -= r;                // exact
+        const int d = (int)((T >> (7 * (kOzS - 1 - p))) & 127);
+        q[p] = __int2bfloat16_rn(neg ? -d : d);  // exact: at most 7 bits
     }
 }
 
@@ -133,7 +155,7 @@ __global__ void __launch_bounds__(256) oz_slice_a_kernel(const double *__restric
         if (i >= n || k >= ldp) continue;
         const double rm = rowmax[i];
         __nv_bfloat16 q[kOzS];
-        oz_slices(isfinite(rm) ? ldexp(tile[r][c], -oz_exponent(rm)) : 0.0, q);
+        oz_digits(isfinite(rm) ? tile[r][c] : 0.0, oz_exponent(rm), q);
 #pragma unroll
         for (int p = 0; p < kOzS; ++p) planes[p * plane_stride + i * ldp + k] = q[p];
     }
@@ -147,12 +169,14 @@ __global__ void oz_slice_x_kernel(const double *__restrict__ X, int64_t ldx, int
     const int64_t j = blockIdx.y;
     if (k >= ldp) return;
     double t = 0.0;
+    int e = 0;
     if (j < m && k < n) {
         const double cm = colmax[j];
-        t = isfinite(cm) ? ldexp(X[k + j * ldx], -oz_exponent(cm)) : 0.0;
+        t = isfinite(cm) ? X[k + j * ldx] : 0.0;
+        e = oz_exponent(cm);
     }
     __nv_bfloat16 q[kOzS];
-    oz_slices(t, q);
+    oz_digits(t, e, q);
 #pragma unroll
     for (int p = 0; p < kOzS; ++p) planes[p * plane_stride + j * ldp + k] = q[p];
 }
