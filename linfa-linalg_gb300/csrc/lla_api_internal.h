@@ -30,6 +30,7 @@ struct MixedWs {
     DevBuf L, s, rowsum, R, Y, diag0, words;  // FP32 factor, scaling, norms, residual, correction
     DevBuf P;                                 // split-K partial products of the residual
     DevBuf oz;                                // exact-slice residual: slices of A and X
+    DevBuf winv;                              // inverted 64 x 64 diagonal blocks of L
     DevBuf F, fdiag;                          // plain FP64 fallback
     DevBuf opA, opB;                          // tensor-core operand planes of one panel
     DevBuf tcerr;                             // tensor-core update status word

@@ -443,7 +443,8 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
     MX_TRY(w.Y.ensure(sizeof(float) * n * m));
     MX_TRY(w.diag0.ensure(sizeof(float) * n));
     MX_TRY(w.words.ensure(sizeof(double) * (8 + 3 * m)));
-    MX_TRY(c->ws.ensure(sizeof(int) * (trsm_ws_ints(n, m) + 1)));
+    MX_TRY(c->ws.ensure(sizeof(int) * (std::max(trsm_ws_ints(n, m), trsm_inv_ws_ints(n, m)) + 1)));
+    MX_TRY(w.winv.ensure(sizeof(float) * diag_inverse_floats(n)));
     MX_TRY(w.words_host.ensure(sizeof(double) * (8 + 3 * m)));
     float *L = (float *)w.L.p;
     double *s = (double *)w.s.p;
@@ -491,6 +492,8 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
         std::memcpy(&finfo, hw + 2, sizeof(int64_t));
         if (finfo >= 0) lowp_ok = false;
     }
+    if (lowp_ok)  // inverses of the 64 x 64 diagonal blocks, reused by every substitution
+        MX_TRY(last_err(diag_inverse_launch(L, n, n, (float *)w.winv.p, st)));
     const bool slices = opts.residual == LLA_RESIDUAL_EXACT_SLICES;
     if (lowp_ok && slices) {  // slices of A, once per solve
         MX_TRY(w.oz.ensure(oz_workspace_bytes(n, m)));
@@ -511,8 +514,9 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
             // correction d = S L^-T L^-1 S r  (FP32), x += d
             MX_TRY(last_err(scale_to_f32_launch(rhs, ldrhs, s, n, m, Y, st)));
             MX_TRY(cudaMemsetAsync(err_word, 0, sizeof(int), st));
-            MX_TRY(last_err(trsm_launch<float>(L, n, n, 1, 0, nullptr, Y, n, m, false, tws, err_word, st)));
-            MX_TRY(last_err(trsm_launch<float>(L, n, n, 0, 1, nullptr, Y, n, m, false, tws, err_word, st)));
+            const float *Wi = (const float *)w.winv.p;
+            MX_TRY(last_err(trsm_inv_launch(L, n, Wi, n, Y, n, m, 0, tws, err_word, st)));
+            MX_TRY(last_err(trsm_inv_launch(L, n, Wi, n, Y, n, m, 1, tws, err_word, st)));
             MX_TRY(cudaMemsetAsync(colmax_r, 0, sizeof(double) * 2 * m, st));
             MX_TRY(last_err(update_x_launch(dX, ldx, s, Y, n, m, colmax_x, st)));
             // r = b - A x  (FP64)
