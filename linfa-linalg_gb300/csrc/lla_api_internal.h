@@ -31,6 +31,10 @@ struct MixedWs {
     DevBuf P;                                 // split-K partial products of the residual
     DevBuf oz;                                // exact-slice residual: slices of A and X
     DevBuf winv;                              // inverted 64 x 64 diagonal blocks of L
+    DevBuf stage;                             // epoch-tagged hand-off words of the substitutions
+    void *stage_seen = nullptr;               // stage allocation that was last cleared
+    size_t stage_seen_cap = 0;
+    unsigned stage_epoch = 0;                 // epoch of the last substitution launch
     DevBuf F, fdiag;                          // plain FP64 fallback
     DevBuf opA, opB;                          // tensor-core operand planes of one panel
     DevBuf tcerr;                             // tensor-core update status word

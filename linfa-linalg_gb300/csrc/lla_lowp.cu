@@ -3,8 +3,9 @@
 //
 // Right-looking with panels of nb = 128 columns:
 //   diag   : one CTA factors the 128 x 128 diagonal block in FP32 (32-column
-//            sub-blocks: a one-warp shuffle Cholesky, a row-parallel solve of
-//            the rows below it, a shared-memory update of the rest);
+//            sub-blocks: an unpredicated one-warp shuffle Cholesky, a
+//            row-parallel solve of the rows below it, a shared-memory update
+//            of the rest; a short last block is padded with the identity);
 //   panel  : L21 = A21 L11^-T in FP32, one thread per row, and the operand
 //            planes of L21 for the tensor cores: a one-, two- or three-term
 //            split of every FP32 value into BF16 (or FP16) parts
@@ -35,89 +36,111 @@ namespace lla {
 
 constexpr int kLpNb = 128;  // panel width
 constexpr int kLpLd = kLpNb + 1;
+constexpr int kLpPd = kLpNb + 4;  // row stride of the transposed 32-column panel (16-byte rows)
 
 // ---------------------------------------------------------------------------
 // diagonal block: b <= 128, one CTA of 1024 threads, block in shared memory
 
 __global__ void __launch_bounds__(1024) lowp_diag_kernel(float *L, int64_t ld, int64_t p, int b,
                                                          int64_t *info, double *min_ratio) {
-    extern __shared__ float sa[];  // [128][129]: sa[r * kLpLd + c] = L11[r][c]
+    extern __shared__ float sa[];  // [128][129]: sa[r * kLpLd + c] = L11[r][c]; then sp[32][kLpPd]
+    float *sp = sa + kLpNb * kLpLd;  // sp[t * kLpPd + r] = L11[r][kb + t] for the rows below
+    __shared__ float rdiag[32];      // reciprocals of the current 32 x 32 factor's diagonal
     __shared__ int failed;
     if (*(volatile int64_t *)info >= 0) return;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // A short last block is padded with the identity (blockdiag(A11, I) factors
+    // as blockdiag(L11, I)), so every step below runs unpredicated on 128 rows.
     for (int e = tid; e < kLpNb * kLpNb; e += 1024) {
         const int r = e % kLpNb, c = e / kLpNb;
-        if (r < b && c <= r) sa[r * kLpLd + c] = L[(p + r) + (p + c) * ld];
+        if (c <= r) sa[r * kLpLd + c] = (r < b) ? L[(p + r) + (p + c) * ld] : (r == c ? 1.f : 0.f);
     }
     if (tid == 0) failed = 0;
     __syncthreads();
     float ratio = 1e30f;
-    for (int kb = 0; kb < b; kb += 32) {
-        const int bs = min(32, b - kb);
-        // (1) one warp: Cholesky of the bs x bs block; lane i holds row kb+i
+#pragma unroll 1
+    for (int kb = 0; kb < kLpNb; kb += 32) {
+        // (1) one warp: Cholesky of the 32 x 32 block; lane i holds row kb+i.
+        // The column loop is branch-free (selects only) so that its shuffles
+        // overlap; entries above the diagonal pick up values never read.
         if (warp == 0) {
             float v[32];
 #pragma unroll
-            for (int c = 0; c < 32; ++c)
-                v[c] = (lane < bs && c <= lane) ? sa[(kb + lane) * kLpLd + kb + c] : 0.f;
+            for (int c = 0; c < 32; ++c) v[c] = (c <= lane) ? sa[(kb + lane) * kLpLd + kb + c] : 0.f;
             bool bad = false;
+            float mypiv = 1.f, myd = 1.f;  // this lane's pivot and L[lane][lane]
 #pragma unroll
             for (int c = 0; c < 32; ++c) {
-                if (c < bs) {
-                    const float piv = __shfl_sync(0xffffffffu, v[c], c);
-                    if (!(piv > 0.f)) bad = true;  // non-positive (or NaN) pivot: breakdown
-                    const float rl = rsqrtf(fmaxf(piv, 1e-30f));  // 1 / L[c][c]
-                    if (lane == c) {
-                        v[c] = piv * rl;  // sqrt(piv)
-                        ratio = fminf(ratio, piv);
-                    }
-                    if (lane > c) v[c] = v[c] * rl;
+                const float piv = __shfl_sync(0xffffffffu, v[c], c);
+                bad |= !(piv > 0.f);  // non-positive (or NaN) pivot: breakdown
+                const float rl = rsqrtf(fmaxf(piv, 1e-30f));  // 1 / L[c][c]
+                const float d = piv * rl;
+                mypiv = (lane == c) ? piv : mypiv;
+                myd = (lane == c) ? d : myd;
+                v[c] = (lane == c) ? d : v[c] * rl;
 #pragma unroll
-                    for (int c2 = c + 1; c2 < 32; ++c2) {
-                        const float t = __shfl_sync(0xffffffffu, v[c], c2);
-                        if (c2 < bs && lane >= c2) v[c2] = fmaf(-v[c], t, v[c2]);
-                    }
+                for (int c2 = c + 1; c2 < 32; ++c2) {
+                    const float t = __shfl_sync(0xffffffffu, v[c], c2);
+                    v[c2] = fmaf(-v[c], t, v[c2]);
                 }
             }
+            if (kb + lane < b) ratio = fminf(ratio, mypiv);
             if (lane == 0 && bad) failed = 1;
-            if (lane < bs) {
 #pragma unroll
-                for (int c = 0; c < 32; ++c)
-                    if (c <= lane) sa[(kb + lane) * kLpLd + kb + c] = v[c];
-            }
+            for (int c = 0; c < 32; ++c)
+                if (c <= lane) sa[(kb + lane) * kLpLd + kb + c] = v[c];
+            rdiag[lane] = 1.f / myd;
         }
         __syncthreads();
         if (failed) break;
-        const int rest0 = kb + bs;
-        // (2) rows below inside the block: row r solves against the bs x bs factor
-        if (tid < b - rest0) {
+        const int rest0 = kb + 32;
+        const int w = kLpNb - rest0;
+        // (2) rows below inside the block: row r solves against the 32 x 32 factor
+        if (tid < w) {
             const int r = rest0 + tid;
             float v[32];
 #pragma unroll
-            for (int c = 0; c < 32; ++c) v[c] = (c < bs) ? sa[r * kLpLd + kb + c] : 0.f;
+            for (int c = 0; c < 32; ++c) v[c] = sa[r * kLpLd + kb + c];
 #pragma unroll
             for (int c = 0; c < 32; ++c) {
-                if (c < bs) {
-                    v[c] = __fdividef(v[c], sa[(kb + c) * kLpLd + kb + c]);
+                v[c] *= rdiag[c];
 #pragma unroll
-                    for (int c2 = c + 1; c2 < 32; ++c2)
-                        if (c2 < bs) v[c2] = fmaf(-v[c], sa[(kb + c2) * kLpLd + kb + c], v[c2]);
-                }
+                for (int c2 = c + 1; c2 < 32; ++c2) v[c2] = fmaf(-v[c], sa[(kb + c2) * kLpLd + kb + c], v[c2]);
             }
 #pragma unroll
-            for (int c = 0; c < 32; ++c)
-                if (c < bs) sa[r * kLpLd + kb + c] = v[c];
+            for (int c = 0; c < 32; ++c) {
+                sa[r * kLpLd + kb + c] = v[c];
+                sp[c * kLpPd + r] = v[c];
+            }
         }
         __syncthreads();
-        // (3) trailing part of the block: a[r][c] -= sum_t a[r][kb+t] a[c][kb+t]
-        const int w = b - rest0;
-        for (int e = tid; e < w * w; e += 1024) {
-            const int r = rest0 + e % w, c = rest0 + e / w;
-            if (c <= r) {
-                float acc = sa[r * kLpLd + c];
-                for (int t = 0; t < bs; ++t)
-                    acc = fmaf(-sa[r * kLpLd + kb + t], sa[c * kLpLd + kb + t], acc);
-                sa[r * kLpLd + c] = acc;
+        // (3) trailing part of the block, a[r][c] -= sum_t a[r][kb+t] a[c][kb+t],
+        // in 4 x 4 register tiles on or below the diagonal
+        const int wt = w / 4;
+        for (int e = tid; e < wt * wt; e += 1024) {
+            const int ti = e % wt, tj = e / wt;
+            if (tj <= ti) {
+                const int r0 = rest0 + 4 * ti, c0 = rest0 + 4 * tj;
+                float acc[4][4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[i][j] = sa[(r0 + i) * kLpLd + c0 + j];
+#pragma unroll 8
+                for (int t = 0; t < 32; ++t) {
+                    const float4 a4 = *reinterpret_cast<const float4 *>(&sp[t * kLpPd + r0]);
+                    const float4 b4 = *reinterpret_cast<const float4 *>(&sp[t * kLpPd + c0]);
+                    const float av[4] = {a4.x, a4.y, a4.z, a4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(-av[i], bv[j], acc[i][j]);
+                }
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (c0 + j <= r0 + i) sa[(r0 + i) * kLpLd + c0 + j] = acc[i][j];
             }
         }
         __syncthreads();
@@ -261,7 +284,7 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
     if (c->mixed.tcerr.ensure(sizeof(int)) != cudaSuccess) return -1;
     err_word = (int *)c->mixed.tcerr.p;
     if (cudaMemsetAsync(err_word, 0, sizeof(int), st) != cudaSuccess) return -1;
-    const size_t smem_l11 = sizeof(float) * kLpNb * kLpLd;
+    const size_t smem_l11 = sizeof(float) * (kLpNb * kLpLd + 32 * kLpPd);
     const size_t smem_panel = sizeof(float) * (2 * kLpNb * kLpLd + kLpNb);
     static bool attr_done = false;
     if (!attr_done) {

@@ -445,6 +445,22 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
     MX_TRY(w.words.ensure(sizeof(double) * (8 + 3 * m)));
     MX_TRY(c->ws.ensure(sizeof(int) * (std::max(trsm_ws_ints(n, m), trsm_inv_ws_ints(n, m)) + 1)));
     MX_TRY(w.winv.ensure(sizeof(float) * diag_inverse_floats(n)));
+    MX_TRY(w.stage.ensure(sizeof(unsigned long long) * trsm_inv_stage_words(n, m)));
+    if (w.stage.p != w.stage_seen || w.stage.cap != w.stage_seen_cap) {
+        MX_TRY(cudaMemsetAsync(w.stage.p, 0, w.stage.cap, st));
+        w.stage_seen = w.stage.p;
+        w.stage_seen_cap = w.stage.cap;
+        w.stage_epoch = 0;
+    }
+    auto next_epoch = [&]() -> cudaError_t {  // a fresh nonzero tag per substitution launch
+        if (++w.stage_epoch == 0) {
+            cudaError_t e = cudaMemsetAsync(w.stage.p, 0, w.stage.cap, st);
+            if (e != cudaSuccess) return e;
+            w.stage_epoch = 1;
+        }
+        return cudaSuccess;
+    };
+    unsigned long long *stage = (unsigned long long *)w.stage.p;
     MX_TRY(w.words_host.ensure(sizeof(double) * (8 + 3 * m)));
     float *L = (float *)w.L.p;
     double *s = (double *)w.s.p;
@@ -515,8 +531,10 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
             MX_TRY(last_err(scale_to_f32_launch(rhs, ldrhs, s, n, m, Y, st)));
             MX_TRY(cudaMemsetAsync(err_word, 0, sizeof(int), st));
             const float *Wi = (const float *)w.winv.p;
-            MX_TRY(last_err(trsm_inv_launch(L, n, Wi, n, Y, n, m, 0, tws, err_word, st)));
-            MX_TRY(last_err(trsm_inv_launch(L, n, Wi, n, Y, n, m, 1, tws, err_word, st)));
+            MX_TRY(next_epoch());
+            MX_TRY(last_err(trsm_inv_launch(L, n, Wi, n, Y, n, m, 0, stage, w.stage_epoch, tws, err_word, st)));
+            MX_TRY(next_epoch());
+            MX_TRY(last_err(trsm_inv_launch(L, n, Wi, n, Y, n, m, 1, stage, w.stage_epoch, tws, err_word, st)));
             MX_TRY(cudaMemsetAsync(colmax_r, 0, sizeof(double) * 2 * m, st));
             MX_TRY(last_err(update_x_launch(dX, ldx, s, Y, n, m, colmax_x, st)));
             // r = b - A x  (FP64)

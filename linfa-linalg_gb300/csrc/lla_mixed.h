@@ -27,11 +27,16 @@ int residual_launch(const double *A, int64_t lda, int64_t n, const double *X, in
                     double *P, cudaStream_t st);
 
 // FP32 substitutions with inverted 64 x 64 diagonal blocks (lla_trsm_inv.cu).
+// W: diag_inverse_floats(n) floats (inverses and the two coupling sets);
+// stage: trsm_inv_stage_words(n, m) 64-bit words, zeroed when allocated;
+// epoch: nonzero and different for every launch on the same stage array.
 size_t diag_inverse_floats(int64_t n);
 size_t trsm_inv_ws_ints(int64_t n, int64_t m);
+size_t trsm_inv_stage_words(int64_t n, int64_t m);
 int diag_inverse_launch(const float *L, int64_t ld, int64_t n, float *W, cudaStream_t st);
 int trsm_inv_launch(const float *L, int64_t ld, const float *W, int64_t n, float *B, int64_t ldb,
-                    int64_t m, int trans, int *ws, int *err_word, cudaStream_t st);
+                    int64_t m, int trans, unsigned long long *stage, unsigned epoch, int *ws, int *err_word,
+                    cudaStream_t st);
 
 // Exact-slice (tensor-core) residual: workspace size, once-per-solve slicing
 // of A, and the per-iteration residual (colmax_x: column maxima of |X|).

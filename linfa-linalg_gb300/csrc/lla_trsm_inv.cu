@@ -2,15 +2,24 @@
 // with inverted diagonal blocks.
 //
 // The refinement solves with the same low-precision factor L eight to ten
-// times, so the inverses W_r = L_rr^-1 of its 64 x 64 diagonal blocks are
-// formed once (one CTA per block) and every substitution becomes a chain of
-// small matrix products:
-//     forward  L Y = B  : Y_r = W_r (B_r - sum_{q<r} L_rq Y_q)
-//     backward L^T X = Y: X_r = W_r^T (Y_r - sum_{q>r} L_qr^T X_q)
+// times, so three small matrices per 64-row block are formed once per factor:
+//     W_r  = L_rr^-1                      (diag_inverse_kernel)
+//     F_r  = W_r L_{r,r-1}                (forward coupling, fuse_kernel)
+//     G_r  = W_r^T L_{r+1,r}^T            (backward coupling, fuse_kernel)
+// and every substitution is a chain of small matrix products:
+//     forward  L Y = B  : Y_r = W_r (B_r - sum_{q<r-1} L_rq Y_q) - F_r Y_{r-1}
+//     backward L^T X = Y: X_r = W_r^T (Y_r - sum_{q>r+1} L_qr^T X_q) - G_r X_{r+1}
 // One CTA per (64-row block, 16-column chunk); CTAs take tickets in
-// processing order and wait (bounded) for the blocks they need, as in the
-// look-back substitution of lla_trsm.cu, but with no sequential step inside a
-// block: the critical path per block is two 64 x 64 x 16 products.
+// processing order.  Everything but the last term is computed while the
+// previous block is still being solved, so the only work on the
+// block-to-block critical path is one 64 x 64 x 16 product.
+//
+// Hand-off between CTAs: a solved value is published as one 64-bit word
+// (launch epoch << 32 | float bits) in a staging array, so a consumer polls
+// the data itself -- one memory round trip per hand-off, no separate flag.
+// The host gives every launch a fresh nonzero epoch and clears the staging
+// array whenever it is (re)allocated, so a word from an earlier launch never
+// matches.  Every wait is bounded and reports LLA_ERR_TIMEOUT.
 #include <cuda_runtime.h>
 
 #include "lla_common.cuh"
@@ -19,7 +28,8 @@
 
 namespace lla {
 
-constexpr int kIvNb = 64, kIvCols = 16;
+constexpr int kIvNb = 64;
+constexpr int kIvTile = kIvNb * kIvNb;
 
 // W_r = L_rr^-1 (lower, FP32), padded with the identity past n.  One CTA of
 // 64 threads per block; thread j computes column j by forward substitution.
@@ -28,7 +38,7 @@ __global__ void __launch_bounds__(64) diag_inverse_kernel(const float *__restric
     __shared__ float sL[kIvNb][kIvNb + 1];
     const int64_t r0 = (int64_t)blockIdx.x * kIvNb;
     const int j = threadIdx.x;
-    for (int e = j; e < kIvNb * kIvNb; e += 64) {
+    for (int e = j; e < kIvTile; e += 64) {
         const int i = e % kIvNb, k = e / kIvNb;
         float v = 0.f;
         if (k <= i) {
@@ -54,27 +64,127 @@ __global__ void __launch_bounds__(64) diag_inverse_kernel(const float *__restric
             w[i] = s / sL[i][i];
         }
     }
-    float *Wr = W + (int64_t)blockIdx.x * kIvNb * kIvNb;  // column-major 64 x 64
+    float *Wr = W + (int64_t)blockIdx.x * kIvTile;  // column-major 64 x 64
 #pragma unroll
     for (int i = 0; i < kIvNb; ++i) Wr[i + j * kIvNb] = w[i];
 }
 
-__device__ __forceinline__ int iv_ld_acquire(const int *p) {
-    int v;
-    asm volatile("ld.acquire.gpu.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+// F_r = W_r L_{r,r-1} and G_r = W_r^T L_{r+1,r}^T (zero where the neighbour
+// block does not exist), both column-major 64 x 64.  One CTA of 256 threads
+// per block; thread (i, kq) forms F[i][k] and G[i][k] for k = kq + 4u.
+__global__ void __launch_bounds__(256) fuse_kernel(const float *__restrict__ L, int64_t ld, int64_t n,
+                                                   const float *__restrict__ W, float *F, float *G) {
+    __shared__ float sW[kIvNb][kIvNb + 1];  // sW[a][b] = W_r[a][b]
+    __shared__ float sC[kIvNb][kIvNb + 1];
+    const int64_t r = blockIdx.x, R = gridDim.x;
+    const int tid = threadIdx.x, i = tid % kIvNb, kq = tid / kIvNb;
+    const float *Wr = W + r * kIvTile;
+    for (int e = tid; e < kIvTile; e += 256) sW[e % kIvNb][e / kIvNb] = Wr[e];
+    // forward: sC[j][k] = L[r*64 + j][(r-1)*64 + k]
+    for (int e = tid; e < kIvTile; e += 256) {
+        const int j = e % kIvNb, k = e / kIvNb;
+        const int64_t gi = r * kIvNb + j, gk = (r - 1) * kIvNb + k;
+        sC[j][k] = (r > 0 && gi < n) ? L[gi + gk * ld] : 0.f;
+    }
+    __syncthreads();
+    float acc[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) acc[u] = 0.f;
+    for (int j = 0; j < kIvNb; ++j) {
+        const float wv = sW[i][j];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) acc[u] = fmaf(wv, sC[j][kq + 4 * u], acc[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) F[r * kIvTile + i + (kq + 4 * u) * kIvNb] = acc[u];
+    __syncthreads();
+    // backward: sC[k][j] = L[(r+1)*64 + k][r*64 + j]; G[i][k] = sum_j W[j][i] sC[k][j]
+    for (int e = tid; e < kIvTile; e += 256) {
+        const int k = e % kIvNb, j = e / kIvNb;
+        const int64_t gk = (r + 1) * kIvNb + k, gj = r * kIvNb + j;
+        sC[k][j] = (r + 1 < R && gk < n) ? L[gk + gj * ld] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 16; ++u) acc[u] = 0.f;
+    for (int j = 0; j < kIvNb; ++j) {
+        const float wv = sW[j][i];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) acc[u] = fmaf(wv, sC[kq + 4 * u][j], acc[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) G[r * kIvTile + i + (kq + 4 * u) * kIvNb] = acc[u];
+}
+
+__device__ __forceinline__ unsigned long long iv_ld_word(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
 
-// trans = 0: L Y = B (blocks ascending); trans = 1: L^T X = B (descending).
-__global__ void __launch_bounds__(256) trsm_inv_kernel(const float *__restrict__ L, int64_t ld,
-                                                       const float *__restrict__ W, int64_t n,
-                                                       float *B, int64_t ldb, int64_t m, int trans,
-                                                       int nchunks, int *ws, int *err_word) {
-    __shared__ float sL[kIvNb][kIvNb + 1];  // sL[k][i]: coefficient of x_k in row i
-    __shared__ float sX[kIvNb][kIvCols];     // solved block / right-hand side
+__device__ __forceinline__ void iv_st_word(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ void iv_cp16(void *dst, const void *src, int bytes) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void iv_cp4(void *dst, const void *src, int bytes) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void iv_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void iv_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Bounded re-read of one hand-off word until it carries this launch's tag.
+__device__ __forceinline__ unsigned long long iv_settle_word(unsigned long long w, const unsigned long long *p,
+                                                             unsigned long long tag, int *err_word,
+                                                             int *abort_flag) {
+    long long spins = 0;
+    while ((w & 0xffffffff00000000ull) != tag) {
+        if (((++spins) & 63) == 0) {
+            if (*(volatile int *)err_word != 0 || spins > kSpinLimit) {
+                atomicCAS(err_word, 0, (int)LLA_ERR_TIMEOUT);
+                *abort_flag = 1;
+                break;
+            }
+            __nanosleep(32);
+        }
+        w = iv_ld_word(p);
+    }
+    return w;
+}
+
+constexpr int kIvCols = 16;   // right-hand-side columns per CTA
+constexpr int kIvLd = 68;     // shared row stride of a staged 64 x 64 tile (floats; 16-byte rows)
+constexpr int kIvStages = 3;  // coupling tiles in flight per CTA
+constexpr size_t kIvSmem =
+    sizeof(float) * ((size_t)kIvStages * kIvNb * kIvLd + 2ull * kIvStages * kIvCols * kIvNb + 2ull * kIvNb * kIvCols);
+
+// TRANS = false: L Y = B (blocks ascending); TRANS = true: L^T X = B (descending).
+// 256 threads: for products, thread (ta = tid % 64, tb = tid / 64) owns row ta
+// and columns 4 tb .. 4 tb + 3 of the CTA's 16.  The coupling tiles and the
+// solved words of earlier blocks stream through a kIvStages-deep cp.async ring.
+template <bool TRANS>
+__global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restrict__ L, int64_t ld,
+                                                          const float *__restrict__ Wall, int64_t n,
+                                                          float *B, int64_t ldb, int64_t m, int nchunks,
+                                                          unsigned long long *ll, int64_t ldl, unsigned epoch,
+                                                          int *counter, int *err_word) {
+    constexpr int C = kIvCols, LPT = kIvTile / 256, NS = kIvStages;
+    constexpr int YCH = kIvNb * C / 2 / 256;  // 16-byte (two-word) copies per thread per stage
+    extern __shared__ __align__(16) float iv_smem[];
+    // sT[s][a][b]: staged tile; sY[s][c][k]: raw solved words; sV[buf][k][c]: their values
+    float(*sT)[kIvNb][kIvLd] = reinterpret_cast<float(*)[kIvNb][kIvLd]>(iv_smem);
+    unsigned long long(*sY)[C][kIvNb] =
+        reinterpret_cast<unsigned long long(*)[C][kIvNb]>(iv_smem + NS * kIvNb * kIvLd);
+    float(*sV)[kIvNb][C] = reinterpret_cast<float(*)[kIvNb][C]>(iv_smem + NS * kIvNb * kIvLd + 2 * NS * C * kIvNb);
     __shared__ int s_ticket, s_abort;
     const int tid = threadIdx.x;
-    int *counter = ws, *flags = ws + 1;
     if (tid == 0) {
         s_ticket = atomicAdd(counter, 1);
         s_abort = 0;
@@ -83,113 +193,233 @@ __global__ void __launch_bounds__(256) trsm_inv_kernel(const float *__restrict__
     const int64_t R = (n + kIvNb - 1) / kIvNb;
     const int64_t pb = s_ticket / nchunks;  // position in processing order
     const int cc = s_ticket % nchunks;
-    const int64_t rb = trans ? R - 1 - pb : pb;
-    const int row = tid % kIvNb, cg = tid / kIvNb;  // 64 rows x 4 column groups of 4
-    const int64_t grow = rb * kIvNb + row;
+    const int64_t rb = TRANS ? R - 1 - pb : pb;
+    const int ta = tid % kIvNb, tb = tid / kIvNb;
+    const int64_t grow = rb * kIvNb + ta;
+    const int64_t col0 = (int64_t)cc * C;
+    const unsigned long long tag = (unsigned long long)epoch << 32;
+    const bool al16 = (ld % 4 == 0) && ((reinterpret_cast<uintptr_t>(L) & 15) == 0);
+
     float acc[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-        const int64_t col = (int64_t)cc * kIvCols + cg * 4 + u;
+        const int64_t col = col0 + tb * 4 + u;
         acc[u] = (grow < n && col < m) ? B[grow + col * ldb] : 0.f;
     }
-    for (int64_t pq = 0; pq < pb; ++pq) {
-        const int64_t qb = trans ? R - 1 - pq : pq;
-        if (tid == 0) {
-            const int *f = flags + pq * nchunks + cc;
-            long long spins = 0;
-            while (iv_ld_acquire(f) == 0) {
-                if (*(volatile int *)err_word != 0 || ++spins > kSpinLimit) {
-                    atomicCAS(err_word, 0, (int)LLA_ERR_TIMEOUT);
-                    s_abort = 1;
-                    break;
+    // this block's inverse and coupling matrix (element (ta, tb + 4u) of each), needed only at the end
+    float preW[LPT], preM[LPT];
+    {
+        const float *Wr = Wall + rb * kIvTile + ta + tb * kIvNb;
+        const float *Mr = Wall + ((TRANS ? 2 : 1) * R + rb) * kIvTile + ta + tb * kIvNb;
+#pragma unroll
+        for (int u = 0; u < LPT; ++u) {
+            preW[u] = Wr[u * 4 * kIvNb];
+            preM[u] = Mr[u * 4 * kIvNb];
+        }
+    }
+    const int64_t nbulk = pb > 0 ? pb - 1 : 0;  // coupling terms before the neighbour's
+
+    // Stage s <- coupling tile and solved words of processing position pq.
+    // Tile: 64 columns a of 64 contiguous rows b (non-trans: a = k, b = i;
+    // trans: a = i, b = k), zero-filled past n.
+    auto issue = [&](int64_t pq, int s) {
+        if (pq < nbulk) {
+            const int64_t qb = TRANS ? R - 1 - pq : pq;
+            const int64_t rowbase = (TRANS ? qb : rb) * kIvNb, colbase = (TRANS ? rb : qb) * kIvNb;
+            if (al16) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int e = tid + 256 * j, a = e >> 4, c4 = e & 15;
+                    const int64_t row = rowbase + 4 * c4, col = colbase + a;
+                    const bool ok = row < n && col < n;
+                    const int bytes = ok ? 4 * (int)(n - row < 4 ? n - row : 4) : 0;
+                    iv_cp16(&sT[s][a][4 * c4], ok ? L + row + col * ld : L, bytes);
                 }
-                __nanosleep(64);
+            } else {
+#pragma unroll 4
+                for (int j = 0; j < 16; ++j) {
+                    const int e = tid + 256 * j, a = e >> 6, b = e & 63;
+                    const int64_t row = rowbase + b, col = colbase + a;
+                    const bool ok = row < n && col < n;
+                    iv_cp4(&sT[s][a][b], ok ? L + row + col * ld : L, ok ? 4 : 0);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < YCH; ++j) {
+                const int e = tid + 256 * j, c = e >> 5, kp = e & 31;
+                const int64_t gk = qb * kIvNb + 2 * kp, col = col0 + c;
+                const bool ok = col < m;
+                iv_cp16(&sY[s][c][2 * kp], ok ? ll + gk + col * ldl : ll, ok ? 16 : 0);
             }
         }
+        iv_commit();
+    };
+    // Values of the words this thread copied into stage s; unpublished ones
+    // are re-read from global memory until they carry this launch's tag.
+    auto settle_stage = [&](int64_t pq, int s, int buf) {
+        const int64_t qb = TRANS ? R - 1 - pq : pq;
+#pragma unroll
+        for (int j = 0; j < YCH; ++j) {
+            const int e = tid + 256 * j, c = e >> 5, kp = e & 31;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int k = 2 * kp + h;
+                const int64_t gk = qb * kIvNb + k, col = col0 + c;
+                float v = 0.f;
+                if (gk < n && col < m) {
+                    const unsigned long long w =
+                        iv_settle_word(sY[s][c][k], ll + gk + col * ldl, tag, err_word, &s_abort);
+                    v = __uint_as_float((unsigned)(w & 0xffffffffull));
+                }
+                sV[buf][k][c] = v;
+            }
+        }
+    };
+
+    // 1. every coupling term but the neighbour's (blocks solved well before this one)
+#pragma unroll
+    for (int s = 0; s < NS - 1; ++s) issue(s, s);
+    for (int64_t pq = 0; pq < nbulk; ++pq) {
+        const int s = (int)(pq % NS), buf = (int)(pq & 1);
+        iv_wait<NS - 2>();
+        settle_stage(pq, s, buf);
         __syncthreads();
         if (s_abort) break;
-        // coupling tile: forward L[rb rows][qb cols], backward L[qb rows][rb cols]^T
-        for (int e = tid; e < kIvNb * kIvNb; e += 256) {
-            const int a = e % kIvNb, b = e / kIvNb;  // consecutive e -> consecutive memory
-            float v;
-            if (!trans) {  // i = a (row of block rb), k = b (row of block qb)
-                const int64_t gi = rb * kIvNb + a, gk = qb * kIvNb + b;
-                v = (gi < n && gk < n) ? L[gi + gk * ld] : 0.f;
-                sL[b][a] = v;
-            } else {  // element L[qb*64 + a][rb*64 + b]: k = a, i = b
-                const int64_t gk = qb * kIvNb + a, gi = rb * kIvNb + b;
-                v = (gi < n && gk < n) ? L[gk + gi * ld] : 0.f;
-                sL[a][b] = v;
+        issue(pq + NS - 1, (int)((pq + NS - 1) % NS));
+        if (!TRANS) {
+#pragma unroll 8
+            for (int k = 0; k < kIvNb; ++k) {
+                const float l = sT[s][k][ta];
+                const float4 x = *reinterpret_cast<const float4 *>(&sV[buf][k][tb * 4]);
+                acc[0] = fmaf(-l, x.x, acc[0]);
+                acc[1] = fmaf(-l, x.y, acc[1]);
+                acc[2] = fmaf(-l, x.z, acc[2]);
+                acc[3] = fmaf(-l, x.w, acc[3]);
+            }
+        } else {
+#pragma unroll 2
+            for (int k4 = 0; k4 < kIvNb / 4; ++k4) {
+                const float4 l4 = *reinterpret_cast<const float4 *>(&sT[s][ta][4 * k4]);
+                const float lv[4] = {l4.x, l4.y, l4.z, l4.w};
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) {
+                    const float4 x = *reinterpret_cast<const float4 *>(&sV[buf][4 * k4 + kk][tb * 4]);
+                    acc[0] = fmaf(-lv[kk], x.x, acc[0]);
+                    acc[1] = fmaf(-lv[kk], x.y, acc[1]);
+                    acc[2] = fmaf(-lv[kk], x.z, acc[2]);
+                    acc[3] = fmaf(-lv[kk], x.w, acc[3]);
+                }
             }
         }
-        for (int e = tid; e < kIvNb * kIvCols; e += 256) {
-            const int k = e % kIvNb, c = e / kIvNb;
-            const int64_t gk = qb * kIvNb + k, col = (int64_t)cc * kIvCols + c;
-            sX[k][c] = (gk < n && col < m) ? __ldcg(&B[gk + col * ldb]) : 0.f;
-        }
-        __syncthreads();
-#pragma unroll 8
-        for (int k = 0; k < kIvNb; ++k) {
-            const float l = sL[k][row];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) acc[u] = fmaf(-l, sX[k][cg * 4 + u], acc[u]);
-        }
-        __syncthreads();
     }
-    if (!s_abort) {
-        // X_rb = W (or W^T) times acc
-#pragma unroll
-        for (int u = 0; u < 4; ++u) sX[row][cg * 4 + u] = acc[u];
-        const float *Wr = W + rb * kIvNb * kIvNb;
-        for (int e = tid; e < kIvNb * kIvNb; e += 256) {
-            const int a = e % kIvNb, b = e / kIvNb;  // W column-major: Wr[a + 64 b] = W[a][b]
-            if (!trans)
-                sL[b][a] = Wr[a + b * kIvNb];  // coefficient of acc_b in row a
-            else
-                sL[a][b] = Wr[a + b * kIvNb];  // W^T[b][a] = W[a][b]: coefficient of acc_a in row b
-        }
-        __syncthreads();
-        float y[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 8
-        for (int k = 0; k < kIvNb; ++k) {
-            const float wv = sL[k][row];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) y[u] = fmaf(wv, sX[k][cg * 4 + u], y[u]);
-        }
+    iv_wait<0>();
+    __syncthreads();
+    if (s_abort) return;
+
+    // 2. t = W_r acc (W_r^T acc when trans); the neighbour's words are read meanwhile
+    unsigned long long wy[4];
+    const int64_t qn = TRANS ? rb + 1 : rb - 1;  // neighbour block
+    if (pb > 0) {
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const int64_t col = (int64_t)cc * kIvCols + cg * 4 + u;
-            if (grow < n && col < m) B[grow + col * ldb] = y[u];
+            const int64_t gk = qn * kIvNb + ta, col = col0 + tb + 4 * u;
+            wy[u] = (gk < n && col < m) ? iv_ld_word(ll + gk + col * ldl) : tag;
         }
     }
-    __threadfence();
+    float(*sK)[kIvLd] = sT[0];  // coefficient tile: sK[k][i]
+    float(*sX)[C] = sV[0];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) sX[ta][tb * 4 + u] = acc[u];
+#pragma unroll
+    for (int u = 0; u < LPT; ++u) {  // preW[u] = W[ta][tb + 4u]
+        if (!TRANS)
+            sK[tb + 4 * u][ta] = preW[u];  // W[i][k]
+        else
+            sK[ta][tb + 4 * u] = preW[u];  // W[k][i]
+    }
     __syncthreads();
-    if (tid == 0) asm volatile("st.release.gpu.b32 [%0], %1;" ::"l"(flags + pb * nchunks + cc), "r"(1) : "memory");
+    float t[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 8
+    for (int k = 0; k < kIvNb; ++k) {
+        const float l = sK[k][ta];
+        const float4 x = *reinterpret_cast<const float4 *>(&sX[k][tb * 4]);
+        t[0] = fmaf(l, x.x, t[0]);
+        t[1] = fmaf(l, x.y, t[1]);
+        t[2] = fmaf(l, x.z, t[2]);
+        t[3] = fmaf(l, x.w, t[3]);
+    }
+    // 3. t -= M_r x_neighbour, M_r (F_r or G_r) stored as the plain coefficient matrix
+    if (pb > 0) {
+        float(*sM)[kIvLd] = sT[1];
+        float(*sN)[C] = sV[1];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t gk = qn * kIvNb + ta, col = col0 + tb + 4 * u;
+            float v = 0.f;
+            if (gk < n && col < m)
+                v = __uint_as_float(
+                    (unsigned)(iv_settle_word(wy[u], ll + gk + col * ldl, tag, err_word, &s_abort) & 0xffffffffull));
+            sN[ta][tb + 4 * u] = v;
+        }
+#pragma unroll
+        for (int u = 0; u < LPT; ++u) sM[tb + 4 * u][ta] = preM[u];  // M[i = ta][k = tb + 4u]
+        __syncthreads();
+        if (s_abort) return;
+#pragma unroll 8
+        for (int k = 0; k < kIvNb; ++k) {
+            const float l = sM[k][ta];
+            const float4 x = *reinterpret_cast<const float4 *>(&sN[k][tb * 4]);
+            t[0] = fmaf(-l, x.x, t[0]);
+            t[1] = fmaf(-l, x.y, t[1]);
+            t[2] = fmaf(-l, x.z, t[2]);
+            t[3] = fmaf(-l, x.w, t[3]);
+        }
+    }
+    // 4. publish
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int64_t col = col0 + tb * 4 + u;
+        if (grow < n && col < m) {
+            B[grow + col * ldb] = t[u];
+            iv_st_word(ll + grow + col * ldl, tag | (unsigned long long)__float_as_uint(t[u]));
+        }
+    }
 }
 
-size_t trsm_inv_ws_ints(int64_t n, int64_t m) {
-    return (size_t)(1 + ((n + kIvNb - 1) / kIvNb) * ((m + kIvCols - 1) / kIvCols));
-}
+size_t trsm_inv_ws_ints(int64_t, int64_t) { return 1; }
 
-size_t diag_inverse_floats(int64_t n) { return (size_t)((n + kIvNb - 1) / kIvNb) * kIvNb * kIvNb; }
+size_t trsm_inv_stage_words(int64_t n, int64_t m) { return (size_t)((n + kIvNb - 1) / kIvNb) * kIvNb * (size_t)m; }
+
+size_t diag_inverse_floats(int64_t n) { return 3 * (size_t)((n + kIvNb - 1) / kIvNb) * kIvTile; }
 
 int diag_inverse_launch(const float *L, int64_t ld, int64_t n, float *W, cudaStream_t st) {
     if (n == 0) return 0;
-    LaunchScope ls(K_MIXED_TRSM, st, (double)n * kIvNb * kIvNb / 3.0);
-    diag_inverse_kernel<<<(unsigned)((n + kIvNb - 1) / kIvNb), 64, 0, st>>>(L, ld, n, W);
+    const int64_t R = (n + kIvNb - 1) / kIvNb;
+    {
+        LaunchScope ls(K_MIXED_TRSM, st, (double)n * kIvTile / 3.0);
+        diag_inverse_kernel<<<(unsigned)R, 64, 0, st>>>(L, ld, n, W);
+        if (cudaGetLastError() != cudaSuccess) return -1;
+    }
+    LaunchScope ls(K_MIXED_TRSM, st, 4.0 * (double)R * kIvTile * kIvNb);
+    fuse_kernel<<<(unsigned)R, 256, 0, st>>>(L, ld, n, W, W + R * kIvTile, W + 2 * R * kIvTile);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 int trsm_inv_launch(const float *L, int64_t ld, const float *W, int64_t n, float *B, int64_t ldb,
-                    int64_t m, int trans, int *ws, int *err_word, cudaStream_t st) {
+                    int64_t m, int trans, unsigned long long *stage, unsigned epoch, int *ws, int *err_word,
+                    cudaStream_t st) {
     if (n == 0 || m == 0) return 0;
+    if (epoch == 0) return -1;
     const int nchunks = (int)((m + kIvCols - 1) / kIvCols);
     const int64_t R = (n + kIvNb - 1) / kIvNb;
-    if (cudaMemsetAsync(ws, 0, sizeof(int) * (1 + R * nchunks), st) != cudaSuccess) return -1;
+    auto kern = trans ? trsm_inv_kernel<true> : trsm_inv_kernel<false>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kIvSmem) != cudaSuccess)
+        return -1;
+    if (cudaMemsetAsync(ws, 0, sizeof(int), st) != cudaSuccess) return -1;
     // algorithmic work: n^2 m flops
     LaunchScope ls(K_MIXED_TRSM, st, (double)n * n * m);
-    trsm_inv_kernel<<<(unsigned)(R * nchunks), 256, 0, st>>>(L, ld, W, n, B, ldb, m, trans, nchunks, ws,
-                                                             err_word);
+    kern<<<(unsigned)(R * nchunks), 256, kIvSmem, st>>>(L, ld, W, n, B, ldb, m, nchunks, stage, R * kIvNb, epoch,
+                                                       ws, err_word);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -53,6 +53,20 @@ def test_refined_reaches_fp64_accuracy(gpu_lla, update, n, kappa):
     assert fe <= 10 * kappa * max(rep["backward_error"], 1e-15), fe  # forward <~ kappa * backward
 
 
+@pytest.mark.parametrize("m", [1, 20, 64, 97])
+def test_refined_many_right_hand_sides(gpu_lla, m):
+    """Column chunks of 16, 32 and 64 in the FP32 substitutions, ragged n."""
+    lla = gpu_lla
+    rng = np.random.default_rng(m)
+    n = 777
+    a = qdq(rng, n, 1e5)
+    b = rng.standard_normal((n, m))
+    x = b.copy()
+    rep = lla.posv_refined(a, x, update="bf16x6")
+    assert rep["converged"] == 1 and rep["fell_back"] == 0, rep
+    assert backward_error(a, x, b) <= 2e-13
+
+
 def test_equilibration_handles_badly_scaled_diagonal(gpu_lla):
     lla = gpu_lla
     rng = np.random.default_rng(3)
