@@ -211,7 +211,7 @@ def main():
     ap.add_argument("--update", default="bf16x6",
                     help="trailing-update form of the mixed path: fp32|bf16|bf16x3|bf16x6|fp16|fp16x3")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed steps of the plain FP64 leg")
-    ap.add_argument("--residual", default="fp64", choices=["fp64", "slices"],
+    ap.add_argument("--residual", default="slices", choices=["fp64", "slices"],
                     help="refinement residual of the headline: FP64 MMA pipe, or exact BF16 slices")
     ap.add_argument("--no-alt", action="store_true", help="skip timing the other residual method")
     ap.add_argument("--workload", default="single", choices=["single", "batch", "serve", "sweep"],

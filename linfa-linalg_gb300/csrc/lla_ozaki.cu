@@ -12,12 +12,17 @@
 // 2^-56 of 2^(e_i+f_j) per product).  Every product alpha*xi is an integer of
 // at most 14 bits; the tensor core sums them in FP32, which is exact as long
 // as a partial sum stays below 2^24: the kernel drains the tensor-memory
-// accumulator every G_d = 16 / (d+1) K-chunks of 64 (at most 16 x 64 terms of
-// 2^14), converts the drained integer exactly and accumulates it in a 64-bit
-// integer per level d; the levels are combined in FP64 at the end.  So the only
-// rounding errors are those of the final FP64 combination and subtraction,
-// like an FP64 GEMM's epilogue -- the residual is as accurate as an FP64 one,
-// computed on the BF16 pipe.
+// accumulators every two K-chunks of 64 (level d gathers at most
+// 2 (d+1) x 64 <= 1024 terms of 2^14) and converts the drained integers exactly.  Levels 0-3 are summed at
+// their relative weights 2^(21-7d) in one 64-bit integer and levels 4-7 at
+// 2^(49-7d) in another (both stay far below 2^63); the two are combined in
+// FP64 at the end.  So the only rounding errors are those of the final FP64
+// combination and subtraction, like an FP64 GEMM's epilogue -- the residual is
+// as accurate as an FP64 one, computed on the BF16 pipe.
+//
+// Loop order: K-chunks outermost, then the slices of A, then those of X: each
+// A slice tile is loaded once per chunk and meets every X slice it pairs
+// with, the eight levels accumulating side by side in tensor memory.
 //
 // Slices of A are built once per solve (A does not change during the
 // refinement); slices of X once per iteration.
@@ -36,14 +41,18 @@ namespace lla {
 
 constexpr int kOzS = 8;                      // slices
 constexpr int kOzM = 128, kOzN = 64, kOzK = 64;
-constexpr int kOzStages = 4;
-constexpr int kOzATile = kOzM * kOzK * 2;    // 16 KiB
-constexpr int kOzBTile = kOzN * kOzK * 2;    // 8 KiB
-constexpr int kOzSmem = 1024 + kOzStages * (kOzATile + kOzBTile) + 256;
+constexpr int kOzAStages = 4;
+constexpr int kOzATile = kOzM * kOzK * 2;    // 16 KiB: one slice of a 128 x 64 A tile
+constexpr int kOzXTile = kOzN * kOzK * 2;    // 8 KiB: one slice of a 64 x 64 X tile
+constexpr int kOzXSet = kOzS * kOzXTile;     // 64 KiB: all slices of one X tile
+constexpr int kOzSmem = 1024 + kOzAStages * kOzATile + 2 * kOzXSet + 256;
 constexpr int kOzThreads = 320;              // 8 epilogue warps + producer + MMA
-constexpr uint32_t kOzCols = 2 * kOzN;       // two FP32 accumulators of 64 columns
+constexpr uint32_t kOzCols = kOzS * kOzN;    // one FP32 accumulator of 64 columns per level: 512
+constexpr int kOzSplitsMax = 8;
 
-__device__ __forceinline__ int oz_group(int d) { return max(1, 16 / (d + 1)); }
+// K-chunks per accumulation window: level 7 gathers 8 pairs x 64 products
+// below 2^14 per chunk, so two chunks stay within 2^24 (exact in FP32).
+constexpr int kOzWin = 2;
 
 // ---- slicing ---------------------------------------------------------------
 
@@ -183,34 +192,44 @@ __global__ void oz_slice_x_kernel(const double *__restrict__ X, int64_t ldx, int
 
 // ---- the tensor-core kernel ------------------------------------------------
 
-// Stage schedule shared by the three roles: level d, groups of G_d K-chunks,
-// pairs (p, d - p).
+// Schedule shared by the three roles.  K-chunks kc of 64 columns; per chunk the
+// X slices (all eight, one 64 KiB TMA box) and then the A slices p = 0..7 (a
+// 4-deep ring).  Slice p of A meets slices q = 0..7-p of X, and the product
+// accumulates at level d = p + q in its own 64 TMEM columns (8 levels = all
+// 512).  Slice p of A meets up to four X slices in one MMA (N <= 256): the X
+// slices are consecutive 64-row blocks of the operand and the levels they
+// feed consecutive accumulators.  Every window of kOzWin chunks the epilogue
+// drains levels 0-3, then 4-7; the MMA issuer restarts each half as soon as it
+// is read out.
 __global__ void __launch_bounds__(kOzThreads, 1) oz_residual_kernel(
     const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmX, int64_t n,
     int64_t m, int kchunks, int splits, double *F, int *err_word) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ int s_abort;
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint8_t *sA = smem;
-    uint8_t *sB = smem + kOzStages * kOzATile;
-    uint64_t *bars = (uint64_t *)(sB + kOzStages * kOzBTile);
-    uint32_t *tslot = (uint32_t *)(bars + 2 * kOzStages + 4);
+    uint8_t *sA = smem;                              // kOzAStages x 16 KiB
+    uint8_t *sX = smem + kOzAStages * kOzATile;      // 2 x 64 KiB
+    uint64_t *bars = (uint64_t *)(sX + 2 * kOzXSet);
+    uint32_t *tslot = (uint32_t *)(bars + 2 * kOzAStages + 7);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kOzStages);
-    const uint32_t tfull0 = smem_u32(bars + 2 * kOzStages), tempty0 = tfull0 + 16;
+    const uint32_t fullA0 = smem_u32(bars), emptyA0 = fullA0 + 8 * kOzAStages;
+    const uint32_t fullX0 = emptyA0 + 8 * kOzAStages, emptyX0 = fullX0 + 16;
+    const uint32_t tfull = emptyX0 + 16, tempty0 = tfull + 8;  // tempty0 + 8 h: levels 4h .. 4h+3 drained
     const int row0 = (int)blockIdx.x * kOzM;
     const int z = blockIdx.y;
     const int cps = (kchunks + splits - 1) / splits;
     const int kc_beg = z * cps, kc_end = min(kchunks, kc_beg + cps);
     if (tid == 0) {
-        for (int s = 0; s < kOzStages; ++s) {
-            mbar_init(full0 + 8 * s, 1);
-            mbar_init(empty0 + 8 * s, 1);
+        for (int s = 0; s < kOzAStages; ++s) {
+            mbar_init(fullA0 + 8 * s, 1);
+            mbar_init(emptyA0 + 8 * s, 1);
         }
-        for (int a = 0; a < 2; ++a) {
-            mbar_init(tfull0 + 8 * a, 1);
-            mbar_init(tempty0 + 8 * a, 256);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(fullX0 + 8 * b, 1);
+            mbar_init(emptyX0 + 8 * b, 1);
         }
+        mbar_init(tfull, 1);
+        for (int h = 0; h < 2; ++h) mbar_init(tempty0 + 8 * h, 256);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
     }
@@ -225,107 +244,121 @@ __global__ void __launch_bounds__(kOzThreads, 1) oz_residual_kernel(
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
-    // instruction descriptor: D F32, A/B BF16, K-major, N = 64, M = 128
-    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kOzN >> 3) << 17) |
-                           ((uint32_t)(kOzM >> 4) << 24);
+    // instruction descriptor without N: D F32, A/B BF16, K-major, M = 128
+    const uint32_t idesc0 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kOzM >> 4) << 24);
 
     if (warp == 8) {
         if (lane == 0) {  // TMA producer
-            int64_t g = 0;
-            for (int d = 0; d < kOzS && !*(volatile int *)&s_abort; ++d) {
-                const int plo = max(0, d - (kOzS - 1)), phi = min(d, kOzS - 1);
-                for (int kc = kc_beg; kc < kc_end; ++kc) {
-                    for (int p = plo; p <= phi; ++p, ++g) {
-                        const int s = (int)(g % kOzStages);
-                        const int64_t round = g / kOzStages;
-                        if (round > 0 &&
-                            !mbar_wait(empty0 + 8 * s, (uint32_t)((round - 1) & 1), err_word)) {
-                            s_abort = 1;
-                            break;
-                        }
-                        mbar_expect_tx(full0 + 8 * s, kOzATile + kOzBTile);
-                        tma_load_3d(smem_u32(sA + s * kOzATile), &tmA, kc * kOzK, row0, p, full0 + 8 * s);
-                        tma_load_3d(smem_u32(sB + s * kOzBTile), &tmX, kc * kOzK, 0, d - p, full0 + 8 * s);
+            int64_t ga = 0;
+            for (int kc = kc_beg, j = 0; kc < kc_end && !*(volatile int *)&s_abort; ++kc, ++j) {
+                const int xb = j & 1, use = j >> 1;
+                if (use > 0 && !mbar_wait(emptyX0 + 8 * xb, (uint32_t)((use - 1) & 1), err_word)) {
+                    s_abort = 1;
+                    break;
+                }
+                mbar_expect_tx(fullX0 + 8 * xb, kOzXSet);
+                tma_load_3d(smem_u32(sX + xb * kOzXSet), &tmX, kc * kOzK, 0, 0, fullX0 + 8 * xb);
+                for (int p = 0; p < kOzS; ++p, ++ga) {
+                    const int s = (int)(ga % kOzAStages);
+                    const int64_t round = ga / kOzAStages;
+                    if (round > 0 && !mbar_wait(emptyA0 + 8 * s, (uint32_t)((round - 1) & 1), err_word)) {
+                        s_abort = 1;
+                        break;
                     }
-                    if (*(volatile int *)&s_abort) break;
+                    mbar_expect_tx(fullA0 + 8 * s, kOzATile);
+                    tma_load_3d(smem_u32(sA + s * kOzATile), &tmA, kc * kOzK, row0, p, fullA0 + 8 * s);
                 }
             }
         }
     } else if (warp == 9) {
         if (lane == 0) {  // MMA issuer
-            int64_t g = 0, grp = 0;
-            for (int d = 0; d < kOzS && !*(volatile int *)&s_abort; ++d) {
-                const int plo = max(0, d - (kOzS - 1)), phi = min(d, kOzS - 1);
-                const int G = oz_group(d);
-                for (int kg = kc_beg; kg < kc_end; kg += G, ++grp) {
-                    const int a = (int)(grp & 1);
-                    const int64_t use = grp >> 1;
-                    if (use > 0 && !mbar_wait(tempty0 + 8 * a, (uint32_t)((use - 1) & 1), err_word)) {
+            int64_t ga = 0;
+            int win = 0;
+            for (int kc = kc_beg, j = 0; kc < kc_end && !*(volatile int *)&s_abort; ++kc, ++j) {
+                const int xb = j & 1, use = j >> 1;
+                const bool wstart = (j % kOzWin) == 0;
+                if (!mbar_wait(fullX0 + 8 * xb, (uint32_t)(use & 1), err_word)) {
+                    s_abort = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t x0 = smem_u32(sX + xb * kOzXSet);
+                for (int p = 0; p < kOzS; ++p, ++ga) {
+                    const int s = (int)(ga % kOzAStages);
+                    if (!mbar_wait(fullA0 + 8 * s, (uint32_t)((ga / kOzAStages) & 1), err_word)) {
                         s_abort = 1;
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t dt = tmem + (uint32_t)(a * kOzN);
-                    bool first = true;
-                    for (int kc = kg; kc < min(kc_end, kg + G); ++kc) {
-                        for (int p = plo; p <= phi; ++p, ++g) {
-                            const int s = (int)(g % kOzStages);
-                            if (!mbar_wait(full0 + 8 * s, (uint32_t)((g / kOzStages) & 1), err_word)) {
+                    // A slice p against X slices q0 .. q1-1 in one MMA of N = 64 (q1 - q0):
+                    // the X slices are consecutive 64-row blocks of one operand and
+                    // the levels p+q0 .. p+q1-1 consecutive 64-column accumulators
+                    const uint64_t ad = sw128_desc(smem_u32(sA + s * kOzATile));
+                    for (int h = 0; h < 2; ++h) {
+                        const int q0 = 4 * h, q1 = min(4 * h + 4, kOzS - p);
+                        if (q0 >= q1) break;
+                        // first product of a window into these levels: wait until the
+                        // epilogue has read them out of the previous window
+                        if (wstart && p == 0 && win > 0) {
+                            if (!mbar_wait(tempty0 + 8 * h, (uint32_t)((win - 1) & 1), err_word)) {
                                 s_abort = 1;
                                 break;
                             }
                             tc_fence_after();
-                            const uint32_t a0 = smem_u32(sA + s * kOzATile);
-                            const uint32_t b0 = smem_u32(sB + s * kOzBTile);
-#pragma unroll
-                            for (int k = 0; k < kOzK / 16; ++k) {
-                                tc_mma(dt, sw128_desc(a0 + 32 * k), sw128_desc(b0 + 32 * k), idesc,
-                                       first ? 0u : 1u);
-                                first = false;
-                            }
-                            tc_commit(empty0 + 8 * s);
                         }
-                        if (*(volatile int *)&s_abort) break;
+                        const uint32_t dt = tmem + (uint32_t)((p + q0) * kOzN);
+                        const uint32_t idesc = idesc0 | ((uint32_t)((kOzN * (q1 - q0)) >> 3) << 17);
+                        const uint64_t bd = sw128_desc(x0 + (uint32_t)(q0 * kOzXTile));
+#pragma unroll
+                        for (int k = 0; k < kOzK / 16; ++k)  // +32 bytes along K per step
+                            tc_mma(dt, ad + 2 * k, bd + 2 * k, idesc, (wstart && p == 0 && k == 0) ? 0u : 1u);
                     }
                     if (*(volatile int *)&s_abort) break;
-                    tc_commit(tfull0 + 8 * a);
+                    tc_commit(emptyA0 + 8 * s);
+                }
+                if (*(volatile int *)&s_abort) break;
+                tc_commit(emptyX0 + 8 * xb);
+                if ((j % kOzWin) == kOzWin - 1 || kc == kc_end - 1) {
+                    tc_commit(tfull);
+                    ++win;
                 }
             }
         }
-    } else {  // epilogue: warp w drains lane quarter w % 4, columns 32 (w / 4) ..
+    } else {  // epilogue: warp w drains lane quarter w % 4, columns 32 (w / 4) .. of every level
         const int qw = warp & 3, half = warp >> 2;
         const int r = qw * 32 + lane;
-        long long I[32];
-        double acc[32];
+        // exact integer sums: hi = sum_{d<4} I_d 2^(21-7d), lo = sum_{d>=4} I_d 2^(49-7d)
+        long long hi[32], lo[32];
 #pragma unroll
-        for (int c = 0; c < 32; ++c) acc[c] = 0.0;
-        int64_t grp = 0;
+        for (int c = 0; c < 32; ++c) hi[c] = lo[c] = 0;
         bool ok = true;
-        for (int d = 0; d < kOzS && ok; ++d) {
-            const int G = oz_group(d);
-#pragma unroll
-            for (int c = 0; c < 32; ++c) I[c] = 0;
-            for (int kg = kc_beg; kg < kc_end; kg += G, ++grp) {
-                const int a = (int)(grp & 1);
-                const int64_t use = grp >> 1;
-                bool w = mbar_wait(tfull0 + 8 * a, (uint32_t)(use & 1), err_word);
-                w = __all_sync(0xffffffffu, w) && !*(volatile int *)&s_abort;
-                if (!w) {
-                    if (lane == 0) s_abort = 1;
-                    ok = false;
-                    break;
-                }
-                tc_fence_after();
-                uint32_t v[32];
-                tc_ld32(tmem + (uint32_t)(a * kOzN) + ((uint32_t)(qw * 32) << 16) + (uint32_t)(half * 32), v);
-#pragma unroll
-                for (int c = 0; c < 32; ++c) I[c] += (long long)__float2int_rn(__uint_as_float(v[c]));
-                tc_fence_before();
-                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tempty0 + 8 * a) : "memory");
+        const int nwin = (kc_end - kc_beg + kOzWin - 1) / kOzWin;
+        for (int win = 0; win < nwin && ok; ++win) {
+            bool w = mbar_wait(tfull, (uint32_t)(win & 1), err_word);
+            w = __all_sync(0xffffffffu, w) && !*(volatile int *)&s_abort;
+            if (!w) {
+                if (lane == 0) s_abort = 1;
+                ok = false;
+                break;
             }
-            const double w = ldexp(1.0, -7 * (d + 2));
+            tc_fence_after();
+#pragma unroll 1
+            for (int d = 0; d < kOzS; ++d) {
+                uint32_t v[32];
+                tc_ld32(tmem + (uint32_t)(d * kOzN) + ((uint32_t)(qw * 32) << 16) + (uint32_t)(half * 32), v);
+                if ((d & 3) == 3) {  // levels d-3 .. d read out
+                    tc_fence_before();
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tempty0 + 8 * (d >> 2)) : "memory");
+                }
+                const long long wd = 1ll << (d < 4 ? 21 - 7 * d : 49 - 7 * d);
+                if (d < 4) {
 #pragma unroll
-            for (int c = 0; c < 32; ++c) acc[c] = fma((double)I[c], w, acc[c]);
+                    for (int c = 0; c < 32; ++c) hi[c] += (long long)__float2int_rn(__uint_as_float(v[c])) * wd;
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) lo[c] += (long long)__float2int_rn(__uint_as_float(v[c])) * wd;
+                }
+            }
         }
         const int64_t i = row0 + r;
         if (ok && i < n) {
@@ -333,7 +366,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) oz_residual_kernel(
 #pragma unroll
             for (int c = 0; c < 32; ++c) {
                 const int64_t j = half * 32 + c;
-                if (j < m) Fz[i + j * n] = acc[c];
+                if (j < m) Fz[i + j * n] = ldexp((double)hi[c], -35) + ldexp((double)lo[c], -63);
             }
         }
     }
@@ -381,7 +414,7 @@ size_t oz_workspace_bytes(int64_t n, int64_t m) {
     return (size_t)kOzS * n * ldp * 2        // A slices
            + (size_t)kOzS * kOzN * ldp * 2   // X slices (one 64-column group)
            + (size_t)n * 8                   // row maxima
-           + (size_t)4 * n * std::min<int64_t>(m, kOzN) * 8 + 4096;  // split partials
+           + (size_t)kOzSplitsMax * n * std::min<int64_t>(m, kOzN) * 8 + 4096;  // split partials
 }
 
 struct OzState {
@@ -400,10 +433,21 @@ static int oz_splits(int64_t n) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 1;
     }
-    const int64_t tiles = (n + kOzM - 1) / kOzM;
-    int s = 1;
-    while (s < 4 && tiles * s < (int64_t)sms && (oz_ldp(n) / kOzK) / (s + 1) >= 8) ++s;
-    return s;
+    // fewest splits whose CTAs fill the waves of one CTA per SM to within 5 %,
+    // keeping at least 8 K-chunks per split
+    const int64_t tiles = (n + kOzM - 1) / kOzM, chunks = oz_ldp(n) / kOzK;
+    int best = 1;
+    double best_eff = 0.0;
+    for (int s = 1; s <= kOzSplitsMax; ++s) {
+        if (s > 1 && chunks / s < 8) break;
+        const int64_t ctas = tiles * s, waves = (ctas + sms - 1) / sms;
+        const double eff = (double)ctas / (double)(waves * sms);
+        if (eff > best_eff + 0.05) {
+            best = s;
+            best_eff = eff;
+        }
+    }
+    return best;
 }
 
 static void oz_carve(void *ws, int64_t n, int64_t m, OzState &o) {
@@ -464,7 +508,7 @@ int oz_residual_launch(const double *X, int64_t ldx, const double *B, int64_t ld
     {
         const cuuint64_t dims[3] = {(cuuint64_t)o.ldp, (cuuint64_t)kOzN, (cuuint64_t)kOzS};
         const cuuint64_t strides[2] = {(cuuint64_t)o.ldp * 2, (cuuint64_t)kOzN * o.ldp * 2};
-        const cuuint32_t box[3] = {(cuuint32_t)kOzK, (cuuint32_t)kOzN, 1};
+        const cuuint32_t box[3] = {(cuuint32_t)kOzK, (cuuint32_t)kOzN, (cuuint32_t)kOzS};  // all slices
         if (enc(&o.tmX, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, o.X, dims, strides, box, estr,
                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
