@@ -38,6 +38,7 @@ struct MixedWs {
     DevBuf F, fdiag;                          // plain FP64 fallback
     DevBuf opA, opB;                          // tensor-core operand planes of one panel
     DevBuf tcerr;                             // tensor-core update status word
+    DevBuf pinv;                              // inverted 32 x 32 diagonal blocks of one panel
     HostBuf words_host;
 };
 

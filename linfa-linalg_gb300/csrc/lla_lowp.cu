@@ -6,7 +6,8 @@
 //            sub-blocks: an unpredicated one-warp shuffle Cholesky, a
 //            row-parallel solve of the rows below it, a shared-memory update
 //            of the rest; a short last block is padded with the identity);
-//   panel  : L21 = A21 L11^-T in FP32, one thread per row, and the operand
+//   panel  : L21 = A21 L11^-T in FP32 by 32-column blocks (products with the
+//            inverted 32 x 32 diagonal blocks of L11), and the operand
 //            planes of L21 for the tensor cores: a one-, two- or three-term
 //            split of every FP32 value into BF16 (or FP16) parts
 //            x ~= h0 + h1 + h2;
@@ -42,8 +43,8 @@ constexpr int kLpPd = kLpNb + 4;  // row stride of the transposed 32-column pane
 // diagonal block: b <= 128, one CTA of 1024 threads, block in shared memory
 
 __global__ void __launch_bounds__(1024) lowp_diag_kernel(float *L, int64_t ld, int64_t p, int b,
-                                                         int64_t *info, double *min_ratio) {
-    extern __shared__ float sa[];  // [128][129]: sa[r * kLpLd + c] = L11[r][c]; then sp[32][kLpPd]
+                                                         int64_t *info, double *min_ratio, float *Wd) {
+    extern __shared__ float sa[];  // [128][129]: sa[r * kLpLd + c] = L11[r][c]; then sp, sw
     float *sp = sa + kLpNb * kLpLd;  // sp[t * kLpPd + r] = L11[r][kb + t] for the rows below
     __shared__ float rdiag[32];      // reciprocals of the current 32 x 32 factor's diagonal
     __shared__ int failed;
@@ -95,22 +96,30 @@ __global__ void __launch_bounds__(1024) lowp_diag_kernel(float *L, int64_t ld, i
         if (failed) break;
         const int rest0 = kb + 32;
         const int w = kLpNb - rest0;
-        // (2) rows below inside the block: row r solves against the 32 x 32 factor
-        if (tid < w) {
-            const int r = rest0 + tid;
+        // (2) rows below inside the block: row r solves against the 32 x 32
+        // factor, x L_JJ^T = a.  32 more threads solve the rows of the identity,
+        // which gives the columns of W_JJ = L_JJ^-1 for the panel kernel.
+        if (tid < w + 32) {
+            const int ie = tid - w;               // identity row, when >= 0
+            const int r = ie < 0 ? rest0 + tid : 0;  // (row 0: any in-bounds address)
             float v[32];
 #pragma unroll
-            for (int c = 0; c < 32; ++c) v[c] = sa[r * kLpLd + kb + c];
+            for (int c = 0; c < 32; ++c) v[c] = (ie < 0) ? sa[r * kLpLd + kb + c] : (c == ie ? 1.f : 0.f);
 #pragma unroll
             for (int c = 0; c < 32; ++c) {
                 v[c] *= rdiag[c];
 #pragma unroll
                 for (int c2 = c + 1; c2 < 32; ++c2) v[c2] = fmaf(-v[c], sa[(kb + c2) * kLpLd + kb + c], v[c2]);
             }
+            if (ie < 0) {
 #pragma unroll
-            for (int c = 0; c < 32; ++c) {
-                sa[r * kLpLd + kb + c] = v[c];
-                sp[c * kLpPd + r] = v[c];
+                for (int c = 0; c < 32; ++c) {
+                    sa[r * kLpLd + kb + c] = v[c];
+                    sp[c * kLpPd + r] = v[c];
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < 32; ++c) Wd[kb * 32 + c * 32 + ie] = v[c];  // W[c][ie], row-major
             }
         }
         __syncthreads();
@@ -168,8 +177,7 @@ __global__ void __launch_bounds__(1024) lowp_diag_kernel(float *L, int64_t ld, i
 }
 
 // ---------------------------------------------------------------------------
-// panel: rows [q, n), q = p + b.  L21 row j = A21 row j * L11^-T (FP32), then
-// the operand planes P_t[r][k] (r = j - q, k < kpad; zero for k >= b).
+// BF16 / FP16 parts of an FP32 value
 
 template <typename H>
 __device__ __forceinline__ H to_half(float x);
@@ -180,70 +188,129 @@ __device__ __forceinline__ __half to_half<__half>(float x) { return __float2half
 __device__ __forceinline__ float from_half(__nv_bfloat16 h) { return __bfloat162float(h); }
 __device__ __forceinline__ float from_half(__half h) { return __half2float(h); }
 
+// ---------------------------------------------------------------------------
+// panel: rows [q, n), q = p + 128.  L21 = A21 L11^-T in FP32 by 32-column
+// blocks J, each a pair of small products (no sequential step):
+//     Y_J = A_J - sum_{I<J} X_I L_JI^T,   X_J = Y_J W_JJ^T,
+// W_JJ = L_JJ^-1 from the diagonal kernel.  Then the operand planes of L21
+// for the tensor cores (zero for k >= b).  One CTA of 256 threads per 64 rows;
+// for products, thread (rt = tid % 32, ct = tid / 32) owns rows rt, rt + 32 and
+// columns 4 ct .. 4 ct + 3 of the current block.
+constexpr int kPnRows = 64;
+constexpr int kPnXd = kPnRows + 4;  // row stride of sXT (k-major copy of the row tile)
+constexpr int kPnLd = kLpNb + 4;    // row stride of sLT (k-major copy of L11)
+constexpr int kPnWd = 32 + 4;       // row stride of sWT (k-major W_JJ)
+constexpr size_t kPnSmem = sizeof(float) * (kLpNb * kPnXd + kLpNb * kPnLd + 4 * 32 * kPnWd);
+
 template <typename H>
-__global__ void __launch_bounds__(128) lowp_panel_kernel(float *L, int64_t ld, int64_t n, int64_t p,
-                                                         int b, H *planes, int64_t plane_stride,
-                                                         int kpad, int terms, const int64_t *info) {
-    // L11 [128][129], 1/diag [128], then one finished row per thread [128][129]
-    extern __shared__ float sm[];
-    float *sl = sm, *rinv = sm + kLpNb * kLpLd, *rows = rinv + kLpNb;
+__global__ void __launch_bounds__(256) lowp_panel_kernel(float *L, int64_t ld, int64_t n, int64_t p,
+                                                         const float *__restrict__ Wd, H *planes,
+                                                         int64_t plane_stride, int kpad, int terms,
+                                                         const int64_t *info) {
+    extern __shared__ __align__(16) float sm[];
+    float *sXT = sm;                         // sXT[k * kPnXd + r] = row r, column k of the tile
+    float *sLT = sXT + kLpNb * kPnXd;        // sLT[k * kPnLd + c] = L11[c][k]
+    float *sWT = sLT + kLpNb * kPnLd;        // sWT[(J * 32 + k) * kPnWd + c] = W_JJ[c][k]
     if (*(volatile const int64_t *)info >= 0) return;
-    for (int e = threadIdx.x; e < kLpNb * kLpNb; e += blockDim.x) {
-        const int r = e % kLpNb, c = e / kLpNb;
-        if (r < b && c <= r) sl[r * kLpLd + c] = L[(p + r) + (p + c) * ld];
+    const int tid = threadIdx.x;
+    const int64_t q = p + kLpNb;
+    const int64_t row0 = q + (int64_t)blockIdx.x * kPnRows;
+    // loads: columns of the row tile and of L11 are contiguous in memory
+    // (constant trip counts, unrolled: many loads in flight per thread)
+    {
+        const int r = tid % kPnRows;
+        const bool ok = row0 + r < n;
+        const float *src = L + (row0 + r) + p * ld;
+#pragma unroll 8
+        for (int k = tid / kPnRows; k < kLpNb; k += 256 / kPnRows) sXT[k * kPnXd + r] = ok ? src[k * ld] : 0.f;
+    }
+    {
+        const int c = tid % kLpNb;
+        const float *src = L + (p + c) + p * ld;
+#pragma unroll 8
+        for (int k = tid / kLpNb; k < kLpNb; k += 256 / kLpNb) sLT[k * kPnLd + c] = (k <= c) ? src[k * ld] : 0.f;
+    }
+#pragma unroll
+    for (int e = tid; e < 4 * 32 * 32; e += 256) {  // Wd[J][c][k] row-major
+        const int k = e % 32, c = (e / 32) % 32, J = e / 1024;
+        sWT[(J * 32 + k) * kPnWd + c] = Wd[e];
     }
     __syncthreads();
-    if (threadIdx.x < b) rinv[threadIdx.x] = 1.0f / sl[threadIdx.x * kLpLd + threadIdx.x];
-    __syncthreads();
-    const int64_t q = p + b;
-    const int64_t j = q + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    float *my = rows + threadIdx.x * kLpLd;  // conflict-free: bank (tid + k) % 32
-    // forward substitution l L11^T = a, 32 columns at a time in registers; the
-    // finished part of the row stays in shared memory
-    for (int kb = 0; kb < b; kb += 32) {
-        float v[32];
+    const int rt = tid % 32, ct = tid / 32;
+#pragma unroll 1
+    for (int J = 0; J < 4; ++J) {
+        const int cj = J * 32 + 4 * ct;  // this thread's first column
+        float acc[2][4];
 #pragma unroll
-        for (int c = 0; c < 32; ++c) v[c] = (kb + c < b) ? L[j + (p + kb + c) * ld] : 0.f;
-        for (int t = 0; t < kb; ++t) {
-            const float lt = my[t];
-#pragma unroll
-            for (int c = 0; c < 32; ++c) v[c] = fmaf(-lt, sl[(kb + c) * kLpLd + t], v[c]);
+        for (int u = 0; u < 4; ++u) {
+            acc[0][u] = sXT[(cj + u) * kPnXd + rt];
+            acc[1][u] = sXT[(cj + u) * kPnXd + rt + 32];
         }
+        // Y_J = A_J - X_{<J} L_J,<J^T
+        for (int k = 0; k < J * 32; ++k) {
+            const float x0 = sXT[k * kPnXd + rt], x1 = sXT[k * kPnXd + rt + 32];
+            const float4 l4 = *reinterpret_cast<const float4 *>(&sLT[k * kPnLd + cj]);
+            const float lv[4] = {l4.x, l4.y, l4.z, l4.w};
 #pragma unroll
-        for (int c = 0; c < 32; ++c) {
-            if (kb + c < b) {
-                v[c] *= rinv[kb + c];
-#pragma unroll
-                for (int c2 = c + 1; c2 < 32; ++c2)
-                    v[c2] = fmaf(-v[c], sl[(kb + c2) * kLpLd + kb + c], v[c2]);
+            for (int u = 0; u < 4; ++u) {
+                acc[0][u] = fmaf(-x0, lv[u], acc[0][u]);
+                acc[1][u] = fmaf(-x1, lv[u], acc[1][u]);
             }
         }
+        __syncthreads();  // every thread has read A_J
 #pragma unroll
-        for (int c = 0; c < 32; ++c) {
-            if (kb + c < b) {
-                my[kb + c] = v[c];
-                L[j + (p + kb + c) * ld] = v[c];
+        for (int u = 0; u < 4; ++u) {
+            sXT[(cj + u) * kPnXd + rt] = acc[0][u];
+            sXT[(cj + u) * kPnXd + rt + 32] = acc[1][u];
+        }
+        __syncthreads();
+        // X_J = Y_J W_JJ^T
+        float x[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+#pragma unroll 8
+        for (int k = 0; k < 32; ++k) {
+            const float y0 = sXT[(J * 32 + k) * kPnXd + rt], y1 = sXT[(J * 32 + k) * kPnXd + rt + 32];
+            const float4 w4 = *reinterpret_cast<const float4 *>(&sWT[(J * 32 + k) * kPnWd + 4 * ct]);
+            const float wv[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                x[0][u] = fmaf(y0, wv[u], x[0][u]);
+                x[1][u] = fmaf(y1, wv[u], x[1][u]);
             }
         }
+        __syncthreads();  // every thread has read Y_J
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            sXT[(cj + u) * kPnXd + rt] = x[0][u];
+            sXT[(cj + u) * kPnXd + rt + 32] = x[1][u];
+        }
+        __syncthreads();
     }
-    // operand planes, 16-byte stores of 8 halves (zero for k >= b)
-    const int64_t r = j - q;
-    for (int k0 = 0; k0 < kpad; k0 += 8) {
+    // L21 back to the factor (columns contiguous)
+    for (int e = tid; e < kLpNb * kPnRows; e += 256) {
+        const int r = e % kPnRows, k = e / kPnRows;
+        const int64_t j = row0 + r;
+        if (j < n) L[j + (p + k) * ld] = sXT[k * kPnXd + r];
+    }
+    // operand planes, 16-byte stores of 8 halves: thread (row, 8-column group)
+    for (int e = tid; e < kPnRows * (kpad / 8); e += 256) {
+        const int r = e % kPnRows, k0 = (e / kPnRows) * 8;
+        const int64_t j = row0 + r;
+        if (j >= n) continue;
         H h[3][8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-            const float x = (k0 + u < b) ? my[k0 + u] : 0.f;
-            const H a0 = to_half<H>(x);
-            const float r1 = x - from_half(a0);  // exact in FP32
+            const float xv = (k0 + u < kLpNb) ? sXT[(k0 + u) * kPnXd + r] : 0.f;
+            const H a0 = to_half<H>(xv);
+            const float r1 = xv - from_half(a0);  // exact in FP32
             const H a1 = to_half<H>(r1);
             const float r2 = r1 - from_half(a1);
             h[0][u] = a0;
             h[1][u] = a1;
             h[2][u] = to_half<H>(r2);
         }
-        for (int t = 0; t < terms; ++t)
-            *(uint4 *)(planes + t * plane_stride + r * kpad + k0) = *(const uint4 *)h[t];
+#pragma unroll
+        for (int t = 0; t < 3; ++t)
+            if (t < terms) *(uint4 *)(planes + t * plane_stride + (j - q) * kpad + k0) = *(const uint4 *)h[t];
     }
 }
 
@@ -285,33 +352,35 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
     err_word = (int *)c->mixed.tcerr.p;
     if (cudaMemsetAsync(err_word, 0, sizeof(int), st) != cudaSuccess) return -1;
     const size_t smem_l11 = sizeof(float) * (kLpNb * kLpLd + 32 * kLpPd);
-    const size_t smem_panel = sizeof(float) * (2 * kLpNb * kLpLd + kLpNb);
-    static bool attr_done = false;
-    if (!attr_done) {
-        cudaFuncSetAttribute(lowp_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_l11);
-        cudaFuncSetAttribute(lowp_panel_kernel<__nv_bfloat16>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_panel);
+    const size_t smem_panel = kPnSmem;
+    if (c->mixed.pinv.ensure(sizeof(float) * 4 * 32 * 32) != cudaSuccess) return -1;
+    float *Wd = (float *)c->mixed.pinv.p;
+    // kernel attributes are per device: set them on every call (cheap)
+    if (cudaFuncSetAttribute(lowp_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_l11) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(lowp_panel_kernel<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_panel) != cudaSuccess ||
         cudaFuncSetAttribute(lowp_panel_kernel<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem_panel);
-        if (tc_update_prepare() != 0) return -1;
-        attr_done = true;
-    }
+                             (int)smem_panel) != cudaSuccess ||
+        tc_update_prepare() != 0)
+        return -1;
     for (int64_t p = 0; p < n; p += kLpNb) {
         const int b = (int)std::min<int64_t>(kLpNb, n - p);
         {
             LaunchScope ls(K_MIXED_DIAG, st, (double)b * b * b / 3.0);
-            lowp_diag_kernel<<<1, 1024, smem_l11, st>>>(L, ld, p, b, info, min_ratio);
+            lowp_diag_kernel<<<1, 1024, smem_l11, st>>>(L, ld, p, b, info, min_ratio, Wd);
         }
         const int64_t rest = n - p - b;
         if (rest <= 0) break;
         {
             LaunchScope ls(K_MIXED_PANEL, st, (double)rest * b * b);
+            // b == 128 whenever rows remain below the block
             if (fp16)
-                lowp_panel_kernel<__half><<<(unsigned)ceil_div(rest, 128), 128, smem_panel, st>>>(
-                    L, ld, n, p, b, (__half *)planes, plane_stride, kpad, terms, info);
+                lowp_panel_kernel<__half><<<(unsigned)ceil_div(rest, kPnRows), 256, smem_panel, st>>>(
+                    L, ld, n, p, Wd, (__half *)planes, plane_stride, kpad, terms, info);
             else
-                lowp_panel_kernel<__nv_bfloat16><<<(unsigned)ceil_div(rest, 128), 128, smem_panel, st>>>(
-                    L, ld, n, p, b, (__nv_bfloat16 *)planes, plane_stride, kpad, terms, info);
+                lowp_panel_kernel<__nv_bfloat16><<<(unsigned)ceil_div(rest, kPnRows), 256, smem_panel, st>>>(
+                    L, ld, n, p, Wd, (__nv_bfloat16 *)planes, plane_stride, kpad, terms, info);
         }
         // algorithmic work of the update: rest(rest+1)/2 entries x b multiply-adds x 2
         LaunchScope ls(K_MIXED_UPDATE, st, (double)rest * (rest + 1) * b);
