@@ -3,12 +3,13 @@
 //
 // Persistent CTAs (one per SM) walk the 128 x 128 lower tiles (I >= J) of the
 // trailing matrix:
-//   * one thread streams 64-wide K chunks of the two operand row blocks with
-//     TMA (cp.async.bulk.tensor, 128-byte swizzle) into a 6-stage
-//     shared-memory ring, completion tracked by mbarriers;
+//   * one thread streams 64-wide K chunks of the two operand row blocks, every
+//     term plane of a chunk in one TMA box (cp.async.bulk.tensor, 128-byte
+//     swizzle), into a shared-memory ring of 2-6 stages, completion tracked by
+//     mbarriers; diagonal tiles load their single row block once;
 //   * one thread issues tcgen05.mma (kind::f16, M = 128, N = 128, K = 16, BF16
-//     or FP16 operands, FP32 accumulator in tensor memory) for every chunk of
-//     every term pair, releasing each stage with tcgen05.commit, alternating
+//     or FP16 operands, FP32 accumulator in tensor memory) for every term pair
+//     of every chunk, releasing each stage with tcgen05.commit, alternating
 //     between two accumulators;
 //   * eight epilogue warps read a finished accumulator from tensor memory
 //     (tcgen05.ld 32x32b, two warps per 32-lane quarter) and subtract it from
@@ -28,10 +29,22 @@
 namespace lla {
 
 constexpr int kTcM = 128, kTcN = 128, kTcK = 64;  // tile and K-chunk
-constexpr int kTcStages = 6;
-constexpr int kTcTileBytes = kTcM * kTcK * 2;  // 16 KiB per operand per stage
-constexpr int kTcSmem = 1024 + 2 * kTcStages * kTcTileBytes + 256;
-constexpr uint32_t kTcCols = 128;  // tensor-memory columns (FP32 128 x 128 accumulator)
+constexpr int kTcTileBytes = kTcM * kTcK * 2;      // 16 KiB: one term plane of one operand
+constexpr int kTcRingBytes = 12 * kTcTileBytes;    // 192 KiB of operand stages
+constexpr int kTcMaxStages = 6;
+constexpr int kTcSmem = 1024 + kTcRingBytes + 256;
+// Stages of the ring: a stage holds every term plane of both operands for one
+// K-chunk (terms x 32 KiB), so each plane is loaded once per chunk and serves
+// all the term pairs that use it.
+__host__ __device__ constexpr int tc_stages(int terms) {
+    return (kTcRingBytes / (2 * terms * kTcTileBytes)) < kTcMaxStages ? kTcRingBytes / (2 * terms * kTcTileBytes)
+                                                                      : kTcMaxStages;
+}
+constexpr uint32_t kTcCols = 128;  // tensor-memory columns of one FP32 128 x 128 accumulator
+// Two accumulators per tile: the leading product h0 h0^T, and the sum of the
+// small cross-term products (summed among themselves first, as FP32 accuracy
+// wants), double-buffered: all 512 columns.
+constexpr uint32_t kTcAlloc = 4 * kTcCols;
 
 __device__ __forceinline__ void tc_tri_tile(int64_t t, int64_t &I, int64_t &J) {
     int64_t i = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
@@ -52,7 +65,7 @@ constexpr int kTcEpiThreads = 256;
 
 __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     const __grid_constant__ CUtensorMap tmap, float *C, int64_t ld, int64_t q, int64_t n, int kchunks,
-    TcPairs pairs, uint32_t idesc, int64_t ntiles, const int64_t *info, int *err_word) {
+    int terms, TcPairs pairs, uint32_t idesc, int64_t ntiles, const int64_t *info, int *err_word) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ int s_abort, s_skip;
     // one reader decides for the whole CTA (another CTA may set err_word meanwhile)
@@ -61,17 +74,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     __syncthreads();
     if (s_skip) return;
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint8_t *sA = smem;
-    uint8_t *sB = smem + kTcStages * kTcTileBytes;
-    uint64_t *bars = (uint64_t *)(smem + 2 * kTcStages * kTcTileBytes);
+    const int S = tc_stages(terms);
+    const uint32_t opnd = (uint32_t)terms * kTcTileBytes;  // one operand's planes in a stage
+    uint8_t *ring = smem;                                   // stage s: A planes, then B planes
+    uint64_t *bars = (uint64_t *)(smem + kTcRingBytes);
     // bars: full[S], empty[S], tmem_full[2], tmem_empty[2]
-    uint32_t *tslot = (uint32_t *)(bars + 2 * kTcStages + 4);
+    uint32_t *tslot = (uint32_t *)(bars + 2 * kTcMaxStages + 4);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kTcStages);
-    const uint32_t tfull0 = smem_u32(bars + 2 * kTcStages), tempty0 = tfull0 + 16;
-    const int per_tile = pairs.n * kchunks;
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kTcMaxStages);
+    const uint32_t tfull0 = smem_u32(bars + 2 * kTcMaxStages), tempty0 = tfull0 + 16;
     if (tid == 0) {
-        for (int s = 0; s < kTcStages; ++s) {
+        for (int s = 0; s < S; ++s) {
             mbar_init(full0 + 8 * s, 1);
             mbar_init(empty0 + 8 * s, 1);
         }
@@ -85,7 +98,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(tslot)),
-                     "r"(2 * kTcCols)
+                     "r"(kTcAlloc)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -100,19 +113,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
             for (int64_t t = blockIdx.x; t < ntiles && !*(volatile int *)&s_abort; t += gridDim.x) {
                 int64_t I, J;
                 tc_tri_tile(t, I, J);
-                for (int it = 0; it < per_tile; ++it, ++g) {
-                    const int s = (int)(g % kTcStages);
-                    const int64_t round = g / kTcStages;
+                for (int kc = 0; kc < kchunks; ++kc, ++g) {
+                    const int s = (int)(g % S);
+                    const int64_t round = g / S;
                     if (round > 0 && !mbar_wait(empty0 + 8 * s, (uint32_t)((round - 1) & 1), err_word)) {
                         s_abort = 1;
                         break;
                     }
-                    mbar_expect_tx(full0 + 8 * s, 2 * kTcTileBytes);
-                    const int pr = it / kchunks, kc = it % kchunks;
-                    tma_load_3d(smem_u32(sA + s * kTcTileBytes), &tmap, kc * kTcK, (int)(I * kTcM),
-                                pairs.pa[pr], full0 + 8 * s);
-                    tma_load_3d(smem_u32(sB + s * kTcTileBytes), &tmap, kc * kTcK, (int)(J * kTcN),
-                                pairs.pb[pr], full0 + 8 * s);
+                    const uint32_t st_a = smem_u32(ring + (size_t)s * 2 * opnd);
+                    mbar_expect_tx(full0 + 8 * s, (I == J ? 1u : 2u) * opnd);
+                    tma_load_3d(st_a, &tmap, kc * kTcK, (int)(I * kTcM), 0, full0 + 8 * s);
+                    if (I != J) tma_load_3d(st_a + opnd, &tmap, kc * kTcK, (int)(J * kTcN), 0, full0 + 8 * s);
                 }
             }
         }
@@ -120,6 +131,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
         if (lane == 0) {  // MMA issuer
             int64_t g = 0, lt = 0;
             for (int64_t t = blockIdx.x; t < ntiles && !*(volatile int *)&s_abort; t += gridDim.x, ++lt) {
+                int64_t I, J;
+                tc_tri_tile(t, I, J);
                 const int a = (int)(lt & 1);
                 const int64_t use = lt >> 1;
                 if (use > 0 && !mbar_wait(tempty0 + 8 * a, (uint32_t)((use - 1) & 1), err_word)) {
@@ -127,20 +140,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
                     break;
                 }
                 tc_fence_after();
-                const uint32_t dt = tmem + (uint32_t)(a * kTcCols);
-                for (int it = 0; it < per_tile; ++it, ++g) {
-                    const int s = (int)(g % kTcStages);
-                    if (!mbar_wait(full0 + 8 * s, (uint32_t)((g / kTcStages) & 1), err_word)) {
+                const uint32_t dt = tmem + (uint32_t)(a * 2 * kTcCols);  // leading; +kTcCols: cross terms
+                for (int kc = 0; kc < kchunks; ++kc, ++g) {
+                    const int s = (int)(g % S);
+                    if (!mbar_wait(full0 + 8 * s, (uint32_t)((g / S) & 1), err_word)) {
                         s_abort = 1;
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t a0 = smem_u32(sA + s * kTcTileBytes);
-                    const uint32_t b0 = smem_u32(sB + s * kTcTileBytes);
+                    const uint32_t st_a = smem_u32(ring + (size_t)s * 2 * opnd);
+                    const uint32_t st_b = (I == J) ? st_a : st_a + opnd;  // a diagonal tile uses its rows twice
+                    int first_x = 1;  // first cross-term product of this chunk
+                    for (int pr = 0; pr < pairs.n; ++pr) {
+                        const bool lead = pairs.pa[pr] == 0 && pairs.pb[pr] == 0;
+                        const uint32_t d = lead ? dt : dt + kTcCols;
+                        const bool fresh = kc == 0 && (lead || first_x);
+                        if (!lead) first_x = 0;
+                        const uint64_t ad = sw128_desc(st_a + (uint32_t)pairs.pa[pr] * kTcTileBytes);
+                        const uint64_t bd = sw128_desc(st_b + (uint32_t)pairs.pb[pr] * kTcTileBytes);
 #pragma unroll
-                    for (int k = 0; k < kTcK / 16; ++k)
-                        tc_mma(dt, sw128_desc(a0 + 32 * k), sw128_desc(b0 + 32 * k), idesc,
-                               (it > 0 || k > 0) ? 1u : 0u);
+                        for (int k = 0; k < kTcK / 16; ++k)  // +32 bytes along K per step
+                            tc_mma(d, ad + 2 * k, bd + 2 * k, idesc, (fresh && k == 0) ? 0u : 1u);
+                    }
                     tc_commit(empty0 + 8 * s);  // frees the stage once these MMAs are done
                 }
                 if (s_abort) break;
@@ -150,6 +171,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     } else {  // warps 0-7: epilogue; warp w drains lane quarter w % 4, columns 64 (w / 4) ..
         int64_t lt = 0;
         const int qw = warp & 3, half = warp >> 2;
+        const bool cross = pairs.n > 1;  // the cross-term accumulator is in use
         const int r = qw * 32 + lane;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
             const int a = (int)(lt & 1);
@@ -176,23 +198,30 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
                 break;
             }
             tc_fence_after();
+            const uint32_t ta = tmem + (uint32_t)(a * 2 * kTcCols) + ((uint32_t)(qw * 32) << 16);
 #pragma unroll
             for (int cb = 0; cb < 2; ++cb) {
-                uint32_t v[32];
-                tc_ld32(tmem + (uint32_t)(a * kTcCols) + ((uint32_t)(qw * 32) << 16) +
-                            (uint32_t)(half * 64 + cb * 32),
-                        v);
 #pragma unroll
-                for (int c = 0; c < 32; ++c) {
-                    const int cc = cb * 32 + c;
-                    const bool in = row_in && cc < cmax && (I != J || half * 64 + cc <= r);
-                    const float x = cur[c] - __uint_as_float(v[c]);
-                    if (cb == 0) {  // fetch the second half before storing the first
-                        const int c2 = 32 + c;
-                        const bool in2 = row_in && c2 < cmax && (I != J || half * 64 + c2 <= r);
-                        cur[c] = in2 ? base[c2 * ld] : 0.f;
+                for (int sb = 0; sb < 2; ++sb) {  // 16 columns: leading and cross-term sums
+                    uint32_t v[16], w[16];
+                    const uint32_t col = (uint32_t)(half * 64 + cb * 32 + sb * 16);
+                    tc_ld16_nowait(ta + col, v);
+                    if (cross) tc_ld16_nowait(ta + kTcCols + col, w);
+                    tc_wait_ld();
+#pragma unroll
+                    for (int c16 = 0; c16 < 16; ++c16) {
+                        const int c = sb * 16 + c16, cc = cb * 32 + c;
+                        const bool in = row_in && cc < cmax && (I != J || half * 64 + cc <= r);
+                        const float prod =
+                            cross ? __uint_as_float(v[c16]) + __uint_as_float(w[c16]) : __uint_as_float(v[c16]);
+                        const float x = cur[c] - prod;
+                        if (cb == 0) {  // fetch the second half before storing the first
+                            const int c2 = 32 + c;
+                            const bool in2 = row_in && c2 < cmax && (I != J || half * 64 + c2 <= r);
+                            cur[c] = in2 ? base[c2 * ld] : 0.f;
+                        }
+                        if (in) base[cc * ld] = x;
                     }
-                    if (in) base[cc * ld] = x;
                 }
             }
             tc_fence_before();
@@ -204,8 +233,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     if (s_abort && tid == 0) atomicCAS(err_word, 0, (int)LLA_ERR_TIMEOUT);
     tc_fence_after();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                     "r"(2 * kTcCols)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcAlloc)
                      : "memory");
 }
 
@@ -236,11 +264,11 @@ int tc_update_prepare() {
 int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, int64_t plane_stride,
                      int64_t rows, int kpad, int terms, bool fp16, const TcPairs &pairs,
                      const int64_t *info, int *err_word, int64_t tiles, cudaStream_t st) {
-    if (!g_encode || rows <= 0 || kpad % kTcK != 0) return -1;
+    if (!g_encode || rows <= 0 || kpad % kTcK != 0 || terms < 1 || terms > 3) return -1;
     CUtensorMap map;
     const cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rows, (cuuint64_t)terms};
     const cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)plane_stride * 2};
-    const cuuint32_t box[3] = {(cuuint32_t)kTcK, (cuuint32_t)kTcM, 1};
+    const cuuint32_t box[3] = {(cuuint32_t)kTcK, (cuuint32_t)kTcM, (cuuint32_t)terms};  // every term plane
     const cuuint32_t estr[3] = {1, 1, 1};
     const CUresult r =
         g_encode(&map, fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
@@ -261,7 +289,7 @@ int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, i
         if (sms <= 0) sms = 1;
     }
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, sms);
-    tc_update_kernel<<<grid, kTcThreads, kTcSmem, st>>>(map, C, ld, q, n, kpad / kTcK, pairs, idesc,
+    tc_update_kernel<<<grid, kTcThreads, kTcSmem, st>>>(map, C, ld, q, n, kpad / kTcK, terms, pairs, idesc,
                                                         tiles, info, err_word);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
