@@ -63,9 +63,21 @@ __device__ __forceinline__ void tc_tri_tile(int64_t t, int64_t &I, int64_t &J) {
 constexpr int kTcThreads = 320;  // 8 epilogue warps, 1 producer warp, 1 MMA warp
 constexpr int kTcEpiThreads = 256;
 
+// Term pairs (a, b) per number of terms, small products first; the last one,
+// (0, 0), is the leading product.
+__device__ __forceinline__ constexpr int tc_npairs(int terms) { return terms == 1 ? 1 : (terms == 2 ? 3 : 6); }
+__device__ __forceinline__ constexpr int tc_pa(int terms, int i) {
+    return terms == 1 ? 0 : (terms == 2 ? (i == 1 ? 1 : 0) : (i == 1 || i == 4 ? 1 : (i == 2 ? 2 : 0)));
+}
+__device__ __forceinline__ constexpr int tc_pb(int terms, int i) {
+    return terms == 1 ? 0 : (terms == 2 ? (i == 0 ? 1 : 0) : (i == 0 ? 2 : (i == 1 || i == 3 ? 1 : 0)));
+}
+
+template <int TERMS>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     const __grid_constant__ CUtensorMap tmap, float *C, int64_t ld, int64_t q, int64_t n, int kchunks,
-    int terms, TcPairs pairs, uint32_t idesc, int64_t ntiles, const int64_t *info, int *err_word) {
+    uint32_t idesc, int64_t ntiles, const int64_t *info, int *err_word) {
+    constexpr int terms = TERMS, NP = tc_npairs(TERMS);
     extern __shared__ uint8_t smem_raw[];
     __shared__ int s_abort, s_skip;
     // one reader decides for the whole CTA (another CTA may set err_word meanwhile)
@@ -150,14 +162,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
                     tc_fence_after();
                     const uint32_t st_a = smem_u32(ring + (size_t)s * 2 * opnd);
                     const uint32_t st_b = (I == J) ? st_a : st_a + opnd;  // a diagonal tile uses its rows twice
-                    int first_x = 1;  // first cross-term product of this chunk
-                    for (int pr = 0; pr < pairs.n; ++pr) {
-                        const bool lead = pairs.pa[pr] == 0 && pairs.pb[pr] == 0;
+                    const uint64_t ad0 = sw128_desc(st_a), bd0 = sw128_desc(st_b);
+#pragma unroll
+                    for (int pr = 0; pr < NP; ++pr) {
+                        const bool lead = pr == NP - 1;  // (0, 0)
                         const uint32_t d = lead ? dt : dt + kTcCols;
-                        const bool fresh = kc == 0 && (lead || first_x);
-                        if (!lead) first_x = 0;
-                        const uint64_t ad = sw128_desc(st_a + (uint32_t)pairs.pa[pr] * kTcTileBytes);
-                        const uint64_t bd = sw128_desc(st_b + (uint32_t)pairs.pb[pr] * kTcTileBytes);
+                        const bool fresh = kc == 0 && (lead || pr == 0);
+                        // descriptors address 16-byte units: a plane is kTcTileBytes / 16 further
+                        const uint64_t ad = ad0 + (uint64_t)(tc_pa(TERMS, pr) * (kTcTileBytes >> 4));
+                        const uint64_t bd = bd0 + (uint64_t)(tc_pb(TERMS, pr) * (kTcTileBytes >> 4));
 #pragma unroll
                         for (int k = 0; k < kTcK / 16; ++k)  // +32 bytes along K per step
                             tc_mma(d, ad + 2 * k, bd + 2 * k, idesc, (fresh && k == 0) ? 0u : 1u);
@@ -171,7 +184,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     } else {  // warps 0-7: epilogue; warp w drains lane quarter w % 4, columns 64 (w / 4) ..
         int64_t lt = 0;
         const int qw = warp & 3, half = warp >> 2;
-        const bool cross = pairs.n > 1;  // the cross-term accumulator is in use
+        constexpr bool cross = NP > 1;  // the cross-term accumulator is in use
         const int r = qw * 32 + lane;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
             const int a = (int)(lt & 1);
@@ -255,8 +268,12 @@ PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
 
 int tc_update_prepare() {
     if (!tma_encoder()) return -1;
-    if (cudaFuncSetAttribute(tc_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) !=
-        cudaSuccess)
+    if (cudaFuncSetAttribute(tc_update_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(tc_update_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(tc_update_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) !=
+            cudaSuccess)
         return -1;
     return 0;
 }
@@ -289,8 +306,12 @@ int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, i
         if (sms <= 0) sms = 1;
     }
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, sms);
-    tc_update_kernel<<<grid, kTcThreads, kTcSmem, st>>>(map, C, ld, q, n, kpad / kTcK, terms, pairs, idesc,
-                                                        tiles, info, err_word);
+    // the pair lists are fixed per number of terms (small products first, (0, 0) last)
+    if (pairs.n != (terms == 1 ? 1 : (terms == 2 ? 3 : 6)) || pairs.pa[pairs.n - 1] != 0 ||
+        pairs.pb[pairs.n - 1] != 0)
+        return -1;
+    auto kern = terms == 1 ? tc_update_kernel<1> : (terms == 2 ? tc_update_kernel<2> : tc_update_kernel<3>);
+    kern<<<grid, kTcThreads, kTcSmem, st>>>(map, C, ld, q, n, kpad / kTcK, idesc, tiles, info, err_word);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
