@@ -343,32 +343,58 @@ def main():
                "kernels": {k: {"ms": v[0] / args.steps, "launches": v[1] // args.steps}
                            for k, v in prof_alt.items()}}
 
-    # roofline of the dominant kernel of the headline (mixed) step
+    # roofline of the dominant kernel of the headline (mixed) step: algorithmic units per
+    # launch from the kernel's own accounting, live CUDA-event durations
     fp64_peak = lla.measure_peak_tflops(0)
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
         if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    bf16 = peaks.get("bf16_tflops", 1900.0)
+    peak_note = "MEASURED_PEAKS.json" if peaks else "fallback (6.8 TB/s, 1.9 PF/s)"
     dom = max(prof, key=lambda k: prof[k][0])
     dom_ms, dom_n, dom_work = prof[dom]
-    achieved = dom_work / (dom_ms * 1e-3) / 1e12
-    if dom in ("mixed_update",):
-        bound, peak, src = "tensor", peaks.get("bf16_tflops", 1891.6), \
-            "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks else "fallback 1.9 PF/s"
+    sec = dom_ms * 1e-3
+    extra = {}
+    if dom == "mixed_update":
+        # HBM-bound: every launch reads and writes the FP32 lower trailing matrix once;
+        # work = sum rest (rest + 1) 128 flops, so bytes = work / 128 * 4
+        alg = dom_work / 128 * 4
+        bound, unit, achieved, peak = "hbm", "GB/s", alg / sec / 1e9, hbm
+        extra = {"algorithmic_bytes_per_launch": alg / dom_n,
+                 "tensor_tflops_executed": 6 * dom_work / sec / 1e12,
+                 "note": "six BF16 term-pair products per tile (bf16x6)" if args.update == "bf16x6" else None}
+    elif dom == "mixed_trsm":
+        # two substitutions per iteration: each reads the FP32 factor's lower triangle once
+        nsub = max(1, dom_n - 2 * args.steps)  # minus the per-factor inverse and coupling kernels
+        alg = nsub * (2.0 * n * n + 16.0 * n * m)
+        bound, unit, achieved, peak = "hbm", "GB/s", alg / sec / 1e9, hbm
+        extra = {"algorithmic_bytes_per_launch": alg / nsub}
+    elif dom == "residual" and args.residual == "slices":
+        # 36 slice-pair products of 2 n^2 m each on the BF16 tensor cores; the eight
+        # BF16 slice planes of A (16 n^2 bytes) stream from HBM once per launch
+        bound, unit, achieved, peak = "tensor", "TFLOP/s", 36 * dom_work / sec / 1e12, bf16
+        extra = {"fp64_equivalent_tflops": dom_work / sec / 1e12,
+                 "algorithmic_bytes_per_launch": 16.0 * n * n}
     else:
-        bound, peak, src = "fp64-tensor", fp64_peak, \
-            "measured live: 8 independent mma.sync m16n8k16 f64 per step on all SMs " \
-            "(the measured peak table has HBM and bf16 only)"
+        bound, unit, achieved, peak = "fp64-tensor", "TFLOP/s", dom_work / sec / 1e12, fp64_peak
+        peak_note = "measured live: 8 independent mma.sync m16n8k16 f64 per step on all SMs"
     traffic, traffic_src = None, None
     tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if os.path.exists(tpath):
-        t = json.load(open(tpath)).get(dom)
-        if t:  # ncu capture of a smaller case, scaled by the units one launch processes
+        t = json.load(open(tpath)).get("residual_slices" if dom == "residual" and args.residual == "slices"
+                                        else dom)
+        if t and "algorithmic_bytes" in t and "algorithmic_bytes_per_launch" in extra:
+            # DRAM bytes / algorithmic bytes of one captured launch, applied to this workload's launches
+            traffic = t["dram_bytes"] / t["algorithmic_bytes"] * extra["algorithmic_bytes_per_launch"]
+            traffic_src = f"{t['source']} (DRAM/algorithmic = {t['dram_bytes'] / t['algorithmic_bytes']:.2f})"
+        elif t:
             traffic = t["dram_bytes"] * (n / t["n_captured"]) ** t["exponent"]
             traffic_src = f"{t['source']}, scaled from n={t['n_captured']} by (n/{t['n_captured']})^{t['exponent']}"
-    roofline = {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak if peak and peak > 0 else None,
+    roofline = {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+                "frac": achieved / peak if peak and peak > 0 else None,
                 "traffic": traffic, "traffic_source": traffic_src,
                 "share_of_step": dom_ms / ms_mixed, "avg_launch_ms": dom_ms / dom_n,
-                "peak_source": src}
+                "peak_source": peak_note, **{k: v for k, v in extra.items() if v is not None}}
 
     # end to end through the C ABI with host (pinned) buffers: lla_dposv_refined reads A
     # and overwrites B with X
