@@ -162,13 +162,17 @@ __device__ __forceinline__ unsigned long long iv_settle_word(unsigned long long 
 constexpr int kIvCols = 16;   // right-hand-side columns per CTA
 constexpr int kIvLd = 68;     // shared row stride of a staged 64 x 64 tile (floats; 16-byte rows)
 constexpr int kIvStages = 3;  // coupling tiles in flight per CTA
-constexpr size_t kIvSmem =
-    sizeof(float) * ((size_t)kIvStages * kIvNb * kIvLd + 2ull * kIvStages * kIvCols * kIvNb + 2ull * kIvNb * kIvCols);
+constexpr int kIvYd = kIvNb + 2;  // words per staged column (padded: 528-byte columns)
+constexpr size_t kIvSmem = sizeof(float) * ((size_t)kIvStages * kIvNb * kIvLd + 2ull * kIvStages * kIvCols * kIvYd +
+                                            2ull * kIvNb * kIvCols);
 
 // TRANS = false: L Y = B (blocks ascending); TRANS = true: L^T X = B (descending).
-// 256 threads: for products, thread (ta = tid % 64, tb = tid / 64) owns row ta
-// and columns 4 tb .. 4 tb + 3 of the CTA's 16.  The coupling tiles and the
-// solved words of earlier blocks stream through a kIvStages-deep cp.async ring.
+// 256 threads.  The coupling tiles and the solved words of earlier blocks
+// stream through a kIvStages-deep cp.async ring; for their products thread
+// (c = tid % 16, rg = tid / 16) owns column c and rows 4 rg .. 4 rg + 3 and
+// reads the words where they landed (validated in place).  For the block's
+// own products (inverse, neighbour) thread (ta = tid % 64, tb = tid / 64)
+// owns row ta and columns 4 tb .. 4 tb + 3.
 template <bool TRANS>
 __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restrict__ L, int64_t ld,
                                                           const float *__restrict__ Wall, int64_t n,
@@ -178,11 +182,11 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
     constexpr int C = kIvCols, LPT = kIvTile / 256, NS = kIvStages;
     constexpr int YCH = kIvNb * C / 2 / 256;  // 16-byte (two-word) copies per thread per stage
     extern __shared__ __align__(16) float iv_smem[];
-    // sT[s][a][b]: staged tile; sY[s][c][k]: raw solved words; sV[buf][k][c]: their values
+    // sT[s][a][b]: staged tile; sY[s][c][k]: solved words; sV[2][k][c]: the block's own products
     float(*sT)[kIvNb][kIvLd] = reinterpret_cast<float(*)[kIvNb][kIvLd]>(iv_smem);
-    unsigned long long(*sY)[C][kIvNb] =
-        reinterpret_cast<unsigned long long(*)[C][kIvNb]>(iv_smem + NS * kIvNb * kIvLd);
-    float(*sV)[kIvNb][C] = reinterpret_cast<float(*)[kIvNb][C]>(iv_smem + NS * kIvNb * kIvLd + 2 * NS * C * kIvNb);
+    unsigned long long(*sY)[C][kIvYd] =
+        reinterpret_cast<unsigned long long(*)[C][kIvYd]>(iv_smem + NS * kIvNb * kIvLd);
+    float(*sV)[kIvNb][C] = reinterpret_cast<float(*)[kIvNb][C]>(iv_smem + NS * kIvNb * kIvLd + 2 * NS * C * kIvYd);
     __shared__ int s_ticket, s_abort;
     const int tid = threadIdx.x;
     if (tid == 0) {
@@ -200,11 +204,12 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
     const unsigned long long tag = (unsigned long long)epoch << 32;
     const bool al16 = (ld % 4 == 0) && ((reinterpret_cast<uintptr_t>(L) & 15) == 0);
 
+    const int bc = tid % C, rg = tid / C;  // bulk mapping: column bc, rows 4 rg .. 4 rg + 3
     float acc[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        const int64_t col = col0 + tb * 4 + u;
-        acc[u] = (grow < n && col < m) ? B[grow + col * ldb] : 0.f;
+    for (int i = 0; i < 4; ++i) {
+        const int64_t row = rb * kIvNb + 4 * rg + i, col = col0 + bc;
+        acc[i] = (row < n && col < m) ? B[row + col * ldb] : 0.f;
     }
     // this block's inverse and coupling matrix (element (ta, tb + 4u) of each), needed only at the end
     float preW[LPT], preM[LPT];
@@ -254,9 +259,11 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
         }
         iv_commit();
     };
-    // Values of the words this thread copied into stage s; unpublished ones
-    // are re-read from global memory until they carry this launch's tag.
-    auto settle_stage = [&](int64_t pq, int s, int buf) {
+    // The words this thread copied into stage s that are not yet published
+    // are re-read from global memory until they carry this launch's tag, and
+    // replaced in place (words past n or m are zero: never written, or
+    // zero-filled by the copy).
+    auto settle_stage = [&](int64_t pq, int s) {
         const int64_t qb = TRANS ? R - 1 - pq : pq;
 #pragma unroll
         for (int j = 0; j < YCH; ++j) {
@@ -265,13 +272,9 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
             for (int h = 0; h < 2; ++h) {
                 const int k = 2 * kp + h;
                 const int64_t gk = qb * kIvNb + k, col = col0 + c;
-                float v = 0.f;
-                if (gk < n && col < m) {
-                    const unsigned long long w =
-                        iv_settle_word(sY[s][c][k], ll + gk + col * ldl, tag, err_word, &s_abort);
-                    v = __uint_as_float((unsigned)(w & 0xffffffffull));
-                }
-                sV[buf][k][c] = v;
+                const unsigned long long w0 = sY[s][c][k];
+                if (gk < n && col < m && (w0 & 0xffffffff00000000ull) != tag)
+                    sY[s][c][k] = iv_settle_word(w0, ll + gk + col * ldl, tag, err_word, &s_abort);
             }
         }
     };
@@ -280,34 +283,39 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
 #pragma unroll
     for (int s = 0; s < NS - 1; ++s) issue(s, s);
     for (int64_t pq = 0; pq < nbulk; ++pq) {
-        const int s = (int)(pq % NS), buf = (int)(pq & 1);
+        const int s = (int)(pq % NS);
         iv_wait<NS - 2>();
-        settle_stage(pq, s, buf);
+        settle_stage(pq, s);
         __syncthreads();
         if (s_abort) break;
         issue(pq + NS - 1, (int)((pq + NS - 1) % NS));
-        if (!TRANS) {
+        const unsigned long long *yc = sY[s][bc];  // column bc of the solved block
+        if (!TRANS) {  // coefficient of x_k in row i: sT[s][k][i]
 #pragma unroll 8
             for (int k = 0; k < kIvNb; ++k) {
-                const float l = sT[s][k][ta];
-                const float4 x = *reinterpret_cast<const float4 *>(&sV[buf][k][tb * 4]);
-                acc[0] = fmaf(-l, x.x, acc[0]);
-                acc[1] = fmaf(-l, x.y, acc[1]);
-                acc[2] = fmaf(-l, x.z, acc[2]);
-                acc[3] = fmaf(-l, x.w, acc[3]);
+                const float4 l4 = *reinterpret_cast<const float4 *>(&sT[s][k][4 * rg]);
+                const float x = __uint_as_float((unsigned)yc[k]);
+                acc[0] = fmaf(-l4.x, x, acc[0]);
+                acc[1] = fmaf(-l4.y, x, acc[1]);
+                acc[2] = fmaf(-l4.z, x, acc[2]);
+                acc[3] = fmaf(-l4.w, x, acc[3]);
             }
-        } else {
+        } else {  // coefficient of x_k in row i: sT[s][i][k]
 #pragma unroll 2
             for (int k4 = 0; k4 < kIvNb / 4; ++k4) {
-                const float4 l4 = *reinterpret_cast<const float4 *>(&sT[s][ta][4 * k4]);
-                const float lv[4] = {l4.x, l4.y, l4.z, l4.w};
+                const ulonglong2 w01 = *reinterpret_cast<const ulonglong2 *>(&yc[4 * k4]);
+                const ulonglong2 w23 = *reinterpret_cast<const ulonglong2 *>(&yc[4 * k4 + 2]);
+                const float x0 = __uint_as_float((unsigned)w01.x), x1 = __uint_as_float((unsigned)w01.y);
+                const float x2 = __uint_as_float((unsigned)w23.x), x3 = __uint_as_float((unsigned)w23.y);
 #pragma unroll
-                for (int kk = 0; kk < 4; ++kk) {
-                    const float4 x = *reinterpret_cast<const float4 *>(&sV[buf][4 * k4 + kk][tb * 4]);
-                    acc[0] = fmaf(-lv[kk], x.x, acc[0]);
-                    acc[1] = fmaf(-lv[kk], x.y, acc[1]);
-                    acc[2] = fmaf(-lv[kk], x.z, acc[2]);
-                    acc[3] = fmaf(-lv[kk], x.w, acc[3]);
+                for (int i = 0; i < 4; ++i) {
+                    const float4 l4 = *reinterpret_cast<const float4 *>(&sT[s][4 * rg + i][4 * k4]);
+                    float a = acc[i];
+                    a = fmaf(-l4.x, x0, a);
+                    a = fmaf(-l4.y, x1, a);
+                    a = fmaf(-l4.z, x2, a);
+                    a = fmaf(-l4.w, x3, a);
+                    acc[i] = a;
                 }
             }
         }
@@ -329,7 +337,7 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
     float(*sK)[kIvLd] = sT[0];  // coefficient tile: sK[k][i]
     float(*sX)[C] = sV[0];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) sX[ta][tb * 4 + u] = acc[u];
+    for (int i = 0; i < 4; ++i) sX[4 * rg + i][bc] = acc[i];
 #pragma unroll
     for (int u = 0; u < LPT; ++u) {  // preW[u] = W[ta][tb + 4u]
         if (!TRANS)
