@@ -166,6 +166,31 @@ int lla_dis_triangular(const double *a, int64_t rows, int64_t cols, int64_t rs, 
 int lla_sis_triangular(const float *a, int64_t rows, int64_t cols, int64_t rs, int64_t cs,
                        int uplo, int *result, lla_error *err);
 
+/* ---- LOBPCG's Cholesky-QR (callers of the path) ----
+ * lla_?orthonormalize replaces `orthonormalize` (src/lobpcg/algorithm.rs:81-96):
+ * G = V^T V (n x k view v, read), L = cholesky_into(G) written to the k x k view
+ * l (lower factor, upper part zeroed), U = V L^-T written to the n x k view u
+ * (solve_triangular_into(V^T, Lower), transposed back).  Returns
+ * LLA_ERR_NOT_POSITIVE_DEFINITE (index = failing row of G, u and l untouched)
+ * when G is not positive definite; LLA_ERR_INVALID_ARG for mismatched views.
+ * The Cholesky of G and the substitution follow the reference's order (EXACT
+ * for k <= 1024 in LLA_ALGO_AUTO); G itself is summed in fixed row chunks.
+ * lla_?apply_constraints replaces `apply_constraints` (:63-76): v (n x k) -=
+ * y (n x ky) U with lyy U = y^T v (lyy: ky x ky lower factor, e.g. from
+ * lla_?cholesky_inplace). */
+int lla_dorthonormalize(const double *v, int64_t rows, int64_t cols, int64_t rs, int64_t cs, double *u,
+                        int64_t urows, int64_t ucols, int64_t urs, int64_t ucs, double *l, int64_t lrows,
+                        int64_t lcols, int64_t lrs, int64_t lcs, lla_error *err);
+int lla_sorthonormalize(const float *v, int64_t rows, int64_t cols, int64_t rs, int64_t cs, float *u,
+                        int64_t urows, int64_t ucols, int64_t urs, int64_t ucs, float *l, int64_t lrows,
+                        int64_t lcols, int64_t lrs, int64_t lcs, lla_error *err);
+int lla_dapply_constraints(double *v, int64_t rows, int64_t cols, int64_t rs, int64_t cs, const double *y,
+                           int64_t yrows, int64_t ycols, int64_t yrs, int64_t ycs, const double *lyy,
+                           int64_t lrows, int64_t lcols, int64_t lrs, int64_t lcs, lla_error *err);
+int lla_sapply_constraints(float *v, int64_t rows, int64_t cols, int64_t rs, int64_t cs, const float *y,
+                           int64_t yrows, int64_t ycols, int64_t yrs, int64_t ycs, const float *lyy,
+                           int64_t lrows, int64_t lcols, int64_t lrs, int64_t lcs, lla_error *err);
+
 /* ---- device-resident entry points (no counterpart in the reference) ----
  * Matrices are column-major device arrays with a leading dimension; `stream`
  * is a cudaStream_t (NULL = the legacy default stream).  Calls are

@@ -150,6 +150,8 @@ for _p in "ds":
         f"lla_{_p}triangular_inplace": (_V + [ctypes.c_int, _E], ctypes.c_int),
         f"lla_{_p}is_triangular": (_V + [ctypes.c_int, ctypes.POINTER(ctypes.c_int), _E],
                                    ctypes.c_int),
+        f"lla_{_p}orthonormalize": (_V + _V + _V + [_E], ctypes.c_int),
+        f"lla_{_p}apply_constraints": (_V + _V + _V + [_E], ctypes.c_int),
         f"lla_{_p}potrf_device": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
                                    ctypes.c_void_p, ctypes.c_void_p, _E], ctypes.c_int),
         f"lla_{_p}trsm_device": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
@@ -385,6 +387,33 @@ def solve_triangular_into(a, b, uplo):
 def solve_triangular(a, b, uplo):
     """SolveTriangular::solve_triangular: solves into a copy of b."""
     return solve_triangular_inplace(a, np.array(b), uplo)
+
+
+def orthonormalize(v):
+    """LOBPCG's Cholesky-QR `orthonormalize` (src/lobpcg/algorithm.rs:81-96):
+    returns (U, L) with L = cholesky_into(V^T V) and U = V L^-T."""
+    if not isinstance(v, np.ndarray) or v.ndim != 2:
+        raise TypeError("expected a 2-D numpy array")
+    n, k = v.shape
+    u = np.empty((n, k), dtype=v.dtype)
+    l = np.empty((k, k), dtype=v.dtype)
+    e = Error()
+    getattr(lib, f"lla_{_prefix(v)}orthonormalize")(*_view(v), *_view(u), *_view(l), ctypes.byref(e))
+    _raise(e)
+    return u, l
+
+
+def apply_constraints(v, cholesky_yy, y):
+    """LOBPCG's `apply_constraints` (src/lobpcg/algorithm.rs:63-76): v -= y U with
+    cholesky_yy U = y^T v; updates v in place and returns it."""
+    _writable(v)
+    _same_dtype(v, y)
+    _same_dtype(v, cholesky_yy)
+    e = Error()
+    getattr(lib, f"lla_{_prefix(v)}apply_constraints")(*_view(v), *_view(y), *_view(cholesky_yy),
+                                                        ctypes.byref(e))
+    _raise(e)
+    return v
 
 
 def triangular_inplace(a, uplo):

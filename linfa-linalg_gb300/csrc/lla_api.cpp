@@ -620,6 +620,114 @@ int is_triangular_impl(const T *a, int64_t rows, int64_t cols, int64_t rs, int64
     return LLA_OK;
 }
 
+// Layout of an output view's device copy (nothing uploaded: every entry is
+// written before the download): the view's own layout when contiguous, else
+// column-major with gather/scatter through the staging buffer at download.
+cudaError_t prepare_out(const View &v, DevBuf &raw, int64_t &drs, int64_t &dcs) {
+    if (rowmajor_contig(v) && !colmajor_contig(v)) {
+        drs = v.cols;
+        dcs = 1;
+    } else {
+        drs = 1;
+        dcs = v.rows;
+    }
+    return raw.ensure((size_t)(v.rows * v.cols) * v.esz);
+}
+
+// orthonormalize (src/lobpcg/algorithm.rs:81-96): G = V^T V, L = cholesky_into(G),
+// U = (L^-1 V^T)^T.
+template <typename T>
+int orthonormalize_impl(const T *v, int64_t rows, int64_t cols, int64_t rs, int64_t cs, T *u, int64_t urows,
+                        int64_t ucols, int64_t urs, int64_t ucs, T *l, int64_t lrows, int64_t lcols, int64_t lrs,
+                        int64_t lcs, lla_error *err) {
+    if (bad_view(v, rows, cols) || bad_view(u, urows, ucols) || bad_view(l, lrows, lcols) || urows != rows ||
+        ucols != cols || lrows != cols || lcols != cols)
+        return lla__set_status(err, LLA_ERR_INVALID_ARG);
+    lla__set_status(err, LLA_OK);
+    const int64_t n = rows, k = cols;
+    if (k == 0) return LLA_OK;
+    Ctx *c = get_ctx(err);
+    if (!c) return err ? err->code : LLA_ERR_NO_DEVICE;
+    View vv{(char *)v, n, k, rs, cs, sizeof(T)};
+    int64_t drs, dcs;
+    LLA_TRY_CUDA(upload(*c, vv, c->raw_a, c->stage_a, drs, dcs));
+    LLA_TRY_CUDA(c->work_b.ensure(sizeof(T) * (n > 0 ? n : 1) * k));
+    LLA_TRY_CUDA(c->work_a.ensure(sizeof(T) * k * k));
+    LLA_TRY_CUDA(c->lob_g.ensure(sizeof(T) * k * k));
+    LLA_TRY_CUDA(c->lob_p.ensure(sizeof(T) * atb_ws_elems(n, k, k)));
+    LLA_TRY_CUDA(c->lob_t.ensure(sizeof(T) * k * (n > 0 ? n : 1)));
+    T *WV = (T *)c->work_b.p, *G = (T *)c->work_a.p, *Gc = (T *)c->lob_g.p, *VT = (T *)c->lob_t.p;
+    LLA_TRY_CUDA(launch_status(import_launch<T>((const T *)c->raw_a.p, drs, dcs, n, k, WV, n, c->stream)));
+    LLA_TRY_CUDA(launch_status(atb_launch<T>(WV, n, WV, n, n, k, k, G, k, (T *)c->lob_p.p, 1, c->stream)));
+    LLA_TRY_CUDA(cudaMemcpyAsync(Gc, G, sizeof(T) * k * k, cudaMemcpyDeviceToDevice, c->stream));
+    int64_t fail = -1;
+    LLA_TRY_CUDA(factor_on_device<T>(*c, G, k, k, use_exact(k), Gc, 1, k, &fail));
+    if (fail >= 0) return not_pd(err, fail);
+    // L: lower factor, upper part zeroed (cholesky_into)
+    View vl{(char *)l, k, k, lrs, lcs, sizeof(T)};
+    int64_t lrs_d, lcs_d;
+    LLA_TRY_CUDA(prepare_out(vl, c->raw_c, lrs_d, lcs_d));
+    LLA_TRY_CUDA(launch_status(export_launch<T>(G, k, (T *)c->raw_c.p, lrs_d, lcs_d, k, k, EXPORT_LOWER_ZERO_UPPER,
+                                                -1, c->stream)));
+    if (n > 0) {
+        // V^T (k x n), L Z = V^T, U = Z^T
+        LLA_TRY_CUDA(launch_status(import_launch<T>(WV, n, 1, k, n, VT, k, c->stream)));
+        int to = 0;
+        LLA_TRY_CUDA(trsm_on_device<T>(*c, G, k, k, /*lower=*/1, /*trans=*/0, nullptr, VT, k, n, use_exact(k), &to));
+        if (to) return lla__set_status(err, LLA_ERR_TIMEOUT);
+        LLA_TRY_CUDA(launch_status(import_launch<T>(VT, k, 1, n, k, WV, n, c->stream)));
+        View vu{(char *)u, n, k, urs, ucs, sizeof(T)};
+        int64_t urs_d, ucs_d;
+        LLA_TRY_CUDA(prepare_out(vu, c->raw_b, urs_d, ucs_d));
+        LLA_TRY_CUDA(launch_status(
+            export_launch<T>(WV, n, (T *)c->raw_b.p, urs_d, ucs_d, n, k, EXPORT_FULL, -1, c->stream)));
+        LLA_TRY_CUDA(download(*c, vu, c->raw_b, c->stage_b));
+    }
+    LLA_TRY_CUDA(download(*c, vl, c->raw_c, c->stage_c));
+    return LLA_OK;
+}
+
+// apply_constraints (src/lobpcg/algorithm.rs:63-76): U from lyy U = y^T v, v -= y U.
+template <typename T>
+int apply_constraints_impl(T *v, int64_t rows, int64_t cols, int64_t rs, int64_t cs, const T *y, int64_t yrows,
+                           int64_t ycols, int64_t yrs, int64_t ycs, const T *lyy, int64_t lrows, int64_t lcols,
+                           int64_t lrs, int64_t lcs, lla_error *err) {
+    if (bad_view(v, rows, cols) || bad_view(y, yrows, ycols) || bad_view(lyy, lrows, lcols) || yrows != rows)
+        return lla__set_status(err, LLA_ERR_INVALID_ARG);
+    if (lrows != lcols) return not_square(err, lrows, lcols);  // solve_triangular_into's check
+    if (lrows != ycols) return wrong_rows(err, lrows, ycols);
+    lla__set_status(err, LLA_OK);
+    const int64_t n = rows, k = cols, ky = ycols;
+    if (n == 0 || k == 0 || ky == 0) return LLA_OK;
+    Ctx *c = get_ctx(err);
+    if (!c) return err ? err->code : LLA_ERR_NO_DEVICE;
+    View vv{(char *)v, n, k, rs, cs, sizeof(T)};
+    View vy{(char *)y, n, ky, yrs, ycs, sizeof(T)};
+    View vl{(char *)lyy, ky, ky, lrs, lcs, sizeof(T)};
+    int64_t vrs, vcs, yrs_d, ycs_d, lrs_d, lcs_d;
+    LLA_TRY_CUDA(upload(*c, vv, c->raw_a, c->stage_a, vrs, vcs));
+    LLA_TRY_CUDA(upload(*c, vy, c->raw_b, c->stage_b, yrs_d, ycs_d));
+    LLA_TRY_CUDA(upload(*c, vl, c->raw_c, c->stage_c, lrs_d, lcs_d));
+    LLA_TRY_CUDA(c->work_a.ensure(sizeof(T) * ky * ky));
+    LLA_TRY_CUDA(c->work_b.ensure(sizeof(T) * n * k));
+    LLA_TRY_CUDA(c->lob_t.ensure(sizeof(T) * n * ky));
+    LLA_TRY_CUDA(c->lob_g.ensure(sizeof(T) * ky * k));
+    LLA_TRY_CUDA(c->lob_p.ensure(sizeof(T) * atb_ws_elems(n, ky, k)));
+    T *WL = (T *)c->work_a.p, *WV = (T *)c->work_b.p, *WY = (T *)c->lob_t.p, *GU = (T *)c->lob_g.p;
+    LLA_TRY_CUDA(launch_status(import_launch<T>((const T *)c->raw_a.p, vrs, vcs, n, k, WV, n, c->stream)));
+    LLA_TRY_CUDA(launch_status(import_launch<T>((const T *)c->raw_b.p, yrs_d, ycs_d, n, ky, WY, n, c->stream)));
+    LLA_TRY_CUDA(launch_status(import_launch<T>((const T *)c->raw_c.p, lrs_d, lcs_d, ky, ky, WL, ky, c->stream)));
+    LLA_TRY_CUDA(launch_status(atb_launch<T>(WY, n, WV, n, n, ky, k, GU, ky, (T *)c->lob_p.p, 0, c->stream)));
+    int to = 0;
+    LLA_TRY_CUDA(trsm_on_device<T>(*c, WL, ky, ky, /*lower=*/1, /*trans=*/0, nullptr, GU, ky, k, use_exact(ky), &to));
+    if (to) return lla__set_status(err, LLA_ERR_TIMEOUT);
+    LLA_TRY_CUDA(launch_status(sub_tall_launch<T>(WV, n, WY, n, GU, ky, n, ky, k, c->stream)));
+    LLA_TRY_CUDA(launch_status(
+        export_launch<T>(WV, n, (T *)c->raw_a.p, vrs, vcs, n, k, EXPORT_FULL, -1, c->stream)));
+    LLA_TRY_CUDA(download(*c, vv, c->raw_a, c->stage_a));
+    return LLA_OK;
+}
+
 }  // namespace
 
 // ---- mixed-precision refined solve on host views ---------------------------
@@ -761,6 +869,30 @@ int lla_dtriangular_inplace(LLA_VIEW_ARGS(double), int uplo, lla_error *err) {
 }
 int lla_striangular_inplace(LLA_VIEW_ARGS(float), int uplo, lla_error *err) {
     return triangular_impl<float>(a, rows, cols, rs, cs, uplo, err);
+}
+int lla_dorthonormalize(const double *v, int64_t rows, int64_t cols, int64_t rs, int64_t cs, double *u,
+                        int64_t urows, int64_t ucols, int64_t urs, int64_t ucs, double *l, int64_t lrows,
+                        int64_t lcols, int64_t lrs, int64_t lcs, lla_error *err) {
+    return orthonormalize_impl<double>(v, rows, cols, rs, cs, u, urows, ucols, urs, ucs, l, lrows, lcols, lrs, lcs,
+                                       err);
+}
+int lla_sorthonormalize(const float *v, int64_t rows, int64_t cols, int64_t rs, int64_t cs, float *u,
+                        int64_t urows, int64_t ucols, int64_t urs, int64_t ucs, float *l, int64_t lrows,
+                        int64_t lcols, int64_t lrs, int64_t lcs, lla_error *err) {
+    return orthonormalize_impl<float>(v, rows, cols, rs, cs, u, urows, ucols, urs, ucs, l, lrows, lcols, lrs, lcs,
+                                      err);
+}
+int lla_dapply_constraints(double *v, int64_t rows, int64_t cols, int64_t rs, int64_t cs, const double *y,
+                           int64_t yrows, int64_t ycols, int64_t yrs, int64_t ycs, const double *lyy,
+                           int64_t lrows, int64_t lcols, int64_t lrs, int64_t lcs, lla_error *err) {
+    return apply_constraints_impl<double>(v, rows, cols, rs, cs, y, yrows, ycols, yrs, ycs, lyy, lrows, lcols, lrs,
+                                          lcs, err);
+}
+int lla_sapply_constraints(float *v, int64_t rows, int64_t cols, int64_t rs, int64_t cs, const float *y,
+                           int64_t yrows, int64_t ycols, int64_t yrs, int64_t ycs, const float *lyy,
+                           int64_t lrows, int64_t lcols, int64_t lrs, int64_t lcs, lla_error *err) {
+    return apply_constraints_impl<float>(v, rows, cols, rs, cs, y, yrows, ycols, yrs, ycs, lyy, lrows, lcols, lrs,
+                                         lcs, err);
 }
 int lla_dis_triangular(LLA_VIEW_ARGS(const double), int uplo, int *result, lla_error *err) {
     return is_triangular_impl<double>(a, rows, cols, rs, cs, uplo, result, err);

@@ -57,6 +57,8 @@ struct Ctx {
     DevBuf ws;                        // triangular-solve tickets and flags
     DevBuf dev_s, dev_d, dev_ws;      // scratch of the device-resident entry points
     HostBuf stage_a, stage_b;         // pinned staging for strided views
+    DevBuf raw_c, lob_g, lob_p, lob_t;  // Cholesky-QR: third view, Gram copy, partials, transposes
+    HostBuf stage_c;
     ~Ctx();
 };
 

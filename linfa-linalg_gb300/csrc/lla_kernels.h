@@ -63,4 +63,17 @@ int is_triangular_launch(const T *R, int64_t rs, int64_t cs, int64_t n, int uplo
 template <typename T>
 int eye_launch(T *W, int64_t ld, int64_t n, cudaStream_t st);
 
+// Tall-skinny products of LOBPCG's Cholesky-QR (lla_lobpcg.cu).
+// C (ka x kb, ldc) = A^T B for A n x ka, B n x kb (column-major); P: workspace
+// of atb_ws_elems(n, ka, kb) elements; symmetric: A == B (only the lower
+// tiles are formed, the upper part mirrors them).  Deterministic.
+size_t atb_ws_elems(int64_t n, int64_t ka, int64_t kb);
+template <typename T>
+int atb_launch(const T *A, int64_t lda, const T *B, int64_t ldb, int64_t n, int64_t ka, int64_t kb, T *C,
+               int64_t ldc, T *P, int symmetric, cudaStream_t st);
+// V (n x k) -= Y (n x ky) U (ky x k).
+template <typename T>
+int sub_tall_launch(T *V, int64_t ldv, const T *Y, int64_t ldy, const T *U, int64_t ldu, int64_t n, int64_t ky,
+                    int64_t k, cudaStream_t st);
+
 }  // namespace lla

@@ -143,3 +143,19 @@ def invc_inplace(a):
 
 def build_info():
     return lib().ora_build_info().decode()
+
+
+def orthonormalize(v):
+    """LOBPCG's Cholesky-QR (src/lobpcg/algorithm.rs:81-96) composed from the
+    restated path: G = V^T V (ndarray's `dot`, i.e. the matrixmultiply crate,
+    is not part of this restatement: numpy's product stands in for it, so G
+    matches the reference to rounding), L = cholesky_into(G)
+    (src/cholesky.rs:24-43), U = solve_triangular_into(V^T, Lower)^T
+    (src/triangular.rs:161-168).  Returns (status dict, U, L)."""
+    g = np.array(v.T @ v, order="C")
+    st = cholesky_inplace(g)
+    if st["code"] != 0:
+        return st, None, None
+    vt = np.array(v.T, order="C")
+    st = solve_triangular_inplace(g, vt, "lower")
+    return st, np.array(vt.T), g
