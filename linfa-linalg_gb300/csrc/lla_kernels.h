@@ -62,6 +62,9 @@ int is_triangular_launch(const T *R, int64_t rs, int64_t cs, int64_t n, int uplo
 // W = identity (n x n, ld).
 template <typename T>
 int eye_launch(T *W, int64_t ld, int64_t n, cudaStream_t st);
+// W[i + j*ld] = W[j + i*ld] for i < j: the strict upper part from the lower one.
+template <typename T>
+int symmetrize_launch(T *W, int64_t ld, int64_t n, cudaStream_t st);
 
 // Tall-skinny products of LOBPCG's Cholesky-QR (lla_lobpcg.cu).
 // C (ka x kb, ldc) = A^T B for A n x ka, B n x kb (column-major); P: workspace

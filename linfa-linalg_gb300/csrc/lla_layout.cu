@@ -143,6 +143,34 @@ int eye_launch(T *W, int64_t ld, int64_t n, cudaStream_t st) {
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+// The strict upper part from the lower one: block (I, J), I <= J, writes the
+// entries i < j of output tile (I, J) from the transposed lower tile (J, I),
+// staged through shared memory so both sides stay coalesced.
+template <typename T>
+__global__ void symmetrize_kernel(T *W, int64_t ld, int64_t n) {
+    __shared__ T tile[32][33];
+    const int64_t I = blockIdx.x, J = blockIdx.y;
+    if (I > J) return;
+    const int64_t i0 = I * 32, j0 = J * 32;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int64_t r = j0 + threadIdx.x, c = i0 + k;  // element (r, c) = (j, i) of the lower tile
+        if (r < n && c < n) tile[threadIdx.x][k] = W[r + c * ld];
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int64_t i = i0 + threadIdx.x, j = j0 + k;
+        if (i < n && j < n && i < j) W[i + j * ld] = tile[k][threadIdx.x];
+    }
+}
+
+template <typename T>
+int symmetrize_launch(T *W, int64_t ld, int64_t n, cudaStream_t st) {
+    if (n == 0) return 0;
+    LaunchScope ls(K_LAYOUT, st);
+    symmetrize_kernel<T><<<tiles2d(n, n), dim3(32, 8), 0, st>>>(W, ld, n);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 #define LLA_INST(T)                                                                              \
     template int import_launch<T>(const T *, int64_t, int64_t, int64_t, int64_t, T *, int64_t,   \
                                   cudaStream_t);                                                 \
@@ -151,7 +179,8 @@ int eye_launch(T *W, int64_t ld, int64_t n, cudaStream_t st) {
     template int mask_launch<T>(T *, int64_t, int64_t, int64_t, int, cudaStream_t);              \
     template int is_triangular_launch<T>(const T *, int64_t, int64_t, int64_t, int, int *,       \
                                          cudaStream_t);                                          \
-    template int eye_launch<T>(T *, int64_t, int64_t, cudaStream_t);
+    template int eye_launch<T>(T *, int64_t, int64_t, cudaStream_t);                            \
+    template int symmetrize_launch<T>(T *, int64_t, int64_t, cudaStream_t);
 LLA_INST(double)
 LLA_INST(float)
 

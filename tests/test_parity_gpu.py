@@ -283,6 +283,26 @@ def test_fast_within_tolerance(fast, n, dtype):
         assert np.abs(L - lr).max() <= 10 * n * eps * np.abs(lr).max() * 10
 
 
+@pytest.mark.parametrize("n", [300, 1100, 2500])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_fast_invc_potri_panels(fast, n, dtype):
+    """FAST-mode InverseC: column panels of L^-1 solved only below their first
+    row, the upper part mirrored (symmetric by construction); accuracy of the
+    FP64 path: ||A inv - I|| within kappa * n * eps."""
+    lla = fast
+    eps = EPS[dtype]
+    rng = np.random.default_rng(200 + n)
+    a = cases.spd_gram(rng, n).astype(dtype)
+    inv = lla.invc(a.copy())
+    assert np.array_equal(inv, inv.T)
+    a_d, inv_d = a.astype(np.float64), inv.astype(np.float64)
+    kappa = np.linalg.cond(a_d)
+    resid = np.abs(a_d @ inv_d - np.eye(n)).max()
+    assert resid <= 10 * n * eps * kappa, (resid, kappa)
+    ref = np.linalg.inv(a_d)
+    assert np.abs(inv_d - ref).max() <= 10 * n * eps * kappa * np.abs(ref).max()
+
+
 def test_device_api_matches_host_api(gpu_lla):
     torch = pytest.importorskip("torch")
     lla = gpu_lla
