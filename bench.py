@@ -21,6 +21,7 @@ ranks divided by the slowest rank's time.
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -75,6 +76,25 @@ def cpu_rate(n_sample, m, workers, seed=1):
         dt = max(dts)
     scale = flops_solve(n_sample, m) / flops_solve(N_DEFAULT, NRHS_DEFAULT)
     return rate_sample * scale, dt
+
+
+def run_cpu_sweep(args):
+    """The oracle (one core) timed directly at n = 512 .. 4096, 64 RHS (and the
+    n=512, 1-RHS single-matrix workload): the CPU side of the scaling table."""
+    from oracle import oracle as ora
+    ora.lib()
+    rows = []
+    for n, m in [(512, 1), (512, 64), (1024, 64), (2048, 64), (4096, 64)]:
+        dt = _cpu_sample((n, m, 7))
+        rows.append({"n": n, "nrhs": m, "seconds": dt, "solves_per_s": 1.0 / dt,
+                     "gflops": flops_solve(n, m) / dt / 1e9})
+    # n^3 fit of the largest timed size, for the sizes not timed directly
+    big = rows[-1]
+    extrap = {str(n): big["seconds"] * flops_solve(n, NRHS_DEFAULT) / flops_solve(big["n"], 64)
+              for n in (8192, 16384)}
+    print(json.dumps({"workload": "cpu-sweep", "impl": "oracle (1 core, -O2 -ffp-contract=off)",
+                      "cores": 1, "rows": rows, "extrapolated_seconds_by_flops": extrap,
+                      "cpu": platform.processor() or platform.machine()}))
 
 
 def run_reference(args):
@@ -199,7 +219,7 @@ def backward_error(torch, A, X, B):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
@@ -214,13 +234,17 @@ def main():
     ap.add_argument("--residual", default="slices", choices=["fp64", "slices"],
                     help="refinement residual of the headline: FP64 MMA pipe, or exact BF16 slices")
     ap.add_argument("--no-alt", action="store_true", help="skip timing the other residual method")
-    ap.add_argument("--workload", default="single", choices=["single", "batch", "serve", "sweep"],
+    ap.add_argument("--workload", default="single",
+                    choices=["single", "batch", "serve", "sweep", "cpu-sweep"],
                     help="single: the n=16384 system (the headline); batch: 10,000 uneven small systems")
     ap.add_argument("--batch-count", type=int, default=10000)
     ap.add_argument("--batch-dtype", default="f64", choices=["f64", "f32"])
     ap.add_argument("--serve-requests", type=int, default=400)
     ap.add_argument("--serve-rates", default="25,50,100", help="Poisson arrival rates (requests/s)")
     args = ap.parse_args()
+    if args.workload == "cpu-sweep":
+        run_cpu_sweep(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return
@@ -302,17 +326,17 @@ def main():
         l0 = lla.kernel_launches()
         if profile:
             lla.profile_start()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(k + 1)]
         with Clocks(local) as clk:
-            e0.record(stream)
-            for _ in range(k):
+            ev[0].record(stream)
+            for i in range(k):
                 step()
-            e1.record(stream)
+                ev[i + 1].record(stream)  # per-solve latency (the steps run back to back)
             torch.cuda.synchronize()
         prof = lla.profile_stop() if profile else None
         launches = lla.kernel_launches() - l0
-        ms = e0.elapsed_time(e1)
+        ms = ev[0].elapsed_time(ev[k])
+        timed.per_step = [ev[i].elapsed_time(ev[i + 1]) for i in range(k)]
         if dist:
             t = torch.tensor([ms], device=dev)
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -325,6 +349,10 @@ def main():
     plain_sps = world * k_plain / (ms_plain / 1e3)
     reports.clear()
     ms_mixed, launches, prof, clocks = timed(mixed_step, args.steps, args.warmup, profile=True)
+    lat = sorted(timed.per_step)
+    latency = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+               "max_ms": lat[-1], "samples": len(lat),
+               "note": "per-solve CUDA-event durations of the timed steps (device-resident A, B)"}
     timed_reports = reports[-args.steps:]
     mixed_sps = world * args.steps / (ms_mixed / 1e3)
     assert all(r["backward_error"] <= BE_TARGET for r in timed_reports), timed_reports
@@ -431,6 +459,7 @@ def main():
                        "l2": "inputs larger than L2 (A = %.2f GB)" % (n * n * 8 / 1e9),
                        "parallelism": "replicas" if world > 1 else "single"},
             "backward_error": max(r["backward_error"] for r in timed_reports),
+            "latency": latency,
             "refinement": {"iterations": rep["iterations"], "backward_error0": rep["backward_error0"],
                            "fell_back": sum(r["fell_back"] for r in timed_reports),
                            "ms_factor": rep["ms_factor"], "ms_refine": rep["ms_refine"],
