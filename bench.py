@@ -579,7 +579,7 @@ def run_batch(args):
                      "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp64_peak if fp64_peak > 0 else None,
                      "peak_source": "measured live (FP64 tensor pipe / FFMA loop on all SMs)"},
-        "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches // (args.warmup + args.steps),
+        "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches * args.steps // (args.warmup + args.steps),
         "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
     }
     print(json.dumps(out))

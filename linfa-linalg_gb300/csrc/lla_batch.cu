@@ -497,9 +497,11 @@ int lla_batch_posv_graph(lla_batch_plan *p, void *dA, void *dB, int32_t *d_info,
         cudaGraph_t g = nullptr;
         e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
+            prof_capturing() = true;
             const cudaError_t le = p->dtype == 8
                                        ? batch_launch<double>(p, (double *)dA, (double *)dB, d_info, cap)
                                        : batch_launch<float>(p, (float *)dA, (float *)dB, d_info, cap);
+            prof_capturing() = false;
             e = cudaStreamEndCapture(cap, &g);
             if (le != cudaSuccess) e = le;
         }
@@ -512,7 +514,11 @@ int lla_batch_posv_graph(lla_batch_plan *p, void *dA, void *dB, int32_t *d_info,
         p->g_info = d_info;
         p->g_stream = st;
     }
-    e = cudaGraphLaunch(p->gexec, st);
+    {
+        // one kernel per replay (plus the counter reset): counted and timed like a launch
+        LaunchScope ls(K_BATCH, st, p->flops);
+        e = cudaGraphLaunch(p->gexec, st);
+    }
     return e == cudaSuccess ? LLA_OK : lla__set_cuda_error(err, e);
 }
 

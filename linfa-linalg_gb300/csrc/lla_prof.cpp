@@ -35,6 +35,10 @@ static double g_ms[K_COUNT], g_work[K_COUNT];
 static int64_t g_count[K_COUNT];
 
 void prof_note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+bool &prof_capturing() {
+    static thread_local bool capturing = false;
+    return capturing;
+}
 bool prof_on() { return g_on.load(std::memory_order_relaxed); }
 
 static cudaEvent_t take_event() {

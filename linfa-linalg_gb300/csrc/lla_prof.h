@@ -39,6 +39,9 @@ const char *kernel_name(int id);
 
 void prof_note_launch();
 bool prof_on();
+// While a thread captures a CUDA graph its launches are not counted or timed
+// (the graph's replays are, where they are launched).
+bool &prof_capturing();
 // Returns a slot index (or -1 when profiling is off) after recording the start event.
 int prof_begin(int kid, cudaStream_t st, double work);
 void prof_end(int slot, cudaStream_t st);
@@ -47,6 +50,10 @@ struct LaunchScope {
     int slot;
     cudaStream_t st;
     LaunchScope(int kid, cudaStream_t s, double work = 0.0) : st(s) {
+        if (prof_capturing()) {
+            slot = -1;
+            return;
+        }
         prof_note_launch();
         slot = prof_on() ? prof_begin(kid, s, work) : -1;
     }
