@@ -205,7 +205,7 @@ constexpr size_t kPnSmem = sizeof(float) * (kLpNb * kPnXd + kLpNb * kPnLd + 4 * 
 template <typename H>
 __global__ void __launch_bounds__(256) lowp_panel_kernel(float *L, int64_t ld, int64_t n, int64_t p,
                                                          const float *__restrict__ Wd, H *planes,
-                                                         int64_t plane_stride, int kpad, int terms,
+                                                         int64_t plane_stride, int64_t ldp, int koff, int terms,
                                                          const int64_t *info) {
     extern __shared__ __align__(16) float sm[];
     float *sXT = sm;                         // sXT[k * kPnXd + r] = row r, column k of the tile
@@ -291,8 +291,9 @@ __global__ void __launch_bounds__(256) lowp_panel_kernel(float *L, int64_t ld, i
         const int64_t j = row0 + r;
         if (j < n) L[j + (p + k) * ld] = sXT[k * kPnXd + r];
     }
-    // operand planes, 16-byte stores of 8 halves: thread (row, 8-column group)
-    for (int e = tid; e < kPnRows * (kpad / 8); e += 256) {
+    // operand planes (row j at j * ldp, columns koff ..), 16-byte stores of 8
+    // halves: thread (row, 8-column group)
+    for (int e = tid; e < kPnRows * (kLpNb / 8); e += 256) {
         const int r = e % kPnRows, k0 = (e / kPnRows) * 8;
         const int64_t j = row0 + r;
         if (j >= n) continue;
@@ -310,17 +311,12 @@ __global__ void __launch_bounds__(256) lowp_panel_kernel(float *L, int64_t ld, i
         }
 #pragma unroll
         for (int t = 0; t < 3; ++t)
-            if (t < terms) *(uint4 *)(planes + t * plane_stride + (j - q) * kpad + k0) = *(const uint4 *)h[t];
+            if (t < terms) *(uint4 *)(planes + t * plane_stride + j * ldp + koff + k0) = *(const uint4 *)h[t];
     }
 }
 
 // ---------------------------------------------------------------------------
 // host loop
-
-static int64_t tri_tiles128(int64_t m) {
-    const int64_t t = ceil_div(m, 128);
-    return t * (t + 1) / 2;
-}
 
 int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &opts, int64_t *info,
                        float *diag0, double *min_ratio, Ctx *c, cudaStream_t st) {
@@ -343,8 +339,10 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
         const int pa[6] = {0, 1, 2, 0, 1, 0}, pb[6] = {2, 1, 0, 1, 0, 0};
         for (int i = 0; i < 6; ++i) pairs.pa[i] = pa[i], pairs.pb[i] = pb[i];
     }
-    const int kpad = kLpNb;
-    const int64_t plane_stride = n * kpad;  // elements per plane
+    // Operand planes indexed by absolute row (row j at j * ldp): two 128-column
+    // halves, one per panel of a pair (see the loop below).
+    const int64_t ldp = 2 * kLpNb;
+    const int64_t plane_stride = n * ldp;  // elements per plane
     if (c->mixed.opA.ensure(sizeof(uint16_t) * plane_stride * terms) != cudaSuccess) return -1;
     void *planes = c->mixed.opA.p;
     int *err_word = nullptr;
@@ -364,29 +362,53 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
                              (int)smem_panel) != cudaSuccess ||
         tc_update_prepare() != 0)
         return -1;
-    for (int64_t p = 0; p < n; p += kLpNb) {
+    const size_t esz = sizeof(uint16_t);
+    auto diag = [&](int64_t p, int b) {
+        LaunchScope ls(K_MIXED_DIAG, st, (double)b * b * b / 3.0);
+        lowp_diag_kernel<<<1, 1024, smem_l11, st>>>(L, ld, p, b, info, min_ratio, Wd);
+    };
+    // L21 and its planes for rows [p + 128, n), written to plane half `half`
+    auto panel = [&](int64_t p, int half) {
+        const int64_t rest = n - p - kLpNb;
+        LaunchScope ls(K_MIXED_PANEL, st, (double)rest * kLpNb * kLpNb);
+        if (fp16)
+            lowp_panel_kernel<__half><<<(unsigned)ceil_div(rest, kPnRows), 256, smem_panel, st>>>(
+                L, ld, n, p, Wd, (__half *)planes, plane_stride, ldp, half * kLpNb, terms, info);
+        else
+            lowp_panel_kernel<__nv_bfloat16><<<(unsigned)ceil_div(rest, kPnRows), 256, smem_panel, st>>>(
+                L, ld, n, p, Wd, (__nv_bfloat16 *)planes, plane_stride, ldp, half * kLpNb, terms, info);
+    };
+    // A22 -= sum of the products of K columns of the planes, rows [q, n)
+    auto update = [&](int64_t q, int kext, bool narrow) -> int {
+        const int64_t rows = n - q;
+        const int64_t cols = narrow ? std::min<int64_t>(kLpNb, rows) : rows;
+        // algorithmic work: the lower trailing entries x kext multiply-adds x 2
+        LaunchScope ls(K_MIXED_UPDATE, st,
+                       narrow ? (double)rows * cols * kext * 2.0 - (double)cols * (cols - 1) * kext
+                              : (double)rows * (rows + 1) * kext);
+        return tc_update_launch(L, ld, q, n, (char *)planes + (size_t)q * ldp * esz, plane_stride, ldp, rows,
+                                kext, terms, fp16, pairs, info, err_word, narrow, st);
+    };
+    // Panels in pairs: after panel p only the next panel's 128 columns are
+    // updated (narrow); panel p + 128 is factored, and then both panels'
+    // products are subtracted from the rest in one pass with K = 256, so the
+    // FP32 trailing matrix is read and written once per pair of panels.
+    for (int64_t p = 0; p < n;) {
         const int b = (int)std::min<int64_t>(kLpNb, n - p);
-        {
-            LaunchScope ls(K_MIXED_DIAG, st, (double)b * b * b / 3.0);
-            lowp_diag_kernel<<<1, 1024, smem_l11, st>>>(L, ld, p, b, info, min_ratio, Wd);
-        }
+        diag(p, b);
         const int64_t rest = n - p - b;
-        if (rest <= 0) break;
-        {
-            LaunchScope ls(K_MIXED_PANEL, st, (double)rest * b * b);
-            // b == 128 whenever rows remain below the block
-            if (fp16)
-                lowp_panel_kernel<__half><<<(unsigned)ceil_div(rest, kPnRows), 256, smem_panel, st>>>(
-                    L, ld, n, p, Wd, (__half *)planes, plane_stride, kpad, terms, info);
-            else
-                lowp_panel_kernel<__nv_bfloat16><<<(unsigned)ceil_div(rest, kPnRows), 256, smem_panel, st>>>(
-                    L, ld, n, p, Wd, (__nv_bfloat16 *)planes, plane_stride, kpad, terms, info);
+        if (rest <= 0) break;  // b == 128 whenever rows remain below the block
+        panel(p, 0);
+        if (rest > kLpNb) {
+            if (update(p + kLpNb, kLpNb, true) != 0) return -1;
+            diag(p + kLpNb, kLpNb);
+            panel(p + kLpNb, 1);
+            if (update(p + 2 * kLpNb, 2 * kLpNb, false) != 0) return -1;
+            p += 2 * kLpNb;
+        } else {
+            if (update(p + kLpNb, kLpNb, false) != 0) return -1;
+            p += kLpNb;
         }
-        // algorithmic work of the update: rest(rest+1)/2 entries x b multiply-adds x 2
-        LaunchScope ls(K_MIXED_UPDATE, st, (double)rest * (rest + 1) * b);
-        if (tc_update_launch(L, ld, p + b, n, planes, plane_stride, rest, kpad, terms, fp16, pairs,
-                             info, err_word, tri_tiles128(rest), st) != 0)
-            return -1;
     }
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -18,14 +18,16 @@ struct TcPairs {
 // descriptors); 0 on success.
 int tc_update_prepare();
 
-// C[q + I*128 + r, q + J*128 + c] -= sum over pairs of planes[a][I*128 + r, :] .
-// planes[b][J*128 + c, :] for the lower tiles I >= J of the rows x rows
-// trailing matrix (FP32, column-major, leading dimension ld, global order n).
-// planes: `terms` planes of rows x kpad BF16 (or FP16) values, plane_stride
-// elements apart, row-major.  Skips all work when *info >= 0; bounded waits
-// record LLA_ERR_TIMEOUT in *err_word.
+// C[q + I*128 + r, q + J*128 + c] -= sum over pairs of planes[a][I*128 + r, :kext] .
+// planes[b][J*128 + c, :kext] for the lower tiles I >= J of the rows x rows
+// trailing matrix (FP32, column-major, leading dimension ld, global order n),
+// or, when narrow, for the tiles of its first tile column only (J = 0).
+// planes: `terms` planes of rows x ldp BF16 (or FP16) values, plane_stride
+// elements apart, row-major, 16-byte aligned; kext (a multiple of 64, <= ldp)
+// columns of each row are the K extent.  Skips all work when *info >= 0;
+// bounded waits record LLA_ERR_TIMEOUT in *err_word.
 int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, int64_t plane_stride,
-                     int64_t rows, int kpad, int terms, bool fp16, const TcPairs &pairs,
-                     const int64_t *info, int *err_word, int64_t tiles, cudaStream_t st);
+                     int64_t ldp, int64_t rows, int kext, int terms, bool fp16, const TcPairs &pairs,
+                     const int64_t *info, int *err_word, bool narrow, cudaStream_t st);
 
 }  // namespace lla

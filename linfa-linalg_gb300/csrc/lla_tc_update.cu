@@ -46,6 +46,17 @@ constexpr uint32_t kTcCols = 128;  // tensor-memory columns of one FP32 128 x 12
 // wants), double-buffered: all 512 columns.
 constexpr uint32_t kTcAlloc = 4 * kTcCols;
 
+__device__ __forceinline__ void tc_tri_tile(int64_t t, int64_t &I, int64_t &J);
+// Tile t of a launch: the lower tiles (I >= J) in row-major order, or, for a
+// narrow update, the tiles (t, 0) of the first tile column only.
+__device__ __forceinline__ void tc_tile(int64_t t, int narrow, int64_t &I, int64_t &J) {
+    if (narrow) {
+        I = t;
+        J = 0;
+    } else {
+        tc_tri_tile(t, I, J);
+    }
+}
 __device__ __forceinline__ void tc_tri_tile(int64_t t, int64_t &I, int64_t &J) {
     int64_t i = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
     while ((i + 1) * (i + 2) / 2 <= t) ++i;
@@ -76,7 +87,7 @@ __device__ __forceinline__ constexpr int tc_pb(int terms, int i) {
 template <int TERMS>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     const __grid_constant__ CUtensorMap tmap, float *C, int64_t ld, int64_t q, int64_t n, int kchunks,
-    uint32_t idesc, int64_t ntiles, const int64_t *info, int *err_word) {
+    uint32_t idesc, int64_t ntiles, int narrow, const int64_t *info, int *err_word) {
     constexpr int terms = TERMS, NP = tc_npairs(TERMS);
     extern __shared__ uint8_t smem_raw[];
     __shared__ int s_abort, s_skip;
@@ -124,7 +135,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
             int64_t g = 0;
             for (int64_t t = blockIdx.x; t < ntiles && !*(volatile int *)&s_abort; t += gridDim.x) {
                 int64_t I, J;
-                tc_tri_tile(t, I, J);
+                tc_tile(t, narrow, I, J);
                 for (int kc = 0; kc < kchunks; ++kc, ++g) {
                     const int s = (int)(g % S);
                     const int64_t round = g / S;
@@ -144,7 +155,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
             int64_t g = 0, lt = 0;
             for (int64_t t = blockIdx.x; t < ntiles && !*(volatile int *)&s_abort; t += gridDim.x, ++lt) {
                 int64_t I, J;
-                tc_tri_tile(t, I, J);
+                tc_tile(t, narrow, I, J);
                 const int a = (int)(lt & 1);
                 const int64_t use = lt >> 1;
                 if (use > 0 && !mbar_wait(tempty0 + 8 * a, (uint32_t)((use - 1) & 1), err_word)) {
@@ -190,7 +201,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
             const int a = (int)(lt & 1);
             const int64_t use = lt >> 1;
             int64_t I, J;
-            tc_tri_tile(t, I, J);
+            tc_tile(t, narrow, I, J);
             const int64_t grow = q + I * kTcM + r;
             const int64_t gcol0 = q + J * kTcN + half * 64;
             const int64_t cmax = n - gcol0;  // columns left in the matrix
@@ -279,12 +290,16 @@ int tc_update_prepare() {
 }
 
 int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, int64_t plane_stride,
-                     int64_t rows, int kpad, int terms, bool fp16, const TcPairs &pairs,
-                     const int64_t *info, int *err_word, int64_t tiles, cudaStream_t st) {
-    if (!g_encode || rows <= 0 || kpad % kTcK != 0 || terms < 1 || terms > 3) return -1;
+                     int64_t ldp, int64_t rows, int kext, int terms, bool fp16, const TcPairs &pairs,
+                     const int64_t *info, int *err_word, bool narrow, cudaStream_t st) {
+    if (!g_encode || rows <= 0 || kext % kTcK != 0 || kext > ldp || (ldp * 2) % 16 != 0 || terms < 1 ||
+        terms > 3 || (reinterpret_cast<uintptr_t>(planes) & 15) != 0)
+        return -1;
+    const int64_t tr = (rows + kTcM - 1) / kTcM;
+    const int64_t tiles = narrow ? tr : tr * (tr + 1) / 2;
     CUtensorMap map;
-    const cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rows, (cuuint64_t)terms};
-    const cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)plane_stride * 2};
+    const cuuint64_t dims[3] = {(cuuint64_t)kext, (cuuint64_t)rows, (cuuint64_t)terms};
+    const cuuint64_t strides[2] = {(cuuint64_t)ldp * 2, (cuuint64_t)plane_stride * 2};
     const cuuint32_t box[3] = {(cuuint32_t)kTcK, (cuuint32_t)kTcM, (cuuint32_t)terms};  // every term plane
     const cuuint32_t estr[3] = {1, 1, 1};
     const CUresult r =
@@ -311,7 +326,8 @@ int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, i
         pairs.pb[pairs.n - 1] != 0)
         return -1;
     auto kern = terms == 1 ? tc_update_kernel<1> : (terms == 2 ? tc_update_kernel<2> : tc_update_kernel<3>);
-    kern<<<grid, kTcThreads, kTcSmem, st>>>(map, C, ld, q, n, kpad / kTcK, idesc, tiles, info, err_word);
+    kern<<<grid, kTcThreads, kTcSmem, st>>>(map, C, ld, q, n, kext / kTcK, idesc, tiles, narrow ? 1 : 0, info,
+                                            err_word);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
