@@ -162,9 +162,44 @@ __device__ __forceinline__ unsigned long long iv_settle_word(unsigned long long 
 constexpr int kIvCols = 16;   // right-hand-side columns per CTA
 constexpr int kIvLd = 68;     // shared row stride of a staged 64 x 64 tile (floats; 16-byte rows)
 constexpr int kIvStages = 3;  // coupling tiles in flight per CTA
+constexpr int64_t kIvHelperMin = 16;  // first position whose coupling terms are split with a helper
 constexpr int kIvYd = kIvNb + 2;  // words per staged column (padded: 528-byte columns)
 constexpr size_t kIvSmem = sizeof(float) * ((size_t)kIvStages * kIvNb * kIvLd + 2ull * kIvStages * kIvCols * kIvYd +
                                             2ull * kIvNb * kIvCols);
+
+// Work items in ticket order.  Group g (g = 0 .. R-1) holds the owners of
+// processing position g (one per column chunk), then the helpers of positions
+// p = 2g+2 and 2g+3 (those with hmin <= p < R): a helper sums the coupling
+// terms q < p/2 of position p, which are all solved once position p/2 - 1 is,
+// so every item waits only on items with smaller tickets.
+__host__ __device__ __forceinline__ int64_t iv_items_before(int64_t g, int64_t R, int64_t hmin, int nch) {
+    const int64_t top = (2 * g + 1 < R - 1 ? 2 * g + 1 : R - 1) - hmin + 1;  // helpers p in [hmin, 2g+1]
+    return (int64_t)nch * (g + (top > 0 ? top : 0));
+}
+__device__ __forceinline__ void iv_decode(int64_t t, int64_t R, int64_t hmin, int nch, bool &helper,
+                                          int64_t &pos, int &chunk) {
+    int64_t lo = 0, hi = R - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) / 2;
+        if (iv_items_before(mid, R, hmin, nch) <= t)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const int64_t idx = t - iv_items_before(lo, R, hmin, nch);
+    if (idx < nch) {
+        helper = false;
+        pos = lo;
+        chunk = (int)idx;
+        return;
+    }
+    helper = true;
+    const int64_t j = (idx - nch) / nch;
+    chunk = (int)((idx - nch) % nch);
+    int64_t p = 2 * lo + 2;
+    if (p < hmin) p = hmin;  // only 2g+3 can qualify then
+    pos = p + j;
+}
 
 // TRANS = false: L Y = B (blocks ascending); TRANS = true: L^T X = B (descending).
 // 256 threads.  The coupling tiles and the solved words of earlier blocks
@@ -178,7 +213,7 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
                                                           const float *__restrict__ Wall, int64_t n,
                                                           float *B, int64_t ldb, int64_t m, int nchunks,
                                                           unsigned long long *ll, int64_t ldl, unsigned epoch,
-                                                          int *counter, int *err_word) {
+                                                          int *counter, int *err_word, int64_t hmin) {
     constexpr int C = kIvCols, LPT = kIvTile / 256, NS = kIvStages;
     constexpr int YCH = kIvNb * C / 2 / 256;  // 16-byte (two-word) copies per thread per stage
     extern __shared__ __align__(16) float iv_smem[];
@@ -195,9 +230,12 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
     }
     __syncthreads();
     const int64_t R = (n + kIvNb - 1) / kIvNb;
-    const int64_t pb = s_ticket / nchunks;  // position in processing order
-    const int cc = s_ticket % nchunks;
+    bool helper;
+    int64_t pb;  // position in processing order
+    int cc;
+    iv_decode(s_ticket, R, hmin, nchunks, helper, pb, cc);
     const int64_t rb = TRANS ? R - 1 - pb : pb;
+    unsigned long long *pl = ll + R * kIvNb * m;  // helpers' partial sums, laid out like ll
     const int ta = tid % kIvNb, tb = tid / kIvNb;
     const int64_t grow = rb * kIvNb + ta;
     const int64_t col0 = (int64_t)cc * C;
@@ -209,7 +247,7 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int64_t row = rb * kIvNb + 4 * rg + i, col = col0 + bc;
-        acc[i] = (row < n && col < m) ? B[row + col * ldb] : 0.f;
+        acc[i] = (!helper && row < n && col < m) ? B[row + col * ldb] : 0.f;
     }
     // this block's inverse and coupling matrix (element (ta, tb + 4u) of each), needed only at the end
     float preW[LPT], preM[LPT];
@@ -222,13 +260,18 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
             preM[u] = Mr[u * 4 * kIvNb];
         }
     }
-    const int64_t nbulk = pb > 0 ? pb - 1 : 0;  // coupling terms before the neighbour's
+    // coupling terms of this item, positions q_lo .. q_lo + nbulk - 1: a helper
+    // takes q < pb/2, its owner the rest before the neighbour's
+    const bool has_helper = pb >= hmin;
+    const int64_t q_lo = (!helper && has_helper) ? pb / 2 : 0;
+    const int64_t nbulk = helper ? pb / 2 : (pb > 0 ? pb - 1 - q_lo : 0);
 
     // Stage s <- coupling tile and solved words of processing position pq.
     // Tile: 64 columns a of 64 contiguous rows b (non-trans: a = k, b = i;
     // trans: a = i, b = k), zero-filled past n.
-    auto issue = [&](int64_t pq, int s) {
-        if (pq < nbulk) {
+    auto issue = [&](int64_t pi, int s) {
+        if (pi < nbulk) {
+            const int64_t pq = q_lo + pi;
             const int64_t qb = TRANS ? R - 1 - pq : pq;
             const int64_t rowbase = (TRANS ? qb : rb) * kIvNb, colbase = (TRANS ? rb : qb) * kIvNb;
             if (al16) {
@@ -263,7 +306,8 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
     // are re-read from global memory until they carry this launch's tag, and
     // replaced in place (words past n or m are zero: never written, or
     // zero-filled by the copy).
-    auto settle_stage = [&](int64_t pq, int s) {
+    auto settle_stage = [&](int64_t pi, int s) {
+        const int64_t pq = q_lo + pi;
         const int64_t qb = TRANS ? R - 1 - pq : pq;
 #pragma unroll
         for (int j = 0; j < YCH; ++j) {
@@ -323,6 +367,25 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
     iv_wait<0>();
     __syncthreads();
     if (s_abort) return;
+    if (helper) {  // publish the partial sum (its coupling terms, negated) for the owner
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int64_t row = rb * kIvNb + 4 * rg + i, col = col0 + bc;
+            if (row < n && col < m) iv_st_word(pl + row + col * ldl, tag | (unsigned long long)__float_as_uint(acc[i]));
+        }
+        return;
+    }
+    if (has_helper) {  // add the helper's partial sum (bounded wait)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int64_t row = rb * kIvNb + 4 * rg + i, col = col0 + bc;
+            if (row < n && col < m) {
+                const unsigned long long *p = pl + row + col * ldl;
+                acc[i] += __uint_as_float(
+                    (unsigned)(iv_settle_word(iv_ld_word(p), p, tag, err_word, &s_abort) & 0xffffffffull));
+            }
+        }
+    }
 
     // 2. t = W_r acc (W_r^T acc when trans); the neighbour's words are read meanwhile
     unsigned long long wy[4];
@@ -396,7 +459,10 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
 
 size_t trsm_inv_ws_ints(int64_t, int64_t) { return 1; }
 
-size_t trsm_inv_stage_words(int64_t n, int64_t m) { return (size_t)((n + kIvNb - 1) / kIvNb) * kIvNb * (size_t)m; }
+// solved values, then the helpers' partial sums
+size_t trsm_inv_stage_words(int64_t n, int64_t m) {
+    return 2 * (size_t)((n + kIvNb - 1) / kIvNb) * kIvNb * (size_t)m;
+}
 
 size_t diag_inverse_floats(int64_t n) { return 3 * (size_t)((n + kIvNb - 1) / kIvNb) * kIvTile; }
 
@@ -426,8 +492,11 @@ int trsm_inv_launch(const float *L, int64_t ld, const float *W, int64_t n, float
     if (cudaMemsetAsync(ws, 0, sizeof(int), st) != cudaSuccess) return -1;
     // algorithmic work: n^2 m flops
     LaunchScope ls(K_MIXED_TRSM, st, (double)n * n * m);
-    kern<<<(unsigned)(R * nchunks), 256, kIvSmem, st>>>(L, ld, W, n, B, ldb, m, nchunks, stage, R * kIvNb, epoch,
-                                                       ws, err_word);
+    // positions from kIvHelperMin on get a helper for the first half of their coupling terms
+    const int64_t hmin = kIvHelperMin;
+    const int64_t items = iv_items_before(R, R, hmin, nchunks);  // every group
+    kern<<<(unsigned)items, 256, kIvSmem, st>>>(L, ld, W, n, B, ldb, m, nchunks, stage, R * kIvNb, epoch, ws,
+                                               err_word, hmin);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
