@@ -53,12 +53,13 @@ def test_refined_reaches_fp64_accuracy(gpu_lla, update, n, kappa):
     assert fe <= 10 * kappa * max(rep["backward_error"], 1e-15), fe  # forward <~ kappa * backward
 
 
-@pytest.mark.parametrize("m", [1, 20, 64, 97])
-def test_refined_many_right_hand_sides(gpu_lla, m):
-    """Column chunks of 16, 32 and 64 in the FP32 substitutions, ragged n."""
+@pytest.mark.parametrize("n,m", [(777, 1), (777, 20), (777, 64), (777, 97), (2111, 37), (4160, 64)])
+def test_refined_many_right_hand_sides(gpu_lla, n, m):
+    """Several 16-column chunks in the FP32 substitutions, ragged n; n >= 1024
+    (16 block rows) brings in the helper items that sum the first half of a late
+    block row's coupling terms."""
     lla = gpu_lla
-    rng = np.random.default_rng(m)
-    n = 777
+    rng = np.random.default_rng(m + n)
     a = qdq(rng, n, 1e5)
     b = rng.standard_normal((n, m))
     x = b.copy()
