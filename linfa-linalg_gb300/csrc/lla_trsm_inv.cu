@@ -165,7 +165,7 @@ constexpr int kIvStages = 3;  // coupling tiles in flight per CTA
 constexpr int64_t kIvHelperMin = 16;  // first position whose coupling terms are split with a helper
 constexpr int kIvYd = kIvNb + 2;  // words per staged column (padded: 528-byte columns)
 constexpr size_t kIvSmem = sizeof(float) * ((size_t)kIvStages * kIvNb * kIvLd + 2ull * kIvStages * kIvCols * kIvYd +
-                                            2ull * kIvNb * kIvCols);
+                                            2ull * kIvNb * kIvCols + 2ull * kIvCols * kIvLd);
 
 // Work items in ticket order.  Group g (g = 0 .. R-1) holds the owners of
 // processing position g (one per column chunk), then the helpers of positions
@@ -203,11 +203,15 @@ __device__ __forceinline__ void iv_decode(int64_t t, int64_t R, int64_t hmin, in
 
 // TRANS = false: L Y = B (blocks ascending); TRANS = true: L^T X = B (descending).
 // 256 threads.  The coupling tiles and the solved words of earlier blocks
-// stream through a kIvStages-deep cp.async ring; for their products thread
-// (c = tid % 16, rg = tid / 16) owns column c and rows 4 rg .. 4 rg + 3 and
-// reads the words where they landed (validated in place).  For the block's
-// own products (inverse, neighbour) thread (ta = tid % 64, tb = tid / 64)
-// owns row ta and columns 4 tb .. 4 tb + 3.
+// stream through a kIvStages-deep cp.async ring.  Each thread validates the
+// words it copied and stores their values into a float copy of the block
+// (sYf[c][k], two buffers).  The coupling products are split over K: warp
+// pair kg sums k in [16 kg, 16 kg + 16) into a 4 x 4 register tile (columns
+// cg + 4 jj; rows 4 rq + j, or rq + 16 j when trans, so that the shared loads
+// are free of bank conflicts), and the four partial sums are added in kg
+// order at the end, into thread (c = tid % 16, rg = tid / 16)'s column c,
+// rows 4 rg .. 4 rg + 3.  For the block's own products (inverse, neighbour)
+// thread (ta = tid % 64, tb = tid / 64) owns row ta and columns 4 tb .. 4 tb + 3.
 template <bool TRANS>
 __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restrict__ L, int64_t ld,
                                                           const float *__restrict__ Wall, int64_t n,
@@ -222,6 +226,9 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
     unsigned long long(*sY)[C][kIvYd] =
         reinterpret_cast<unsigned long long(*)[C][kIvYd]>(iv_smem + NS * kIvNb * kIvLd);
     float(*sV)[kIvNb][C] = reinterpret_cast<float(*)[kIvNb][C]>(iv_smem + NS * kIvNb * kIvLd + 2 * NS * C * kIvYd);
+    float(*sYf)[C][kIvLd] =
+        reinterpret_cast<float(*)[C][kIvLd]>(iv_smem + NS * kIvNb * kIvLd + 2 * NS * C * kIvYd + 2 * kIvNb * C);
+    static_assert(NS >= 3, "the partial sums reuse stage 2");
     __shared__ int s_ticket, s_abort;
     const int tid = threadIdx.x;
     if (tid == 0) {
@@ -303,69 +310,97 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
         iv_commit();
     };
     // The words this thread copied into stage s that are not yet published
-    // are re-read from global memory until they carry this launch's tag, and
-    // replaced in place (words past n or m are zero: never written, or
+    // are re-read from global memory until they carry this launch's tag; their
+    // values go to sYf[buf] (words past n or m are zero: never written, or
     // zero-filled by the copy).
-    auto settle_stage = [&](int64_t pi, int s) {
+    auto settle_stage = [&](int64_t pi, int s, int buf) {
         const int64_t pq = q_lo + pi;
         const int64_t qb = TRANS ? R - 1 - pq : pq;
 #pragma unroll
         for (int j = 0; j < YCH; ++j) {
             const int e = tid + 256 * j, c = e >> 5, kp = e & 31;
+            float v[2];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const int k = 2 * kp + h;
                 const int64_t gk = qb * kIvNb + k, col = col0 + c;
-                const unsigned long long w0 = sY[s][c][k];
+                unsigned long long w0 = sY[s][c][k];
                 if (gk < n && col < m && (w0 & 0xffffffff00000000ull) != tag)
-                    sY[s][c][k] = iv_settle_word(w0, ll + gk + col * ldl, tag, err_word, &s_abort);
+                    w0 = iv_settle_word(w0, ll + gk + col * ldl, tag, err_word, &s_abort);
+                v[h] = __uint_as_float((unsigned)w0);
             }
+            *reinterpret_cast<float2 *>(&sYf[buf][c][2 * kp]) = make_float2(v[0], v[1]);
         }
     };
 
     // 1. every coupling term but the neighbour's (blocks solved well before this one)
+    const int kg = tid >> 6, cg = tid & 3, rq = (tid & 63) >> 2;
+    float part[4][4];  // part[j][jj]: row (trans ? rq + 16 j : 4 rq + j), column cg + 4 jj
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) part[j][jj] = 0.f;
 #pragma unroll
     for (int s = 0; s < NS - 1; ++s) issue(s, s);
     for (int64_t pq = 0; pq < nbulk; ++pq) {
-        const int s = (int)(pq % NS);
+        const int s = (int)(pq % NS), buf = (int)(pq & 1);
         iv_wait<NS - 2>();
-        settle_stage(pq, s);
+        settle_stage(pq, s, buf);
         __syncthreads();
         if (s_abort) break;
         issue(pq + NS - 1, (int)((pq + NS - 1) % NS));
-        const unsigned long long *yc = sY[s][bc];  // column bc of the solved block
-        if (!TRANS) {  // coefficient of x_k in row i: sT[s][k][i]
-#pragma unroll 8
-            for (int k = 0; k < kIvNb; ++k) {
-                const float4 l4 = *reinterpret_cast<const float4 *>(&sT[s][k][4 * rg]);
-                const float x = __uint_as_float((unsigned)yc[k]);
-                acc[0] = fmaf(-l4.x, x, acc[0]);
-                acc[1] = fmaf(-l4.y, x, acc[1]);
-                acc[2] = fmaf(-l4.z, x, acc[2]);
-                acc[3] = fmaf(-l4.w, x, acc[3]);
-            }
-        } else {  // coefficient of x_k in row i: sT[s][i][k]
-#pragma unroll 2
-            for (int k4 = 0; k4 < kIvNb / 4; ++k4) {
-                const ulonglong2 w01 = *reinterpret_cast<const ulonglong2 *>(&yc[4 * k4]);
-                const ulonglong2 w23 = *reinterpret_cast<const ulonglong2 *>(&yc[4 * k4 + 2]);
-                const float x0 = __uint_as_float((unsigned)w01.x), x1 = __uint_as_float((unsigned)w01.y);
-                const float x2 = __uint_as_float((unsigned)w23.x), x3 = __uint_as_float((unsigned)w23.y);
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const float4 l4 = *reinterpret_cast<const float4 *>(&sT[s][4 * rg + i][4 * k4]);
-                    float a = acc[i];
-                    a = fmaf(-l4.x, x0, a);
-                    a = fmaf(-l4.y, x1, a);
-                    a = fmaf(-l4.z, x2, a);
-                    a = fmaf(-l4.w, x3, a);
-                    acc[i] = a;
+        for (int k4 = 0; k4 < 4; ++k4) {
+            const int k0 = 16 * kg + 4 * k4;
+            float4 x[4];
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) x[jj] = *reinterpret_cast<const float4 *>(&sYf[buf][cg + 4 * jj][k0]);
+            if (!TRANS) {  // coefficient of x_k in row i: sT[s][k][i]
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) {
+                    const float4 l4 = *reinterpret_cast<const float4 *>(&sT[s][k0 + kk][4 * rq]);
+#pragma unroll
+                    for (int jj = 0; jj < 4; ++jj) {
+                        const float xv = kk == 0 ? x[jj].x : kk == 1 ? x[jj].y : kk == 2 ? x[jj].z : x[jj].w;
+                        part[0][jj] = fmaf(-l4.x, xv, part[0][jj]);
+                        part[1][jj] = fmaf(-l4.y, xv, part[1][jj]);
+                        part[2][jj] = fmaf(-l4.z, xv, part[2][jj]);
+                        part[3][jj] = fmaf(-l4.w, xv, part[3][jj]);
+                    }
+                }
+            } else {  // coefficient of x_k in row i: sT[s][i][k]
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const float4 l4 = *reinterpret_cast<const float4 *>(&sT[s][rq + 16 * j][k0]);
+#pragma unroll
+                    for (int jj = 0; jj < 4; ++jj) {
+                        float a = part[j][jj];
+                        a = fmaf(-l4.x, x[jj].x, a);
+                        a = fmaf(-l4.y, x[jj].y, a);
+                        a = fmaf(-l4.z, x[jj].z, a);
+                        a = fmaf(-l4.w, x[jj].w, a);
+                        part[j][jj] = a;
+                    }
                 }
             }
         }
     }
     iv_wait<0>();
     __syncthreads();
+    {  // add the four K-quarters' partial sums in order (stage 2 is free now)
+        float *red = &sT[2][0][0];  // red[kg][row][col], row stride 17
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj)
+                red[kg * kIvNb * 17 + (TRANS ? rq + 16 * j : 4 * rq + j) * 17 + cg + 4 * jj] = part[j][jj];
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float *r = red + (4 * rg + i) * 17 + bc;
+            acc[i] = (((acc[i] + r[0]) + r[kIvNb * 17]) + r[2 * kIvNb * 17]) + r[3 * kIvNb * 17];
+        }
+    }
     if (s_abort) return;
     if (helper) {  // publish the partial sum (its coupling terms, negated) for the owner
 #pragma unroll
