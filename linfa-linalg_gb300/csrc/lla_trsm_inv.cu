@@ -140,23 +140,29 @@ __device__ __forceinline__ void iv_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// Bounded re-read of one hand-off word until it carries this launch's tag.
-__device__ __forceinline__ unsigned long long iv_settle_word(unsigned long long w, const unsigned long long *p,
-                                                             unsigned long long tag, int *err_word,
-                                                             int *abort_flag) {
+// Bounded re-read of up to four hand-off words (p[u] == nullptr: none)
+// until each carries this launch's tag; the words are re-read together, so a
+// hand-off costs one memory round trip however many of them were late.
+__device__ __forceinline__ void iv_settle4(unsigned long long (&w)[4], const unsigned long long *const (&p)[4],
+                                           unsigned long long tag, int *err_word, int *abort_flag) {
     long long spins = 0;
-    while ((w & 0xffffffff00000000ull) != tag) {
+    for (;;) {
+        bool done = true;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) done &= (p[u] == nullptr) || ((w[u] & 0xffffffff00000000ull) == tag);
+        if (done) return;
         if (((++spins) & 63) == 0) {
             if (*(volatile int *)err_word != 0 || spins > kSpinLimit) {
                 atomicCAS(err_word, 0, (int)LLA_ERR_TIMEOUT);
                 *abort_flag = 1;
-                break;
+                return;
             }
             __nanosleep(32);
         }
-        w = iv_ld_word(p);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (p[u] != nullptr && (w[u] & 0xffffffff00000000ull) != tag) w[u] = iv_ld_word(p[u]);
     }
-    return w;
 }
 
 constexpr int kIvCols = 16;   // right-hand-side columns per CTA
@@ -313,23 +319,29 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
     // are re-read from global memory until they carry this launch's tag; their
     // values go to sYf[buf] (words past n or m are zero: never written, or
     // zero-filled by the copy).
+    static_assert(YCH == 2, "a thread settles the four words of its two copies together");
     auto settle_stage = [&](int64_t pi, int s, int buf) {
         const int64_t pq = q_lo + pi;
         const int64_t qb = TRANS ? R - 1 - pq : pq;
+        unsigned long long w[4];
+        const unsigned long long *p[4];
 #pragma unroll
         for (int j = 0; j < YCH; ++j) {
             const int e = tid + 256 * j, c = e >> 5, kp = e & 31;
-            float v[2];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const int k = 2 * kp + h;
                 const int64_t gk = qb * kIvNb + k, col = col0 + c;
-                unsigned long long w0 = sY[s][c][k];
-                if (gk < n && col < m && (w0 & 0xffffffff00000000ull) != tag)
-                    w0 = iv_settle_word(w0, ll + gk + col * ldl, tag, err_word, &s_abort);
-                v[h] = __uint_as_float((unsigned)w0);
+                w[2 * j + h] = sY[s][c][k];
+                p[2 * j + h] = (gk < n && col < m) ? ll + gk + col * ldl : nullptr;
             }
-            *reinterpret_cast<float2 *>(&sYf[buf][c][2 * kp]) = make_float2(v[0], v[1]);
+        }
+        iv_settle4(w, p, tag, err_word, &s_abort);
+#pragma unroll
+        for (int j = 0; j < YCH; ++j) {
+            const int e = tid + 256 * j, c = e >> 5, kp = e & 31;
+            *reinterpret_cast<float2 *>(&sYf[buf][c][2 * kp]) =
+                make_float2(__uint_as_float((unsigned)w[2 * j]), __uint_as_float((unsigned)w[2 * j + 1]));
         }
     };
 
@@ -411,15 +423,18 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
         return;
     }
     if (has_helper) {  // add the helper's partial sum (bounded wait)
+        unsigned long long w[4];
+        const unsigned long long *p[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const int64_t row = rb * kIvNb + 4 * rg + i, col = col0 + bc;
-            if (row < n && col < m) {
-                const unsigned long long *p = pl + row + col * ldl;
-                acc[i] += __uint_as_float(
-                    (unsigned)(iv_settle_word(iv_ld_word(p), p, tag, err_word, &s_abort) & 0xffffffffull));
-            }
+            p[i] = (row < n && col < m) ? pl + row + col * ldl : nullptr;
+            w[i] = p[i] ? iv_ld_word(p[i]) : 0ull;
         }
+        iv_settle4(w, p, tag, err_word, &s_abort);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            if (p[i]) acc[i] += __uint_as_float((unsigned)(w[i] & 0xffffffffull));
     }
 
     // 2. t = W_r acc (W_r^T acc when trans); the neighbour's words are read meanwhile
@@ -458,15 +473,15 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
     if (pb > 0) {
         float(*sM)[kIvLd] = sT[1];
         float(*sN)[C] = sV[1];
+        const unsigned long long *p[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const int64_t gk = qn * kIvNb + ta, col = col0 + tb + 4 * u;
-            float v = 0.f;
-            if (gk < n && col < m)
-                v = __uint_as_float(
-                    (unsigned)(iv_settle_word(wy[u], ll + gk + col * ldl, tag, err_word, &s_abort) & 0xffffffffull));
-            sN[ta][tb + 4 * u] = v;
+            p[u] = (gk < n && col < m) ? ll + gk + col * ldl : nullptr;
         }
+        iv_settle4(wy, p, tag, err_word, &s_abort);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) sN[ta][tb + 4 * u] = p[u] ? __uint_as_float((unsigned)wy[u]) : 0.f;
 #pragma unroll
         for (int u = 0; u < LPT; ++u) sM[tb + 4 * u][ta] = preM[u];  // M[i = ta][k = tb + 4u]
         __syncthreads();
