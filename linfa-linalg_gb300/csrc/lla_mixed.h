@@ -27,7 +27,7 @@ int residual_launch(const double *A, int64_t lda, int64_t n, const double *X, in
                     double *P, cudaStream_t st);
 
 // FP32 substitutions with inverted 64 x 64 diagonal blocks (lla_trsm_inv.cu).
-// W: diag_inverse_floats(n) floats (inverses and the two coupling sets);
+// W: diag_inverse_floats(n) floats (inverses and the four coupling sets);
 // stage: trsm_inv_stage_words(n, m) 64-bit words, zeroed when allocated;
 // epoch: nonzero and different for every launch on the same stage array.
 size_t diag_inverse_floats(int64_t n);

@@ -2,17 +2,18 @@
 // with inverted diagonal blocks.
 //
 // The refinement solves with the same low-precision factor L eight to ten
-// times, so three small matrices per 64-row block are formed once per factor:
-//     W_r  = L_rr^-1                      (diag_inverse_kernel)
-//     F_r  = W_r L_{r,r-1}                (forward coupling, fuse_kernel)
-//     G_r  = W_r^T L_{r+1,r}^T            (backward coupling, fuse_kernel)
+// times, so five small matrices per 64-row block are formed once per factor:
+//     W_r   = L_rr^-1                     (diag_inverse_kernel)
+//     F_r^d = W_r L_{r,r-d}               (forward coupling, d = 1, 2; fuse_kernel)
+//     G_r^d = W_r^T L_{r+d,r}^T           (backward coupling, d = 1, 2; fuse_kernel)
 // and every substitution is a chain of small matrix products:
-//     forward  L Y = B  : Y_r = W_r (B_r - sum_{q<r-1} L_rq Y_q) - F_r Y_{r-1}
-//     backward L^T X = Y: X_r = W_r^T (Y_r - sum_{q>r+1} L_qr^T X_q) - G_r X_{r+1}
+//     forward  L Y = B  : Y_r = W_r (B_r - sum_{q<r-2} L_rq Y_q) - F_r^2 Y_{r-2} - F_r^1 Y_{r-1}
+//     backward L^T X = Y: X_r = W_r^T (Y_r - sum_{q>r+2} L_qr^T X_q) - G_r^2 X_{r+2} - G_r^1 X_{r+1}
 // One CTA per (64-row block, 16-column chunk); CTAs take tickets in
-// processing order.  Everything but the last term is computed while the
-// previous block is still being solved, so the only work on the
-// block-to-block critical path is one 64 x 64 x 16 product.
+// processing order.  The sum over blocks solved three or more steps earlier
+// and its product with W_r are formed while the two previous blocks are
+// still being solved, the second neighbour's term while the first is, so the
+// only work on the block-to-block critical path is one 64 x 64 x 16 product.
 //
 // Hand-off between CTAs: a solved value is published as one 64-bit word
 // (launch epoch << 32 | float bits) in a staging array, so a consumer polls
@@ -69,22 +70,24 @@ __global__ void __launch_bounds__(64) diag_inverse_kernel(const float *__restric
     for (int i = 0; i < kIvNb; ++i) Wr[i + j * kIvNb] = w[i];
 }
 
-// F_r = W_r L_{r,r-1} and G_r = W_r^T L_{r+1,r}^T (zero where the neighbour
-// block does not exist), both column-major 64 x 64.  One CTA of 256 threads
-// per block; thread (i, kq) forms F[i][k] and G[i][k] for k = kq + 4u.
+// F_r^d = W_r L_{r,r-d} and G_r^d = W_r^T L_{r+d,r}^T for d = blockIdx.y + 1
+// (zero where that block does not exist), both column-major 64 x 64, in the
+// sets 2d - 1 and 2d after the inverses (set 0).  One CTA of 256 threads per
+// (block, d); thread (i, kq) forms F[i][k] and G[i][k] for k = kq + 4u.
 __global__ void __launch_bounds__(256) fuse_kernel(const float *__restrict__ L, int64_t ld, int64_t n,
-                                                   const float *__restrict__ W, float *F, float *G) {
+                                                   float *Wall) {
     __shared__ float sW[kIvNb][kIvNb + 1];  // sW[a][b] = W_r[a][b]
     __shared__ float sC[kIvNb][kIvNb + 1];
-    const int64_t r = blockIdx.x, R = gridDim.x;
+    const int64_t r = blockIdx.x, R = gridDim.x, d = blockIdx.y + 1;
     const int tid = threadIdx.x, i = tid % kIvNb, kq = tid / kIvNb;
-    const float *Wr = W + r * kIvTile;
+    const float *Wr = Wall + r * kIvTile;
+    float *F = Wall + (2 * d - 1) * R * kIvTile, *G = Wall + 2 * d * R * kIvTile;
     for (int e = tid; e < kIvTile; e += 256) sW[e % kIvNb][e / kIvNb] = Wr[e];
-    // forward: sC[j][k] = L[r*64 + j][(r-1)*64 + k]
+    // forward: sC[j][k] = L[r*64 + j][(r-d)*64 + k]
     for (int e = tid; e < kIvTile; e += 256) {
         const int j = e % kIvNb, k = e / kIvNb;
-        const int64_t gi = r * kIvNb + j, gk = (r - 1) * kIvNb + k;
-        sC[j][k] = (r > 0 && gi < n) ? L[gi + gk * ld] : 0.f;
+        const int64_t gi = r * kIvNb + j, gk = (r - d) * kIvNb + k;
+        sC[j][k] = (r >= d && gi < n) ? L[gi + gk * ld] : 0.f;
     }
     __syncthreads();
     float acc[16];
@@ -98,11 +101,11 @@ __global__ void __launch_bounds__(256) fuse_kernel(const float *__restrict__ L, 
 #pragma unroll
     for (int u = 0; u < 16; ++u) F[r * kIvTile + i + (kq + 4 * u) * kIvNb] = acc[u];
     __syncthreads();
-    // backward: sC[k][j] = L[(r+1)*64 + k][r*64 + j]; G[i][k] = sum_j W[j][i] sC[k][j]
+    // backward: sC[k][j] = L[(r+d)*64 + k][r*64 + j]; G[i][k] = sum_j W[j][i] sC[k][j]
     for (int e = tid; e < kIvTile; e += 256) {
         const int k = e % kIvNb, j = e / kIvNb;
-        const int64_t gk = (r + 1) * kIvNb + k, gj = r * kIvNb + j;
-        sC[k][j] = (r + 1 < R && gk < n) ? L[gk + gj * ld] : 0.f;
+        const int64_t gk = (r + d) * kIvNb + k, gj = r * kIvNb + j;
+        sC[k][j] = (r + d < R && gk < n) ? L[gk + gj * ld] : 0.f;
     }
     __syncthreads();
 #pragma unroll
@@ -234,7 +237,7 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
     float(*sV)[kIvNb][C] = reinterpret_cast<float(*)[kIvNb][C]>(iv_smem + NS * kIvNb * kIvLd + 2 * NS * C * kIvYd);
     float(*sYf)[C][kIvLd] =
         reinterpret_cast<float(*)[C][kIvLd]>(iv_smem + NS * kIvNb * kIvLd + 2 * NS * C * kIvYd + 2 * kIvNb * C);
-    static_assert(NS >= 3, "the partial sums reuse stage 2");
+    static_assert(NS >= 3, "the partial sums and the second neighbour's coupling matrix reuse stage 2");
     __shared__ int s_ticket, s_abort;
     const int tid = threadIdx.x;
     if (tid == 0) {
@@ -274,10 +277,10 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
         }
     }
     // coupling terms of this item, positions q_lo .. q_lo + nbulk - 1: a helper
-    // takes q < pb/2, its owner the rest before the neighbour's
+    // takes q < pb/2, its owner the rest before the two neighbours'
     const bool has_helper = pb >= hmin;
     const int64_t q_lo = (!helper && has_helper) ? pb / 2 : 0;
-    const int64_t nbulk = helper ? pb / 2 : (pb > 0 ? pb - 1 - q_lo : 0);
+    const int64_t nbulk = helper ? pb / 2 : (pb > 1 ? pb - 2 - q_lo : 0);
 
     // Stage s <- coupling tile and solved words of processing position pq.
     // Tile: 64 columns a of 64 contiguous rows b (non-trans: a = k, b = i;
@@ -437,15 +440,27 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
             if (p[i]) acc[i] += __uint_as_float((unsigned)(w[i] & 0xffffffffull));
     }
 
-    // 2. t = W_r acc (W_r^T acc when trans); the neighbour's words are read meanwhile
-    unsigned long long wy[4];
-    const int64_t qn = TRANS ? rb + 1 : rb - 1;  // neighbour block
+    // 2. t = W_r acc (W_r^T acc when trans); both neighbours' words and the
+    // second neighbour's coupling matrix are read meanwhile
+    unsigned long long wy[4], wy2[4];
+    float preM2[LPT];
+    const int64_t qn = TRANS ? rb + 1 : rb - 1, qn2 = TRANS ? rb + 2 : rb - 2;  // neighbour blocks
     if (pb > 0) {
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const int64_t gk = qn * kIvNb + ta, col = col0 + tb + 4 * u;
             wy[u] = (gk < n && col < m) ? iv_ld_word(ll + gk + col * ldl) : tag;
         }
+    }
+    if (pb > 1) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t gk = qn2 * kIvNb + ta, col = col0 + tb + 4 * u;
+            wy2[u] = (gk < n && col < m) ? iv_ld_word(ll + gk + col * ldl) : tag;
+        }
+        const float *M2r = Wall + ((TRANS ? 4 : 3) * R + rb) * kIvTile + ta + tb * kIvNb;
+#pragma unroll
+        for (int u = 0; u < LPT; ++u) preM2[u] = M2r[u * 4 * kIvNb];
     }
     float(*sK)[kIvLd] = sT[0];  // coefficient tile: sK[k][i]
     float(*sX)[C] = sV[0];
@@ -469,7 +484,34 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
         t[2] = fmaf(l, x.z, t[2]);
         t[3] = fmaf(l, x.w, t[3]);
     }
-    // 3. t -= M_r x_neighbour, M_r (F_r or G_r) stored as the plain coefficient matrix
+    // 3. t -= M2_r x_second_neighbour, then t -= M_r x_neighbour; M_r, M2_r
+    // (F_r^1, F_r^2 or G_r^1, G_r^2) stored as plain coefficient matrices
+    if (pb > 1) {
+        float(*sM)[kIvLd] = sT[2];
+        float(*sN)[C] = reinterpret_cast<float(*)[C]>(&sYf[0][0][0]);  // 64 x 16 (free after the bulk)
+        const unsigned long long *p[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t gk = qn2 * kIvNb + ta, col = col0 + tb + 4 * u;
+            p[u] = (gk < n && col < m) ? ll + gk + col * ldl : nullptr;
+        }
+        iv_settle4(wy2, p, tag, err_word, &s_abort);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) sN[ta][tb + 4 * u] = p[u] ? __uint_as_float((unsigned)wy2[u]) : 0.f;
+#pragma unroll
+        for (int u = 0; u < LPT; ++u) sM[tb + 4 * u][ta] = preM2[u];
+        __syncthreads();
+        if (s_abort) return;
+#pragma unroll 8
+        for (int k = 0; k < kIvNb; ++k) {
+            const float l = sM[k][ta];
+            const float4 x = *reinterpret_cast<const float4 *>(&sN[k][tb * 4]);
+            t[0] = fmaf(-l, x.x, t[0]);
+            t[1] = fmaf(-l, x.y, t[1]);
+            t[2] = fmaf(-l, x.z, t[2]);
+            t[3] = fmaf(-l, x.w, t[3]);
+        }
+    }
     if (pb > 0) {
         float(*sM)[kIvLd] = sT[1];
         float(*sN)[C] = sV[1];
@@ -514,7 +556,7 @@ size_t trsm_inv_stage_words(int64_t n, int64_t m) {
     return 2 * (size_t)((n + kIvNb - 1) / kIvNb) * kIvNb * (size_t)m;
 }
 
-size_t diag_inverse_floats(int64_t n) { return 3 * (size_t)((n + kIvNb - 1) / kIvNb) * kIvTile; }
+size_t diag_inverse_floats(int64_t n) { return 5 * (size_t)((n + kIvNb - 1) / kIvNb) * kIvTile; }
 
 int diag_inverse_launch(const float *L, int64_t ld, int64_t n, float *W, cudaStream_t st) {
     if (n == 0) return 0;
@@ -524,8 +566,8 @@ int diag_inverse_launch(const float *L, int64_t ld, int64_t n, float *W, cudaStr
         diag_inverse_kernel<<<(unsigned)R, 64, 0, st>>>(L, ld, n, W);
         if (cudaGetLastError() != cudaSuccess) return -1;
     }
-    LaunchScope ls(K_MIXED_TRSM, st, 4.0 * (double)R * kIvTile * kIvNb);
-    fuse_kernel<<<(unsigned)R, 256, 0, st>>>(L, ld, n, W, W + R * kIvTile, W + 2 * R * kIvTile);
+    LaunchScope ls(K_MIXED_TRSM, st, 8.0 * (double)R * kIvTile * kIvNb);
+    fuse_kernel<<<dim3((unsigned)R, 2), 256, 0, st>>>(L, ld, n, W);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
