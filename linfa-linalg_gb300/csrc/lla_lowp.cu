@@ -39,6 +39,17 @@ constexpr int kLpNb = 128;  // panel width
 constexpr int kLpLd = kLpNb + 1;
 constexpr int kLpPd = kLpNb + 4;  // row stride of the transposed 32-column panel (16-byte rows)
 
+// asynchronous global -> shared copies (all of a thread's copies in flight at once)
+__device__ __forceinline__ void lp_cp4(float *dst, const float *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void lp_cp16(float *dst, const float *src, int bytes) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void lp_cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // ---------------------------------------------------------------------------
 // diagonal block: b <= 128, one CTA of 1024 threads, block in shared memory
 
@@ -54,9 +65,15 @@ __global__ void __launch_bounds__(1024) lowp_diag_kernel(float *L, int64_t ld, i
     // as blockdiag(L11, I)), so every step below runs unpredicated on 128 rows.
     for (int e = tid; e < kLpNb * kLpNb; e += 1024) {
         const int r = e % kLpNb, c = e / kLpNb;
-        if (c <= r) sa[r * kLpLd + c] = (r < b) ? L[(p + r) + (p + c) * ld] : (r == c ? 1.f : 0.f);
+        if (c <= r) {
+            if (r < b)
+                lp_cp4(&sa[r * kLpLd + c], &L[(p + r) + (p + c) * ld]);
+            else
+                sa[r * kLpLd + c] = (r == c) ? 1.f : 0.f;
+        }
     }
     if (tid == 0) failed = 0;
+    lp_cp_wait_all();
     __syncthreads();
     float ratio = 1e30f;
 #pragma unroll 1
@@ -119,7 +136,7 @@ __global__ void __launch_bounds__(1024) lowp_diag_kernel(float *L, int64_t ld, i
                 }
             } else {
 #pragma unroll
-                for (int c = 0; c < 32; ++c) Wd[kb * 32 + c * 32 + ie] = v[c];  // W[c][ie], row-major
+                for (int c = 0; c < 32; ++c) Wd[kb * 32 + ie * 32 + c] = v[c];  // W[c][ie] at [J][ie][c]
             }
         }
         __syncthreads();
@@ -192,7 +209,8 @@ __device__ __forceinline__ float from_half(__half h) { return __half2float(h); }
 // panel: rows [q, n), q = p + 128.  L21 = A21 L11^-T in FP32 by 32-column
 // blocks J, each a pair of small products (no sequential step):
 //     Y_J = A_J - sum_{I<J} X_I L_JI^T,   X_J = Y_J W_JJ^T,
-// W_JJ = L_JJ^-1 from the diagonal kernel.  Then the operand planes of L21
+// W_JJ = L_JJ^-1 from the diagonal kernel (Wd[J][k][c] = W_JJ[c][k]); only the
+// blocks of L11 below its diagonal blocks are read.  Then the operand planes of L21
 // for the tensor cores (zero for k >= b).  One CTA of 256 threads per 64 rows;
 // for products, thread (rt = tid % 32, ct = tid / 32) owns rows rt, rt + 32 and
 // columns 4 ct .. 4 ct + 3 of the current block.
@@ -215,25 +233,47 @@ __global__ void __launch_bounds__(256) lowp_panel_kernel(float *L, int64_t ld, i
     const int tid = threadIdx.x;
     const int64_t q = p + kLpNb;
     const int64_t row0 = q + (int64_t)blockIdx.x * kPnRows;
-    // loads: columns of the row tile and of L11 are contiguous in memory
-    // (constant trip counts, unrolled: many loads in flight per thread)
-    {
-        const int r = tid % kPnRows;
-        const bool ok = row0 + r < n;
-        const float *src = L + (row0 + r) + p * ld;
+    // Columns of the row tile and of L11 are contiguous in memory.  With
+    // 16-byte aligned columns every input is copied by cp.async, all of a
+    // thread's copies in flight at once; otherwise by plain loads.
+    if (ld % 4 == 0 && (reinterpret_cast<uintptr_t>(L) & 15) == 0) {
+        // row tile: sXT[k][r] = L[row0 + r][p + k], 16 four-row chunks per column
+        for (int e = tid; e < kLpNb * (kPnRows / 4); e += 256) {
+            const int k = e / (kPnRows / 4), c4 = e % (kPnRows / 4);
+            const int64_t r = row0 + 4 * c4;
+            const int valid = n - r >= 4 ? 4 : (n - r > 0 ? (int)(n - r) : 0);
+            lp_cp16(&sXT[k * kPnXd + 4 * c4], valid ? L + r + (p + k) * ld : L, 4 * valid);
+        }
+        // L11 below its diagonal blocks: column k < 96, rows c in [32 (k/32 + 1), 128)
+        for (int e = tid; e < 32 * (24 + 16 + 8); e += 256) {
+            const int kb = e < 32 * 24 ? 0 : (e < 32 * 40 ? 1 : 2);
+            const int idx = e - (kb == 0 ? 0 : (kb == 1 ? 32 * 24 : 32 * 40)), per = 24 - 8 * kb;
+            const int k = 32 * kb + idx / per, c = 32 * (kb + 1) + 4 * (idx % per);
+            lp_cp16(&sLT[k * kPnLd + c], L + (p + c) + (p + k) * ld, 16);
+        }
+        // W_JJ, k-major rows of 32
+        for (int e = tid; e < 4 * 32 * 8; e += 256) {
+            const int row = e / 8, c4 = e % 8;
+            lp_cp16(&sWT[row * kPnWd + 4 * c4], Wd + row * 32 + 4 * c4, 16);
+        }
+        lp_cp_wait_all();
+    } else {
+        {
+            const int r = tid % kPnRows;
+            const bool ok = row0 + r < n;
+            const float *src = L + (row0 + r) + p * ld;
 #pragma unroll 8
-        for (int k = tid / kPnRows; k < kLpNb; k += 256 / kPnRows) sXT[k * kPnXd + r] = ok ? src[k * ld] : 0.f;
-    }
-    {
-        const int c = tid % kLpNb;
-        const float *src = L + (p + c) + p * ld;
+            for (int k = tid / kPnRows; k < kLpNb; k += 256 / kPnRows) sXT[k * kPnXd + r] = ok ? src[k * ld] : 0.f;
+        }
+        {
+            const int c = tid % kLpNb;
+            const float *src = L + (p + c) + p * ld;
 #pragma unroll 8
-        for (int k = tid / kLpNb; k < kLpNb; k += 256 / kLpNb) sLT[k * kPnLd + c] = (k <= c) ? src[k * ld] : 0.f;
-    }
+            for (int k = tid / kLpNb; k < kLpNb; k += 256 / kLpNb)
+                sLT[k * kPnLd + c] = (32 * (k / 32 + 1) <= c) ? src[k * ld] : 0.f;
+        }
 #pragma unroll
-    for (int e = tid; e < 4 * 32 * 32; e += 256) {  // Wd[J][c][k] row-major
-        const int k = e % 32, c = (e / 32) % 32, J = e / 1024;
-        sWT[(J * 32 + k) * kPnWd + c] = Wd[e];
+        for (int e = tid; e < 4 * 32 * 32; e += 256) sWT[(e / 32) * kPnWd + e % 32] = Wd[e];
     }
     __syncthreads();
     const int rt = tid % 32, ct = tid / 32;
