@@ -216,9 +216,10 @@ __device__ __forceinline__ float from_half(__half h) { return __half2float(h); }
 // columns 4 ct .. 4 ct + 3 of the current block.
 constexpr int kPnRows = 64;
 constexpr int kPnXd = kPnRows + 4;  // row stride of sXT (k-major copy of the row tile)
-constexpr int kPnLd = kLpNb + 4;    // row stride of sLT (k-major copy of L11)
+constexpr int kPnLd = kLpNb + 4;    // row stride of sLT (k-major copy of L11, columns k < 96)
 constexpr int kPnWd = 32 + 4;       // row stride of sWT (k-major W_JJ)
-constexpr size_t kPnSmem = sizeof(float) * (kLpNb * kPnXd + kLpNb * kPnLd + 4 * 32 * kPnWd);
+// 103,936 bytes: two CTAs per SM
+constexpr size_t kPnSmem = sizeof(float) * (kLpNb * kPnXd + (kLpNb - 32) * kPnLd + 4 * 32 * kPnWd);
 
 template <typename H>
 __global__ void __launch_bounds__(256) lowp_panel_kernel(float *L, int64_t ld, int64_t n, int64_t p,
@@ -228,7 +229,7 @@ __global__ void __launch_bounds__(256) lowp_panel_kernel(float *L, int64_t ld, i
     extern __shared__ __align__(16) float sm[];
     float *sXT = sm;                         // sXT[k * kPnXd + r] = row r, column k of the tile
     float *sLT = sXT + kLpNb * kPnXd;        // sLT[k * kPnLd + c] = L11[c][k]
-    float *sWT = sLT + kLpNb * kPnLd;        // sWT[(J * 32 + k) * kPnWd + c] = W_JJ[c][k]
+    float *sWT = sLT + (kLpNb - 32) * kPnLd;  // sWT[(J * 32 + k) * kPnWd + c] = W_JJ[c][k]
     if (*(volatile const int64_t *)info >= 0) return;
     const int tid = threadIdx.x;
     const int64_t q = p + kLpNb;
@@ -269,7 +270,7 @@ __global__ void __launch_bounds__(256) lowp_panel_kernel(float *L, int64_t ld, i
             const int c = tid % kLpNb;
             const float *src = L + (p + c) + p * ld;
 #pragma unroll 8
-            for (int k = tid / kLpNb; k < kLpNb; k += 256 / kLpNb)
+            for (int k = tid / kLpNb; k < kLpNb - 32; k += 256 / kLpNb)
                 sLT[k * kPnLd + c] = (32 * (k / 32 + 1) <= c) ? src[k * ld] : 0.f;
         }
 #pragma unroll
