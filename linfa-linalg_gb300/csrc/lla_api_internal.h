@@ -29,6 +29,7 @@ struct HostBuf {
 struct MixedWs {
     DevBuf L, s, rowsum, R, Y, diag0, words;  // FP32 factor, scaling, norms, residual, correction
     DevBuf P;                                 // split-K partial products of the residual
+    DevBuf sympart;                           // per-tile partial row sums / maxima of |A|
     DevBuf oz;                                // exact-slice residual: slices of A and X
     DevBuf winv;                              // inverted 64 x 64 diagonal blocks of L
     DevBuf stage;                             // epoch-tagged hand-off words of the substitutions

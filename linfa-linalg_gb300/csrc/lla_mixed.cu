@@ -62,54 +62,106 @@ __global__ void equil_scale_kernel(const double *A, int64_t lda, int64_t n, int 
     s[i] = ldexp(1.0, -(e >= 0 ? e / 2 : -((-e + 1) / 2)));
 }
 
-// W[i,j] = fp32(s_i a_ij s_j) for the lower triangle (i >= j), column-major.
-__global__ void equil_convert_kernel(const double *__restrict__ A, int64_t lda, int64_t n,
-                                     const double *__restrict__ s, float *W, int64_t ldw) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t j = blockIdx.y;
-    if (i >= n) return;
-    for (int64_t jj = j; jj < n; jj += gridDim.y)
-        if (i >= jj) W[i + jj * ldw] = (float)(s[i] * A[i + jj * lda] * s[jj]);
+// One pass over the lower triangle of A in 64 x 64 tiles (I, J), I >= J:
+// W = fp32(S A S) (lower triangle, column-major), and per tile the partial
+// row sums / maxima of |a_ik| over its columns (elements on or below the
+// diagonal) and the partial column sums / maxima over its rows (elements
+// strictly below the diagonal, which stand for the upper triangle of A_sym).
+// No atomics: sym_rows_kernel adds the partials of each row in a fixed order.
+// Partials, n_pad = R * 64 apart: P[0][J] row sums, P[1][J] row maxima (tile
+// column J), P[2][I] column sums, P[3][I] column maxima (tile row I).
+// FP64 arithmetic is scarce on this GPU, so every element costs one FP64 add
+// for its row and one for its column; the maxima are taken on the bit
+// patterns (non-negative doubles order like unsigned integers).
+// Thread (r = tid % 64, cg = tid / 64): row r, columns 16 cg .. 16 cg + 15.
+constexpr int kSymT = 64;
+template <bool MAX>
+__global__ void __launch_bounds__(256) sym_tile_kernel(const double *__restrict__ A, int64_t lda, int64_t n,
+                                                       const double *__restrict__ s, float *W, int64_t ldw,
+                                                       double *P) {
+    const int64_t I = blockIdx.y, J = blockIdx.x;
+    if (J > I) return;
+    const int64_t R = gridDim.y, npad = R * kSymT;
+    __shared__ double prs[4][kSymT];
+    __shared__ unsigned long long prm[4][kSymT];
+    __shared__ unsigned long long sv[kSymT][kSymT + 1];  // sv[c][r]: bits of |a| for the column partials
+    const int tid = threadIdx.x, r = tid % kSymT, cg = tid / kSymT;
+    const int64_t i = I * kSymT + r;
+    const double si = i < n ? s[i] : 0.0;
+    double rs = 0.0;
+    unsigned long long rm = 0ull;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+        const int c = 16 * cg + u;
+        const int64_t k = J * kSymT + c;
+        const bool lower = i < n && k < n && (I > J || r >= c);
+        const double a = lower ? A[i + k * lda] : 0.0;
+        if (lower) W[i + k * ldw] = (float)(si * a * s[k]);
+        const unsigned long long v = (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull;
+        rs += __longlong_as_double((long long)v);
+        if (MAX) rm = v > rm ? v : rm;
+        sv[c][r] = (I > J || r > c) ? v : 0ull;
+    }
+    prs[cg][r] = rs;
+    if (MAX) prm[cg][r] = rm;
+    __syncthreads();
+    if (tid < kSymT) {  // row partial of row tid
+        P[J * npad + I * kSymT + tid] = ((prs[0][tid] + prs[1][tid]) + prs[2][tid]) + prs[3][tid];
+        if (MAX) {
+            unsigned long long m = prm[0][tid];
+#pragma unroll
+            for (int g = 1; g < 4; ++g) m = prm[g][tid] > m ? prm[g][tid] : m;
+            P[(R + J) * npad + I * kSymT + tid] = __longlong_as_double((long long)m);
+        }
+    } else if (tid < 2 * kSymT) {  // column partial of column c
+        const int c = tid - kSymT;
+        double cs = 0.0;
+        unsigned long long cm = 0ull;
+#pragma unroll 8
+        for (int q = 0; q < kSymT; ++q) {
+            const unsigned long long v = sv[c][q];
+            cs += __longlong_as_double((long long)v);
+            if (MAX) cm = v > cm ? v : cm;
+        }
+        P[(2 * R + I) * npad + J * kSymT + c] = cs;
+        if (MAX) P[(3 * R + I) * npad + J * kSymT + c] = __longlong_as_double((long long)cm);
+    }
 }
 
-// Row sums of |A_sym| (A_sym from the lower triangle): one block per 32-column
-// strip [k0, k0+32).  Element (i, k), i >= k, adds |a_ik| to row i (a per-row
-// partial, one atomic per strip) and, off the diagonal, to row k (per-thread
-// column partials, reduced across the block at the end).
-__global__ void __launch_bounds__(256) sym_rowsum_kernel(const double *__restrict__ A, int64_t lda,
-                                                         int64_t n, double *rowsum) {
-    __shared__ double red[8][32];
-    const int64_t k0 = (int64_t)blockIdx.x * 32;
-    double colp[32];
-#pragma unroll
-    for (int c = 0; c < 32; ++c) colp[c] = 0.0;
-    for (int64_t i = k0 + threadIdx.x; i < n; i += blockDim.x) {
-        double racc = 0.0;
-#pragma unroll
-        for (int c = 0; c < 32; ++c) {
-            const int64_t k = k0 + c;
-            if (k < n && k <= i) {
-                const double v = fabs(A[i + k * lda]);
-                racc += v;
-                if (k != i) colp[c] += v;
-            }
+// rowsum[i] (and rowmax[i]) from the tile partials: tile columns J <= i/64 in
+// order, then tile rows I >= i/64 in order (maxima on the bit patterns; a NaN
+// maximum reads as +inf).
+__global__ void sym_rows_kernel(const double *__restrict__ P, int64_t R, int64_t n, double *rowsum,
+                                double *rowmax) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t b = i / kSymT, npad = R * kSymT;
+    const unsigned long long *Pb = reinterpret_cast<const unsigned long long *>(P);
+    double sum = 0.0;
+    unsigned long long mx = 0ull;
+#pragma unroll 8
+    for (int64_t J = 0; J <= b; ++J) {
+        sum += P[J * npad + i];
+        if (rowmax) {
+            const unsigned long long v = Pb[(R + J) * npad + i];
+            mx = v > mx ? v : mx;
         }
-        atomicAdd(&rowsum[i], racc);
     }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-#pragma unroll
-    for (int c = 0; c < 32; ++c) {
-        double v = colp[c];
-#pragma unroll
-        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) red[warp][c] = v;
+#pragma unroll 8
+    for (int64_t I = b; I < R; ++I) {
+        sum += P[(2 * R + I) * npad + i];
+        if (rowmax) {
+            const unsigned long long v = Pb[(3 * R + I) * npad + i];
+            mx = v > mx ? v : mx;
+        }
     }
-    __syncthreads();
-    if (threadIdx.x < 32 && k0 + threadIdx.x < n) {
-        double v = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
-        atomicAdd(&rowsum[k0 + threadIdx.x], v);
-    }
+    rowsum[i] = sum;
+    if (rowmax) rowmax[i] = __longlong_as_double((long long)(mx > 0x7ff0000000000000ull ? 0x7ff0000000000000ull : mx));
+}
+
+size_t sym_part_doubles(int64_t n) {
+    const int64_t R = (n + kSymT - 1) / kSymT;
+    return (size_t)4 * R * R * kSymT;
 }
 
 __global__ void max_reduce_kernel(const double *v, int64_t n, double *out) {
@@ -291,20 +343,26 @@ __global__ void residual_combine_kernel(const double *__restrict__ P, int splits
 static unsigned gx(int64_t n, int b) { return (unsigned)ceil_div(n, b); }
 
 int equilibrate_launch(const double *A, int64_t lda, int64_t n, bool scale, double *s, float *W,
-                       int64_t ldw, double *rowsum, double *anorm, int *bad, cudaStream_t st) {
+                       int64_t ldw, double *rowsum, double *anorm, double *rowmax, double *part, int *bad,
+                       cudaStream_t st) {
     {
         LaunchScope ls(K_MIXED_CONVERT, st, 8.0 * n);
         equil_scale_kernel<<<gx(n, 256), 256, 0, st>>>(A, lda, n, scale ? 1 : 0, s, bad);
     }
+    const int64_t R = (n + kSymT - 1) / kSymT;
+    if (R > 65535) return -1;
     {
-        LaunchScope ls(K_MIXED_CONVERT, st, 6.0 * n * (n + 1) / 2);
-        equil_convert_kernel<<<dim3(gx(n, 256), (unsigned)std::min<int64_t>(n, 4096)), 256, 0, st>>>(
-            A, lda, n, s, W, ldw);
+        // algorithmic bytes: the lower triangle of A read, that of W written
+        LaunchScope ls(K_MIXED_CONVERT, st, 12.0 * n * (n + 1) / 2);
+        if (rowmax)
+            sym_tile_kernel<true><<<dim3((unsigned)R, (unsigned)R), 256, 0, st>>>(A, lda, n, s, W, ldw, part);
+        else
+            sym_tile_kernel<false><<<dim3((unsigned)R, (unsigned)R), 256, 0, st>>>(A, lda, n, s, W, ldw, part);
+        if (cudaGetLastError() != cudaSuccess) return -1;
     }
-    if (cudaMemsetAsync(rowsum, 0, sizeof(double) * n, st) != cudaSuccess) return -1;
     {
-        LaunchScope ls(K_MISC, st, 8.0 * n * (n + 1) / 2);
-        sym_rowsum_kernel<<<gx(n, 32), 256, 0, st>>>(A, lda, n, rowsum);
+        LaunchScope ls(K_MIXED_CONVERT, st, 8.0 * R * n * (rowmax ? 2 : 1));
+        sym_rows_kernel<<<gx(n, 256), 256, 0, st>>>(part, R, n, rowsum, rowmax);
     }
     {
         LaunchScope ls(K_MISC, st);
@@ -493,8 +551,15 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
     }
     // 1. equilibrate (and ||A||_inf, ||b_j||_inf)
     auto t0 = std::chrono::steady_clock::now();
+    const bool slices = opts.residual == LLA_RESIDUAL_EXACT_SLICES;
+    MX_TRY(w.sympart.ensure(sizeof(double) * sym_part_doubles(n)));
+    double *oz_rm = nullptr;  // row maxima of |A| for the exact-slice residual, formed in the same pass
+    if (slices) {
+        MX_TRY(w.oz.ensure(oz_workspace_bytes(n, m)));
+        oz_rm = oz_rowmax(w.oz.p, n, m);
+    }
     MX_TRY(last_err(equilibrate_launch(dA, lda, n, opts.equilibrate != 0, s, L, n,
-                                       (double *)w.rowsum.p, anorm, bad, st)));
+                                       (double *)w.rowsum.p, anorm, oz_rm, (double *)w.sympart.p, bad, st)));
     MX_TRY(last_err(colmax_launch(dB, ldb, n, m, colmax_b, st)));
     // 2. low-precision factorisation
     bool lowp_ok = true;
@@ -510,11 +575,8 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
     }
     if (lowp_ok)  // inverses of the 64 x 64 diagonal blocks, reused by every substitution
         MX_TRY(last_err(diag_inverse_launch(L, n, n, (float *)w.winv.p, st)));
-    const bool slices = opts.residual == LLA_RESIDUAL_EXACT_SLICES;
-    if (lowp_ok && slices) {  // slices of A, once per solve
-        MX_TRY(w.oz.ensure(oz_workspace_bytes(n, m)));
-        MX_TRY(last_err(oz_prepare(dA, lda, n, m, w.oz.p, st)));
-    }
+    if (lowp_ok && slices)  // slices of A, once per solve
+        MX_TRY(last_err(oz_prepare(dA, lda, n, m, w.oz.p, true, st)));
     r.ms_factor = ms_since(t0);
     r.factor_failed = lowp_ok ? 0 : 1;
     // 3. refinement
@@ -643,7 +705,7 @@ extern "C" int lla_dresidual_device(const double *dA, int64_t n, int64_t lda, co
                                         (double *)w.P.p, st)));
     } else {
         MX_TRY(w.oz.ensure(oz_workspace_bytes(n, m)));
-        MX_TRY(last_err(oz_prepare(dA, lda, n, m, w.oz.p, st)));
+        MX_TRY(last_err(oz_prepare(dA, lda, n, m, w.oz.p, false, st)));
         MX_TRY(last_err(colmax_launch(dX, ldx, n, m, colmax_x, st)));
         MX_TRY(last_err(oz_residual_launch(dX, ldx, dB, ldb, dR, ldr, n, m, colmax_x, colmax_r, w.oz.p,
                                            err_word, st)));

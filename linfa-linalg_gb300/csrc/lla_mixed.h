@@ -16,8 +16,13 @@ struct Ctx;
 int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &opts, int64_t *info,
                        float *diag0, double *min_ratio, Ctx *c, cudaStream_t st);
 
+// Power-of-two scaling s, W = fp32(S A S) (lower), the row sums of |A| and
+// ||A||_inf in one pass over A; rowmax (may be NULL): the row maxima of |A| too.
+// part: sym_part_doubles(n) doubles of per-tile partial sums.
+size_t sym_part_doubles(int64_t n);
 int equilibrate_launch(const double *A, int64_t lda, int64_t n, bool scale, double *s, float *W,
-                       int64_t ldw, double *rowsum, double *anorm, int *bad, cudaStream_t st);
+                       int64_t ldw, double *rowsum, double *anorm, double *rowmax, double *part, int *bad,
+                       cudaStream_t st);
 int colmax_launch(const double *M, int64_t ld, int64_t n, int64_t m, double *colmax, cudaStream_t st);
 // R = B - A_sym X in FP64; P: workspace of residual_splits(n, m) * n * m
 // doubles for the split-K partials (NULL: no split).
@@ -40,8 +45,11 @@ int trsm_inv_launch(const float *L, int64_t ld, const float *W, int64_t n, float
 
 // Exact-slice (tensor-core) residual: workspace size, once-per-solve slicing
 // of A, and the per-iteration residual (colmax_x: column maxima of |X|).
+// rowmax_ready: the row maxima at oz_rowmax(ws, n, m) were already formed
+// (equilibrate_launch); otherwise oz_prepare forms them.
 size_t oz_workspace_bytes(int64_t n, int64_t m);
-int oz_prepare(const double *A, int64_t lda, int64_t n, int64_t m, void *ws, cudaStream_t st);
+double *oz_rowmax(void *ws, int64_t n, int64_t m);
+int oz_prepare(const double *A, int64_t lda, int64_t n, int64_t m, void *ws, bool rowmax_ready, cudaStream_t st);
 int oz_residual_launch(const double *X, int64_t ldx, const double *B, int64_t ldb, double *R, int64_t ldr,
                        int64_t n, int64_t m, const double *colmax_x, double *colmax_r, void *ws,
                        int *err_word, cudaStream_t st);

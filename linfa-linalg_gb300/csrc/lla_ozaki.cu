@@ -463,12 +463,18 @@ static void oz_carve(void *ws, int64_t n, int64_t m, OzState &o) {
     o.splits = oz_splits(n);
 }
 
-// Once per solve: row maxima and slices of A.
-int oz_prepare(const double *A, int64_t lda, int64_t n, int64_t m, void *ws, cudaStream_t st) {
+double *oz_rowmax(void *ws, int64_t n, int64_t m) {
     OzState o;
     oz_carve(ws, n, m, o);
-    if (cudaMemsetAsync(o.rowmax, 0, sizeof(double) * n, st) != cudaSuccess) return -1;
-    {
+    return o.rowmax;
+}
+
+// Once per solve: row maxima (unless already formed) and slices of A.
+int oz_prepare(const double *A, int64_t lda, int64_t n, int64_t m, void *ws, bool rowmax_ready, cudaStream_t st) {
+    OzState o;
+    oz_carve(ws, n, m, o);
+    if (!rowmax_ready) {
+        if (cudaMemsetAsync(o.rowmax, 0, sizeof(double) * n, st) != cudaSuccess) return -1;
         LaunchScope ls(K_OZ_SLICE, st, 8.0 * n * n);
         oz_rowmax_kernel<<<(unsigned)((n + 31) / 32), 256, 0, st>>>(A, lda, n, o.rowmax);
     }
