@@ -88,6 +88,8 @@ __global__ void __launch_bounds__(256) sym_tile_kernel(const double *__restrict_
     const int tid = threadIdx.x, r = tid % kSymT, cg = tid / kSymT;
     const int64_t i = I * kSymT + r;
     const double si = i < n ? s[i] : 0.0;
+    // s holds powers of two: the scaling adds e_i + e_k to the exponent field
+    const int ei = (int)((__double_as_longlong(si) >> 52) & 0x7ff) - 1023;
     double rs = 0.0;
     unsigned long long rm = 0ull;
 #pragma unroll
@@ -96,7 +98,18 @@ __global__ void __launch_bounds__(256) sym_tile_kernel(const double *__restrict_
         const int64_t k = J * kSymT + c;
         const bool lower = i < n && k < n && (I > J || r >= c);
         const double a = lower ? A[i + k * lda] : 0.0;
-        if (lower) W[i + k * ldw] = (float)(si * a * s[k]);
+        if (lower) {
+            const double sk = s[k];
+            const int es = ei + (int)((__double_as_longlong(sk) >> 52) & 0x7ff) - 1023;
+            const long long ab = __double_as_longlong(a);
+            const int ex = (int)((ab >> 52) & 0x7ff), ne = ex + es;
+            // normal in and out: exact exponent shift; otherwise (zero, subnormal,
+            // inf/NaN, out of range) the plain product
+            const double as = (ex != 0 && ex != 0x7ff && ne > 0 && ne < 0x7ff)
+                                  ? __longlong_as_double(ab + ((long long)es << 52))
+                                  : si * a * sk;
+            W[i + k * ldw] = (float)as;
+        }
         const unsigned long long v = (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull;
         rs += __longlong_as_double((long long)v);
         if (MAX) rm = v > rm ? v : rm;
