@@ -38,6 +38,31 @@ BE_TARGET = 1e-13
 METRIC = "SPD solves/s at backward error <= 1e-13 (n=16384, 64 RHS, kappa=1e6)"
 
 
+def mixed_update_bytes(n, nb=128):
+    """FP32 trailing-matrix bytes (read + write of the lower part) of the tensor-core
+    updates of one low-precision factorisation, and their launch count: panels in
+    pairs, a narrow update of the next 128-column block, then one update of the rest."""
+    tot, launches, p = 0.0, 0, 0
+    while p < n:
+        b = min(nb, n - p)
+        rest = n - p - b
+        if rest <= 0:
+            break
+        if rest > nb:
+            rows = n - p - nb
+            tot += (rows * nb - nb * (nb - 1) / 2) * 8
+            rows = n - p - 2 * nb
+            tot += rows * (rows + 1) / 2 * 8
+            launches += 2
+            p += 2 * nb
+        else:
+            rows = n - p - nb
+            tot += rows * (rows + 1) / 2 * 8
+            launches += 1
+            p += nb
+    return tot, launches
+
+
 def flops_solve(n, m):
     """Cholesky n^3/3 + two triangular solves 2 n^2 m."""
     return n ** 3 / 3.0 + 2.0 * n * n * m
@@ -384,13 +409,22 @@ def main():
     sec = dom_ms * 1e-3
     extra = {}
     if dom == "mixed_update":
-        # HBM-bound: every launch reads and writes the FP32 lower trailing matrix once;
-        # work = sum rest (rest + 1) 128 flops, so bytes = work / 128 * 4
-        alg = dom_work / 128 * 4
-        bound, unit, achieved, peak = "hbm", "GB/s", alg / sec / 1e9, hbm
-        extra = {"algorithmic_bytes_per_launch": alg / dom_n,
-                 "tensor_tflops_executed": 6 * dom_work / sec / 1e12,
-                 "note": "six BF16 term-pair products per tile (bf16x6)" if args.update == "bf16x6" else None}
+        # Panels in pairs: per pair a narrow launch (K = 128, one 128-column block) and
+        # one K = 256 launch over the rest of the trailing matrix.  Per 128 x 128 tile the
+        # term products execute products * 2 * 128^2 * K tensor flops against 128 KB of
+        # FP32 read + write (384 flop/B for bf16x6 at K = 256, above the ridge point
+        # bf16 peak / HBM), so the tensor pipe is the roofline; the HBM side is reported
+        # beside it from the exact bytes of the pair schedule.
+        products = {"bf16": 1, "fp16": 1, "bf16x3": 3, "fp16x3": 3, "bf16x6": 6}.get(args.update, 1)
+        upd_bytes, upd_launches = mixed_update_bytes(n)
+        solves = dom_n / upd_launches
+        bound, unit, achieved, peak = "tensor", "TFLOP/s", products * dom_work / sec / 1e12, bf16
+        extra = {"algorithmic_bytes_per_launch": upd_bytes / upd_launches,
+                 "tensor_products": products,
+                 "hbm_gbs": upd_bytes * solves / sec / 1e9,
+                 "hbm_frac": upd_bytes * solves / sec / 1e9 / hbm,
+                 "note": "executed tensor flops (term products x 2 x lower-tile MACs) over the burst bf16 "
+                         "peak; clocks stayed at the maximum SM clock"}
     elif dom == "mixed_trsm":
         # two substitutions per iteration: each reads the FP32 factor's lower triangle once
         nsub = max(1, dom_n - 2 * args.steps)  # minus the per-factor inverse and coupling kernels
