@@ -26,6 +26,7 @@
 #include "lla_common.cuh"
 #include "lla_mixed.h"
 #include "lla_prof.h"
+#include "lla_trsm_sched.h"
 
 namespace lla {
 
@@ -175,40 +176,6 @@ constexpr int64_t kIvHelperMin = 16;  // first position whose coupling terms are
 constexpr int kIvYd = kIvNb + 2;  // words per staged column (padded: 528-byte columns)
 constexpr size_t kIvSmem = sizeof(float) * ((size_t)kIvStages * kIvNb * kIvLd + 2ull * kIvStages * kIvCols * kIvYd +
                                             2ull * kIvNb * kIvCols + 2ull * kIvCols * kIvLd);
-
-// Work items in ticket order.  Group g (g = 0 .. R-1) holds the owners of
-// processing position g (one per column chunk), then the helpers of positions
-// p = 2g+2 and 2g+3 (those with hmin <= p < R): a helper sums the coupling
-// terms q < p/2 of position p, which are all solved once position p/2 - 1 is,
-// so every item waits only on items with smaller tickets.
-__host__ __device__ __forceinline__ int64_t iv_items_before(int64_t g, int64_t R, int64_t hmin, int nch) {
-    const int64_t top = (2 * g + 1 < R - 1 ? 2 * g + 1 : R - 1) - hmin + 1;  // helpers p in [hmin, 2g+1]
-    return (int64_t)nch * (g + (top > 0 ? top : 0));
-}
-__device__ __forceinline__ void iv_decode(int64_t t, int64_t R, int64_t hmin, int nch, bool &helper,
-                                          int64_t &pos, int &chunk) {
-    int64_t lo = 0, hi = R - 1;
-    while (lo < hi) {
-        const int64_t mid = (lo + hi + 1) / 2;
-        if (iv_items_before(mid, R, hmin, nch) <= t)
-            lo = mid;
-        else
-            hi = mid - 1;
-    }
-    const int64_t idx = t - iv_items_before(lo, R, hmin, nch);
-    if (idx < nch) {
-        helper = false;
-        pos = lo;
-        chunk = (int)idx;
-        return;
-    }
-    helper = true;
-    const int64_t j = (idx - nch) / nch;
-    chunk = (int)((idx - nch) % nch);
-    int64_t p = 2 * lo + 2;
-    if (p < hmin) p = hmin;  // only 2g+3 can qualify then
-    pos = p + j;
-}
 
 // TRANS = false: L Y = B (blocks ascending); TRANS = true: L^T X = B (descending).
 // 256 threads.  The coupling tiles and the solved words of earlier blocks

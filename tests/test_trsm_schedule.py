@@ -1,0 +1,80 @@
+"""Ticket order of the FP32 substitutions (csrc/lla_trsm_sched.h), checked on the
+host with the kernel's own header: every work item is decoded exactly once, and
+every item waits only on items with smaller tickets (owners on the previous
+owners of their column chunk, which includes the two neighbours; owners on
+their helper; helpers on the owners of the positions they sum), so CTAs that
+take tickets in order can never wait on a CTA that has not been scheduled."""
+import os
+import shutil
+import subprocess
+import tempfile
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, "linfa-linalg_gb300", "csrc")
+
+HARNESS = r"""
+#include <cstdio>
+#include <map>
+#include <tuple>
+#include <vector>
+#include "lla_trsm_sched.h"
+using namespace lla;
+int main() {
+    const int64_t Rs[] = {1, 2, 3, 4, 5, 16, 17, 18, 33, 40, 100, 129, 256, 257};
+    const int nchs[] = {1, 2, 3, 4, 7};
+    const int64_t hmins[] = {2, 3, 16, 1 << 30};
+    long long checked = 0;
+    for (int64_t R : Rs)
+        for (int nch : nchs)
+            for (int64_t hmin : hmins) {
+                const int64_t total = iv_items_before(R, R, hmin, nch);
+                std::map<std::tuple<int, int64_t, int>, int64_t> seen;
+                for (int64_t t = 0; t < total; ++t) {
+                    bool helper; int64_t pos; int chunk;
+                    iv_decode(t, R, hmin, nch, helper, pos, chunk);
+                    if (pos < 0 || pos >= R || chunk < 0 || chunk >= nch || (helper && pos < hmin)) {
+                        std::printf("bad item R=%lld nch=%d hmin=%lld t=%lld\n", (long long)R, nch, (long long)hmin, (long long)t);
+                        return 1;
+                    }
+                    if (!seen.emplace(std::make_tuple((int)helper, pos, chunk), t).second) {
+                        std::printf("duplicate R=%lld t=%lld\n", (long long)R, (long long)t);
+                        return 1;
+                    }
+                }
+                const int64_t helpers = R > hmin ? R - hmin : 0;
+                if ((int64_t)seen.size() != nch * (R + helpers)) {
+                    std::printf("count R=%lld nch=%d hmin=%lld: %zu\n", (long long)R, nch, (long long)hmin, seen.size());
+                    return 1;
+                }
+                for (const auto &kv : seen) {
+                    const int helper = std::get<0>(kv.first);
+                    const int64_t p = std::get<1>(kv.first);
+                    const int c = std::get<2>(kv.first);
+                    const int64_t t = kv.second;
+                    if (helper) {  // sums the coupling terms q < p/2
+                        for (int64_t q = 0; q < p / 2; ++q)
+                            if (seen.at(std::make_tuple(0, q, c)) >= t) { std::printf("helper wait\n"); return 1; }
+                    } else {
+                        if (p > 0 && seen.at(std::make_tuple(0, p - 1, c)) >= t) { std::printf("owner wait\n"); return 1; }
+                        if (p >= hmin && seen.at(std::make_tuple(1, p, c)) >= t) { std::printf("helper order\n"); return 1; }
+                    }
+                    ++checked;
+                }
+            }
+    std::printf("ok %lld\n", checked);
+    return 0;
+}
+"""
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_ticket_order_has_no_forward_waits():
+    d = tempfile.mkdtemp(prefix="lla_sched_")
+    src, exe = os.path.join(d, "sched.cpp"), os.path.join(d, "sched")
+    with open(src, "w") as f:
+        f.write(HARNESS)
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", CSRC, src, "-o", exe], check=True, timeout=120)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.startswith("ok"), r.stdout + r.stderr
