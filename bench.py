@@ -38,6 +38,23 @@ BE_TARGET = 1e-13
 METRIC = "SPD solves/s at backward error <= 1e-13 (n=16384, 64 RHS, kappa=1e6)"
 
 
+def max_over_ranks(dist, ms, device):
+    """The slowest rank's time for the timed region (ranks are replicas, each solving
+    its own system), then a barrier so that no rank starts the next phase early."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def job_rate(world, steps, ms):
+    """Solves per second of the whole job: every rank solved `steps` systems within ms."""
+    return world * steps / (ms / 1e3)
+
+
 def mixed_update_bytes(n, nb=128):
     """FP32 trailing-matrix bytes (read + write of the lower part) of the tensor-core
     updates of one low-precision factorisation, and their launch count: panels in
@@ -362,16 +379,12 @@ def main():
         launches = lla.kernel_launches() - l0
         ms = ev[0].elapsed_time(ev[k])
         timed.per_step = [ev[i].elapsed_time(ev[i + 1]) for i in range(k)]
-        if dist:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-            dist.barrier()
+        ms = max_over_ranks(dist, ms, dev)
         return ms, launches, prof, clk.summary()
 
     k_plain = max(1, min(args.steps, args.plain_steps))
     ms_plain, _, prof_plain, _ = timed(plain_step, k_plain, min(args.warmup, 3), profile=True)
-    plain_sps = world * k_plain / (ms_plain / 1e3)
+    plain_sps = job_rate(world, k_plain, ms_plain)
     reports.clear()
     ms_mixed, launches, prof, clocks = timed(mixed_step, args.steps, args.warmup, profile=True)
     lat = sorted(timed.per_step)
@@ -379,7 +392,7 @@ def main():
                "max_ms": lat[-1], "samples": len(lat),
                "note": "per-solve CUDA-event durations of the timed steps (device-resident A, B)"}
     timed_reports = reports[-args.steps:]
-    mixed_sps = world * args.steps / (ms_mixed / 1e3)
+    mixed_sps = job_rate(world, args.steps, ms_mixed)
     assert all(r["backward_error"] <= BE_TARGET for r in timed_reports), timed_reports
     # the other residual method, timed the same way (reported beside the headline)
     alt = None
@@ -390,7 +403,7 @@ def main():
         torch.cuda.synchronize()
         be_alt = backward_error(torch, A0, Xm, B0)
         assert be_alt <= BE_TARGET and all(r["backward_error"] <= BE_TARGET for r in reports), be_alt
-        alt = {"residual": other, "value": world * args.steps / (ms_alt / 1e3), "unit": "solves/s",
+        alt = {"residual": other, "value": job_rate(world, args.steps, ms_alt), "unit": "solves/s",
                "ms_per_step": ms_alt / args.steps, "iterations": reports[-1]["iterations"],
                "backward_error": be_alt,
                "kernels": {k: {"ms": v[0] / args.steps, "launches": v[1] // args.steps}

@@ -78,3 +78,39 @@ def test_reference_arm_json_line():
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def _replica_rank(rank, world, port, outdir):
+    import torch.distributed as dist
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    try:
+        bench = load_bench()
+        ms = [10.0, 12.5, 11.0, 9.0][rank]  # this rank's timed region
+        got = bench.max_over_ranks(dist, ms, "cpu")
+        with open(os.path.join(outdir, f"rank{rank}.json"), "w") as f:
+            json.dump({"max_ms": got, "rate": bench.job_rate(world, 5, got)}, f)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_replicas_max_over_ranks_gloo():
+    """The N > 1 bench path (replicas, one process per GPU): every rank ends with the
+    slowest rank's time, and the whole-job rate counts all ranks' solves over it."""
+    import socket
+    import tempfile
+
+    import torch.multiprocessing as mp
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    outdir = tempfile.mkdtemp(prefix="lla_gloo_")
+    world = 2
+    mp.spawn(_replica_rank, args=(world, port, outdir), nprocs=world, join=True)
+    for r in range(world):
+        with open(os.path.join(outdir, f"rank{r}.json")) as f:
+            d = json.load(f)
+        assert d["max_ms"] == 12.5
+        assert abs(d["rate"] - world * 5 / 12.5e-3) < 1e-9
+    bench = load_bench()
+    assert bench.max_over_ranks(None, 7.0, "cpu") == 7.0
