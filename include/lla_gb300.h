@@ -209,11 +209,19 @@ int lla_spotrf_device(float *dA, int64_t n, int64_t ld, int algo, int64_t *d_inf
 /* Triangular solve with the lower-triangular factor L (column-major, ld):
  * trans = 0 solves L X = B, trans = 1 solves L^T X = B; dB (n x m, ldb) is
  * overwritten with X.  algo as above (EXACT follows the reference's
- * substitution order). */
+ * substitution order).  Asynchronous: a bounded device wait that gave up
+ * (X then not valid) is recorded in the calling thread's status word, which
+ * lla_device_status reports. */
 int lla_dtrsm_device(const double *dL, int64_t n, int64_t ld, int trans, double *dB, int64_t m,
                      int64_t ldb, int algo, void *stream, lla_error *err);
 int lla_strsm_device(const float *dL, int64_t n, int64_t ld, int trans, float *dB, int64_t m,
                      int64_t ldb, int algo, void *stream, lla_error *err);
+
+/* Synchronises `stream` and reports whether a bounded device wait of an
+ * asynchronous call made on this host thread (lla_?trsm_device) gave up since
+ * the last query: LLA_ERR_TIMEOUT (the X of such a call is not valid) or
+ * LLA_OK; the record is cleared.  No counterpart in the reference. */
+int lla_device_status(void *stream, lla_error *err);
 
 /* Allocation-free variant of lla_dtrsm_device (same arguments and results).
  * It has no counterpart in the reference.  It exists for callers that must
@@ -227,6 +235,13 @@ int lla_strsm_device(const float *dL, int64_t n, int64_t ld, int trans, float *d
  * array: calls that overlap on the GPU race. */
 int lla_dtrsm_device_noalloc(const double *dL, int64_t n, int64_t ld, int trans, double *dB,
                              int64_t m, int64_t ldb, int algo, void *stream, lla_error *err);
+/* Synchronises `stream` and reports LLA_ERR_TIMEOUT when a bounded wait of an
+ * lla_dtrsm_device_noalloc call on the current device gave up since the last
+ * query (that call's X is not valid), else LLA_OK; clears the record.  The
+ * record lives in the same fixed array, so it is per device, shared by all
+ * host threads; this call allocates nothing either.  No counterpart in the
+ * reference. */
+int lla_dtrsm_device_noalloc_status(void *stream, lla_error *err);
 
 
 /* ---- mixed-precision refined solve (no counterpart in the reference) -----
@@ -236,7 +251,10 @@ int lla_dtrsm_device_noalloc(const double *dL, int64_t n, int64_t ld, int trans,
  * backward error max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf +
  * ||b_j||_inf) <= tol, and a fallback to the plain FP64 factorisation when the
  * low-precision factorisation breaks down or the refinement stalls.  The FP64
- * fallback decides NotPositiveDefinite. */
+ * fallback decides NotPositiveDefinite: a failed or near-singular
+ * (pivot / a_kk < 1e-10) FMA-order factorisation is re-run in the reference's
+ * own operation order (src/cholesky.rs:51-76), whose verdict and failing row
+ * are returned, as the host-view entry points do. */
 enum lla_update {
     LLA_UPDATE_FP32 = 0,    /* FP32 SIMT trailing updates */
     LLA_UPDATE_BF16 = 1,    /* tcgen05: one BF16 term per operand, FP32 accumulation */
@@ -437,6 +455,13 @@ const char *lla_profile_kernel_name(int index);
 /* Measured arithmetic peak in TFLOP/s of this GPU: which = 0 FP64 tensor pipe
  * (mma m16n8k16 .f64), 1 FP64 FMA, 2 FP32 FMA; negative on error. */
 double lla_measure_peak_tflops(int which);
+/* Failure injection for tests of the timeout reporting: the next
+ * triangular-solve launch in this process (lla_?trsm_device,
+ * lla_dtrsm_device_noalloc or a host-view solve) loses its first block --
+ * never solved, never published -- and its bounded waits give up after
+ * `spin_limit` polls (0: the default limit of a few seconds), so the call
+ * reports LLA_ERR_TIMEOUT without faulting the device.  One shot. */
+int lla_debug_inject_lost_handoff(int64_t spin_limit);
 
 #ifdef __cplusplus
 }

@@ -137,6 +137,9 @@ EXPORTS = {
     "lla_server_release_factor": ([ctypes.c_void_p, ctypes.c_int64], ctypes.c_int),
     "lla_server_get_stats": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "lla_server_destroy": ([ctypes.c_void_p], None),
+    "lla_device_status": ([ctypes.c_void_p, _E], ctypes.c_int),
+    "lla_dtrsm_device_noalloc_status": ([ctypes.c_void_p, _E], ctypes.c_int),
+    "lla_debug_inject_lost_handoff": ([ctypes.c_int64], ctypes.c_int),
 }
 for _p in "ds":
     EXPORTS.update({
@@ -482,6 +485,23 @@ def trsm_device(L, B, trans, algo=ALGO_FAST, stream=None):
                                         _stream_ptr(stream), ctypes.byref(e))
     _raise(e)
     return B
+
+
+def device_status(stream=None):
+    """Synchronises `stream` and raises DeviceError(LLA_ERR_TIMEOUT) when a
+    bounded wait of an asynchronous device call of this thread gave up since
+    the last query (that call's result is not valid); clears the record."""
+    e = Error()
+    lib.lla_device_status(_stream_ptr(stream), ctypes.byref(e))
+    _raise(e)
+
+
+def debug_inject_lost_handoff(spin_limit=1000):
+    """Test-only: the next triangular-solve launch loses its first block and its
+    waits give up after `spin_limit` polls (see include/lla_gb300.h)."""
+    rc = lib.lla_debug_inject_lost_handoff(int(spin_limit))
+    if rc != OK:
+        raise ValueError(spin_limit)
 
 
 # ---- mixed-precision refined solve (no counterpart in the reference) --------

@@ -816,6 +816,19 @@ static int potrf_device_impl(T *dA, int64_t n, int64_t ld, int algo, int64_t *d_
     return LLA_OK;
 }
 
+// The calling thread's device-call status word (allocated and zeroed once;
+// the asynchronous device entry points record a timed-out wait there).
+static cudaError_t device_status_word(Ctx &c, cudaStream_t st, int **out) {
+    cudaError_t e = c.status_dev.ensure(sizeof(int));
+    if (e != cudaSuccess) return e;
+    if (!c.status_clear) {
+        if ((e = cudaMemsetAsync(c.status_dev.p, 0, sizeof(int), st)) != cudaSuccess) return e;
+        c.status_clear = true;
+    }
+    *out = (int *)c.status_dev.p;
+    return cudaSuccess;
+}
+
 template <typename T>
 static int trsm_device_impl(const T *dL, int64_t n, int64_t ld, int trans, T *dB, int64_t m,
                             int64_t ldb, int algo, void *stream, lla_error *err) {
@@ -830,16 +843,34 @@ static int trsm_device_impl(const T *dL, int64_t n, int64_t ld, int trans, T *dB
     LLA_TRY_CUDA(c->dev_ws.ensure(sizeof(int) * (trsm_ws_ints(n, m) + 1)));
     int *ws = (int *)c->dev_ws.p;
     int *err_word = ws + trsm_ws_ints(n, m);
+    int *sticky = nullptr;
+    LLA_TRY_CUDA(device_status_word(*c, st, &sticky));
     LLA_TRY_CUDA(cudaMemsetAsync(err_word, 0, sizeof(int), st));
     // trans = 0: L X = B (lower, processing ascending); trans = 1: L^T X = B
     LLA_TRY_CUDA(launch_status(trsm_launch<T>(dL, ld, n, trans ? 0 : 1, trans ? 1 : 0, nullptr, dB,
-                                              ldb, m, algo == LLA_ALGO_EXACT, ws, err_word, st)));
+                                              ldb, m, algo == LLA_ALGO_EXACT, ws, err_word, st, sticky)));
     return LLA_OK;
 }
 
 #define LLA_VIEW_ARGS(T) T *a, int64_t rows, int64_t cols, int64_t rs, int64_t cs
 
 extern "C" {
+
+int lla_device_status(void *stream, lla_error *err) {
+    lla__set_status(err, LLA_OK);
+    Ctx *c = get_ctx(err);
+    if (!c) return err ? err->code : LLA_ERR_NO_DEVICE;
+    cudaStream_t st = (cudaStream_t)stream;
+    LLA_TRY_CUDA(cudaStreamSynchronize(st));
+    if (!c->status_dev.p || !c->status_clear) return LLA_OK;  // nothing recorded yet
+    int word = 0;
+    LLA_TRY_CUDA(cudaMemcpyAsync(&word, c->status_dev.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    LLA_TRY_CUDA(cudaStreamSynchronize(st));
+    if (word == 0) return LLA_OK;
+    LLA_TRY_CUDA(cudaMemsetAsync(c->status_dev.p, 0, sizeof(int), st));
+    LLA_TRY_CUDA(cudaStreamSynchronize(st));
+    return lla__set_status(err, word);
+}
 
 int lla_dcholesky_inplace(LLA_VIEW_ARGS(double), int dirty, lla_error *err) {
     return cholesky_impl<double>(a, rows, cols, rs, cs, dirty, err);

@@ -36,7 +36,7 @@ struct MixedWs {
     void *stage_seen = nullptr;               // stage allocation that was last cleared
     size_t stage_seen_cap = 0;
     unsigned stage_epoch = 0;                 // epoch of the last substitution launch
-    DevBuf F, fdiag;                          // plain FP64 fallback
+    DevBuf F, fdiag, S;                       // plain FP64 fallback (S: exact-order verdict scratch)
     DevBuf opA, opB;                          // tensor-core operand planes of one panel
     DevBuf tcerr;                             // tensor-core update status word
     DevBuf pinv;                              // inverted 32 x 32 diagonal blocks of one panel
@@ -57,6 +57,8 @@ struct Ctx {
     DevBuf aux_x;                     // solution of the refined solve
     DevBuf ws;                        // triangular-solve tickets and flags
     DevBuf dev_s, dev_d, dev_ws;      // scratch of the device-resident entry points
+    DevBuf status_dev;                // device-call status word (read by lla_device_status)
+    bool status_clear = false;        // status_dev has been zeroed since its allocation
     HostBuf stage_a, stage_b;         // pinned staging for strided views
     DevBuf raw_c, lob_g, lob_p, lob_t;  // Cholesky-QR: third view, Gram copy, partials, transposes
     HostBuf stage_c;

@@ -22,10 +22,13 @@ int potrf_fast_launch(T *W, int64_t n, int64_t ld, int64_t *d_info, T *diag0, do
                       cudaStream_t st);
 
 // Triangular solve op(T) X = B in place (see lla_trsm.cu).  ws: trsm_ws_ints
-// ints of scratch; err_word: device int, 0 on entry.
+// ints of scratch; err_word: device int, 0 on entry; sticky (optional): a
+// device status word that also receives LLA_ERR_TIMEOUT and is never cleared
+// by the launch (the record that lla_device_status reads).
 template <typename T>
 int trsm_launch(const T *M, int64_t ld, int64_t n, int lower, int trans, const T *diag, T *B,
-                int64_t ldb, int64_t m, bool exact, int *ws, int *err_word, cudaStream_t st);
+                int64_t ldb, int64_t m, bool exact, int *ws, int *err_word, cudaStream_t st,
+                int *sticky = nullptr);
 size_t trsm_ws_ints(int64_t n, int64_t m);
 
 // One system of a batched solve: order n, m right-hand sides, caller index,

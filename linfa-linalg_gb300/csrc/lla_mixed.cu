@@ -459,6 +459,10 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 
 }  // namespace
 
+// Smallest pivot_k / a_kk that the FMA-order fallback factorisation accepts
+// without the exact-order re-run (the host-view entry points use the same guard).
+constexpr double kFallbackPivotGuard = 1e-10;
+
 extern "C" void lla_refine_opts_default(lla_refine_opts *o) {
     if (!o) return;
     std::memset(o, 0, sizeof(*o));
@@ -658,12 +662,26 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
         double *F = (double *)w.F.p;
         MX_TRY(cudaMemcpy2DAsync(F, sizeof(double) * n, dA, sizeof(double) * lda, sizeof(double) * n, n,
                                  cudaMemcpyDeviceToDevice, st));
+        const double big = 1e300;
         int64_t minus1 = -1;
         MX_TRY(cudaMemcpyAsync(info, &minus1, sizeof(int64_t), cudaMemcpyHostToDevice, st));
-        MX_TRY(last_err(potrf_fast_launch<double>(F, n, n, info, (double *)w.fdiag.p, nullptr, st)));
+        MX_TRY(cudaMemcpyAsync(min_ratio, &big, sizeof(double), cudaMemcpyHostToDevice, st));
+        MX_TRY(last_err(potrf_fast_launch<double>(F, n, n, info, (double *)w.fdiag.p, min_ratio, st)));
         MX_TRY(read_words(4));
         int64_t finfo;
         std::memcpy(&finfo, hw + 2, sizeof(int64_t));
+        if (finfo >= 0 || !(hw[1] >= kFallbackPivotGuard)) {
+            // A failed or near-singular FMA-order factorisation: the verdict is
+            // decided by a factorisation in the reference's own operation order
+            // (src/cholesky.rs:51-76), whose first failing row is returned.
+            MX_TRY(w.S.ensure(sizeof(double) * n * n));
+            MX_TRY(cudaMemcpy2DAsync(F, sizeof(double) * n, dA, sizeof(double) * lda, sizeof(double) * n, n,
+                                     cudaMemcpyDeviceToDevice, st));
+            MX_TRY(cudaMemcpyAsync(info, &minus1, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+            MX_TRY(last_err(potrf_exact_launch<double>(F, (double *)w.S.p, (double *)w.fdiag.p, n, n, info, st)));
+            MX_TRY(read_words(4));
+            std::memcpy(&finfo, hw + 2, sizeof(int64_t));
+        }
         if (finfo >= 0) {
             r.ms_fallback = ms_since(t0);
             if (rep) *rep = r;
@@ -681,6 +699,11 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
         MX_TRY(last_err(residual_launch(dA, lda, n, dX, ldx, dB, ldb, R, n, m, colmax_r,
                                         (double *)w.P.p, st)));
         MX_TRY(read_words(8 + 3 * m));
+        if (((int *)(hw + 3))[1] != 0) {  // a substitution's bounded wait gave up: X is not valid
+            r.ms_fallback = ms_since(t0);
+            if (rep) *rep = r;
+            return lla__set_status(err, LLA_ERR_TIMEOUT);
+        }
         double e = 0.0;
         for (int64_t j = 0; j < m; ++j) {
             const double den = hw[0] * hw[8 + m + j] + hw[8 + 2 * m + j];

@@ -23,6 +23,8 @@
 //
 // T[r, c] (logical) = trans ? M[c, r] : M[r, c]; `diag` (optional) overrides
 // the diagonal as the reference's diag_fn does (src/triangular.rs:133-144).
+#include <atomic>
+
 #include "lla_common.cuh"
 #include "lla_kernels.h"
 #include "lla_prof.h"
@@ -47,7 +49,8 @@ __global__ void __launch_bounds__(256) trsm_lookback(const T *__restrict__ M, in
                                                      int lower, int trans,
                                                      const T *__restrict__ diag, T *B, int64_t ldb,
                                                      int64_t m, int mc, int n_chunks, int *ws,
-                                                     int *err_word) {
+                                                     int *err_word, int *sticky, long long spin_limit,
+                                                     int lose_first) {
     using Ar = Arith<T>;
     __shared__ T ts[kTrsmNb][kTrsmNb + 1];
     __shared__ T xs[kTrsmMaxMc][kTrsmNb];
@@ -61,6 +64,9 @@ __global__ void __launch_bounds__(256) trsm_lookback(const T *__restrict__ M, in
         s_abort = 0;
     }
     __syncthreads();
+    // failure injection (tests only): the first item is lost -- never solved,
+    // never published -- so every wait on it runs out
+    if (lose_first && s_ticket == 0) return;
     const int64_t rb = s_ticket / n_chunks;
     const int cc = s_ticket % n_chunks;
     const int64_t col = (int64_t)cc * mc + ty;
@@ -81,8 +87,9 @@ __global__ void __launch_bounds__(256) trsm_lookback(const T *__restrict__ M, in
                     s_abort = 1;
                     break;
                 }
-                if (++spins > kSpinLimit) {
+                if (++spins > spin_limit) {
                     atomicCAS(err_word, 0, (int)LLA_ERR_TIMEOUT);
+                    if (sticky) atomicCAS(sticky, 0, (int)LLA_ERR_TIMEOUT);
                     s_abort = 1;
                     break;
                 }
@@ -151,9 +158,26 @@ __global__ void __launch_bounds__(256) trsm_lookback(const T *__restrict__ M, in
     if (tid == 0) st_release(flags + rb * n_chunks + cc, 1);
 }
 
+// One-shot failure injection for the tests of timeout reporting
+// (lla_debug_inject_lost_handoff): the next triangular-solve launch loses its
+// first item and its waits give up after the armed number of polls.
+static std::atomic<long long> g_inject_spin{-1};  // -1: nothing armed
+
+struct TrsmWaitCfg {
+    long long spin_limit;
+    int lose_first;
+};
+
+static TrsmWaitCfg take_wait_cfg() {
+    const long long s = g_inject_spin.exchange(-1);
+    if (s < 0) return {kSpinLimit, 0};
+    return {s > 0 ? s : kSpinLimit, 1};
+}
+
 template <typename T>
 int trsm_launch(const T *M, int64_t ld, int64_t n, int lower, int trans, const T *diag, T *B,
-                int64_t ldb, int64_t m, bool exact, int *ws, int *err_word, cudaStream_t st) {
+                int64_t ldb, int64_t m, bool exact, int *ws, int *err_word, cudaStream_t st,
+                int *sticky) {
     if (n == 0 || m == 0) return 0;
     const int mc = (int)std::min<int64_t>(kTrsmMaxMc, m);
     const int64_t chunks = ceil_div(m, mc);
@@ -161,14 +185,17 @@ int trsm_launch(const T *M, int64_t ld, int64_t n, int lower, int trans, const T
     if (cudaMemsetAsync(ws, 0, sizeof(int) * (1 + R * chunks), st) != cudaSuccess) return -1;
     const dim3 block(kTrsmNb, mc);
     const unsigned grid = (unsigned)(R * chunks);
+    const TrsmWaitCfg wc = take_wait_cfg();
     // algorithmic work: n^2 * m flops (n(n-1)/2 multiply-adds and n divisions per column)
     LaunchScope ls(K_TRSM, st, (double)n * n * m);
     if (exact)
         trsm_lookback<T, true><<<grid, block, 0, st>>>(M, ld, n, lower, trans, diag, B, ldb, m, mc,
-                                                       (int)chunks, ws, err_word);
+                                                       (int)chunks, ws, err_word, sticky,
+                                                       wc.spin_limit, wc.lose_first);
     else
         trsm_lookback<T, false><<<grid, block, 0, st>>>(M, ld, n, lower, trans, diag, B, ldb, m,
-                                                        mc, (int)chunks, ws, err_word);
+                                                        mc, (int)chunks, ws, err_word, sticky,
+                                                        wc.spin_limit, wc.lose_first);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -179,9 +206,9 @@ size_t trsm_ws_ints(int64_t n, int64_t m) {
 }
 
 template int trsm_launch<double>(const double *, int64_t, int64_t, int, int, const double *,
-                                 double *, int64_t, int64_t, bool, int *, int *, cudaStream_t);
+                                 double *, int64_t, int64_t, bool, int *, int *, cudaStream_t, int *);
 template int trsm_launch<float>(const float *, int64_t, int64_t, int, int, const float *, float *,
-                                int64_t, int64_t, bool, int *, int *, cudaStream_t);
+                                int64_t, int64_t, bool, int *, int *, cudaStream_t, int *);
 
 }  // namespace lla
 
@@ -201,12 +228,15 @@ template int trsm_launch<float>(const float *, int64_t, int64_t, int, int, const
 // names a stand-in object); the device address is obtained once per device
 // with cudaGetSymbolAddress, on the first call made while that device is
 // current, and cached.  That first call therefore also does the set-up and
-// should come before any stream capture.
+// should come before any stream capture.  The cache is not refreshed after a
+// cudaDeviceReset (which unloads the module), so the entry point must not be
+// used across a device reset.
 //
 // All calls share the one array and it keeps the last call's contents: each
 // call clears the part it uses before its launch, and calls whose work
 // overlaps on the GPU (different streams, or different host threads without
-// ordering) race on it.
+// ordering) race on it.  A bounded wait that gives up is recorded in the
+// array's status word, which lla_dtrsm_device_noalloc_status reads and clears.
 
 #include <mutex>
 
@@ -214,8 +244,11 @@ namespace lla {
 
 constexpr int kNoAllocMaxFlags = 1 << 16;  // row blocks x RHS chunks
 constexpr int kNoAllocMaxDevices = 64;
-// [0] ticket counter, [1 .. kNoAllocMaxFlags] flags, [kNoAllocMaxFlags + 1] error word
-static __device__ __align__(256) int g_trsm_noalloc_scratch[kNoAllocMaxFlags + 2];
+// [0] ticket counter, [1 .. kNoAllocMaxFlags] flags, [kNoAllocMaxFlags + 1]
+// error word of the current call, [kNoAllocMaxFlags + 2] status word (kept
+// until lla_dtrsm_device_noalloc_status clears it)
+constexpr int kNoAllocErr = kNoAllocMaxFlags + 1, kNoAllocStatus = kNoAllocMaxFlags + 2;
+static __device__ __align__(256) int g_trsm_noalloc_scratch[kNoAllocMaxFlags + 3];
 
 static std::mutex g_noalloc_mu;
 static int *g_noalloc_addr[kNoAllocMaxDevices] = {};
@@ -255,24 +288,56 @@ extern "C" int lla_dtrsm_device_noalloc(const double *dL, int64_t n, int64_t ld,
     cudaError_t e = noalloc_scratch(&scratch);
     if (e != cudaSuccess) return lla__set_cuda_error(err, e);
     cudaStream_t st = (cudaStream_t)stream;
-    int *err_word = scratch + kNoAllocMaxFlags + 1;
+    int *err_word = scratch + kNoAllocErr;
     e = cudaMemsetAsync(scratch, 0, sizeof(int) * (size_t)(1 + R * chunks), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(err_word, 0, sizeof(int), st);
     if (e != cudaSuccess) return lla__set_cuda_error(err, e);
-    prof_note_launch();
     const dim3 block(kTrsmNb, mc);
     const unsigned grid = (unsigned)(R * chunks);
     // trans = 0: L X = B (lower, ascending); trans = 1: L^T X = B (descending)
     const int lower = trans ? 0 : 1;
-    if (algo == LLA_ALGO_EXACT)
-        trsm_lookback<double, true><<<grid, block, 0, st>>>(dL, ld, n, lower, trans ? 1 : 0,
-                                                            nullptr, dB, ldb, m, mc, (int)chunks,
-                                                            scratch, err_word);
-    else
-        trsm_lookback<double, false><<<grid, block, 0, st>>>(dL, ld, n, lower, trans ? 1 : 0,
-                                                             nullptr, dB, ldb, m, mc, (int)chunks,
-                                                             scratch, err_word);
+    const TrsmWaitCfg wc = take_wait_cfg();
+    {
+        // counted and timed like the allocating entry point's launches
+        LaunchScope ls(K_TRSM, st, (double)n * n * m);
+        if (algo == LLA_ALGO_EXACT)
+            trsm_lookback<double, true><<<grid, block, 0, st>>>(
+                dL, ld, n, lower, trans ? 1 : 0, nullptr, dB, ldb, m, mc, (int)chunks, scratch, err_word,
+                scratch + kNoAllocStatus, wc.spin_limit, wc.lose_first);
+        else
+            trsm_lookback<double, false><<<grid, block, 0, st>>>(
+                dL, ld, n, lower, trans ? 1 : 0, nullptr, dB, ldb, m, mc, (int)chunks, scratch, err_word,
+                scratch + kNoAllocStatus, wc.spin_limit, wc.lose_first);
+    }
     e = cudaGetLastError();
     if (e != cudaSuccess) return lla__set_cuda_error(err, e);
+    return LLA_OK;
+}
+
+// Synchronises `stream`, reads the status word that the allocation-free
+// solves on the current device share, and clears it.  Allocates nothing.
+extern "C" int lla_dtrsm_device_noalloc_status(void *stream, lla_error *err) {
+    using namespace lla;
+    lla__set_status(err, LLA_OK);
+    int *scratch = nullptr;
+    cudaError_t e = noalloc_scratch(&scratch);
+    if (e != cudaSuccess) return lla__set_cuda_error(err, e);
+    cudaStream_t st = (cudaStream_t)stream;
+    int word = 0;
+    e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&word, scratch + kNoAllocStatus, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess && word != 0) e = cudaMemsetAsync(scratch + kNoAllocStatus, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return lla__set_cuda_error(err, e);
+    return word ? lla__set_status(err, word) : LLA_OK;
+}
+
+// Arms the one-shot failure injection of the next triangular-solve launch
+// (tests of timeout reporting only).
+extern "C" int lla_debug_inject_lost_handoff(int64_t spin_limit) {
+    if (spin_limit < 0) return LLA_ERR_INVALID_ARG;
+    lla::g_inject_spin.store((long long)spin_limit);
     return LLA_OK;
 }

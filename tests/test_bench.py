@@ -74,7 +74,12 @@ def test_reference_arm_json_line():
     assert line["steps"] == 1 and line["warmup"] == 1 and line["n_gpus"] == 1
     assert line["config"]["workload"].startswith("single SPD solve n=16384")
     cb = line["cpu_baseline"]
-    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == line["value"]
+    # the reference is single-threaded: one pinned core, and the n = 16384 figure is
+    # extrapolated from the directly timed sample
+    assert cb["kind"] in ("port", "reference") and cb["cores"] == 1 and cb["value"] == line["value"]
+    assert line["extrapolated"] is True and cb["extrapolated"] is True
+    assert line["measured"]["n"] == 192 and line["measured"]["nrhs"] == 64
+    assert abs(line["ms_per_step"] - 1000 * line["measured"]["seconds_median"]) < 1e-6
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0

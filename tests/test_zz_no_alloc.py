@@ -73,3 +73,55 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(gpu_lla):
     assert fn(dummy.data_ptr(), n, n, 0, dummy.data_ptr(), 1, n, 1, None, None) == TOO_LARGE
     assert fn(dummy.data_ptr(), 1024, 1024, 0, dummy.data_ptr(), 8 * 2049, 1024, 1, None,
               None) == TOO_LARGE
+
+
+def test_noalloc_uses_every_flag(gpu_lla):
+    """Exactly 65,536 flags (32 row blocks x 2,048 RHS chunks of 8): accepted,
+    and the last flag, next to the array's status words, is used correctly."""
+    torch = pytest.importorskip("torch")
+    lib = ctypes.CDLL(gpu_lla.LIB_PATH)
+    ref_fn, noalloc_fn = _fn(lib, "lla_dtrsm_device"), _fn(lib, "lla_dtrsm_device_noalloc")
+    rng = np.random.default_rng(65536)
+    n, m = 1024, 8 * 2048
+    g = rng.standard_normal((n, n))
+    L = torch.linalg.cholesky(torch.tensor(g @ g.T / n + np.eye(n), device="cuda"))
+    Lc = L.T.contiguous().T
+    B = torch.randn(m, n, dtype=torch.float64, device="cuda").T  # column-major, ld = n
+    stream = torch.cuda.current_stream().cuda_stream
+    X_ref, X_new = B.clone(), B.clone()
+    assert ref_fn(Lc.data_ptr(), n, n, 0, X_ref.data_ptr(), m, n, 1, stream, None) == 0
+    assert noalloc_fn(Lc.data_ptr(), n, n, 0, X_new.data_ptr(), m, n, 1, stream, None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(X_ref, X_new)
+    st = lib.lla_dtrsm_device_noalloc_status
+    st.argtypes, st.restype = [ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int
+    assert st(stream, None) == 0
+
+
+def test_noalloc_reports_a_lost_handoff(gpu_lla):
+    """A bounded wait that gives up (the injected lost hand-off: a flag that
+    nothing sets) is reported by lla_dtrsm_device_noalloc_status, which also
+    clears it; the next call is correct again."""
+    torch = pytest.importorskip("torch")
+    lib = ctypes.CDLL(gpu_lla.LIB_PATH)
+    fn = _fn(lib, "lla_dtrsm_device_noalloc")
+    st = lib.lla_dtrsm_device_noalloc_status
+    st.argtypes, st.restype = [ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int
+    rng = np.random.default_rng(19)
+    n, m = 2048, 8
+    g = rng.standard_normal((n, n))
+    L = torch.linalg.cholesky(torch.tensor(g @ g.T / n + np.eye(n), device="cuda"))
+    Lc = L.T.contiguous().T
+    B = torch.tensor(rng.standard_normal((n, m)), device="cuda").T.contiguous().T
+    stream = torch.cuda.current_stream().cuda_stream
+    assert st(stream, None) == 0
+    gpu_lla.debug_inject_lost_handoff(2000)
+    X = B.clone()
+    assert fn(Lc.data_ptr(), n, n, 0, X.data_ptr(), m, n, 2, stream, None) == 0
+    assert st(stream, None) == 19  # LLA_ERR_TIMEOUT
+    assert st(stream, None) == 0
+    X = B.clone()
+    assert fn(Lc.data_ptr(), n, n, 0, X.data_ptr(), m, n, 2, stream, None) == 0
+    assert st(stream, None) == 0
+    r = np.tril(L.cpu().numpy()) @ X.cpu().numpy() - B.cpu().numpy()
+    assert np.abs(r).max() <= 1e-10 * np.abs(B.cpu().numpy()).max()
