@@ -102,22 +102,30 @@ def _cpu_sample(args):
     return dt
 
 
-def cpu_rate(n_sample, m, workers, seed=1):
-    """Solves/s of the oracle on `workers` processes (one solve each),
-    scaled from n_sample to the n = 16384 system by the flop model."""
-    import multiprocessing as mp
-    if workers <= 1:
+class OneCore:
+    """Pins the calling process to one host core (the reference is
+    single-threaded) and restores its affinity afterwards."""
+
+    def __enter__(self):
+        self.prev = None
+        if hasattr(os, "sched_getaffinity"):
+            self.prev = os.sched_getaffinity(0)
+            os.sched_setaffinity(0, {min(self.prev)})
+        return self
+
+    def __exit__(self, *a):
+        if self.prev is not None:
+            os.sched_setaffinity(0, self.prev)
+
+
+def cpu_rate(n_sample, m, seed=1):
+    """The oracle's single-core solve of an n_sample system with m right-hand
+    sides, timed directly; returns (seconds, solves/s of the n = 16384 system
+    extrapolated from it by the flop model n^3/3 + 2 n^2 m)."""
+    with OneCore():
         dt = _cpu_sample((n_sample, m, seed))
-        rate_sample = 1.0 / dt
-    else:
-        # concurrent independent solves; each worker times its own solve only
-        ctx = mp.get_context("spawn")
-        with ctx.Pool(workers) as pool:
-            dts = pool.map(_cpu_sample, [(n_sample, m, seed + i) for i in range(workers)])
-        rate_sample = sum(1.0 / d for d in dts)
-        dt = max(dts)
     scale = flops_solve(n_sample, m) / flops_solve(N_DEFAULT, NRHS_DEFAULT)
-    return rate_sample * scale, dt
+    return dt, scale / dt
 
 
 def run_cpu_sweep(args):
@@ -126,10 +134,11 @@ def run_cpu_sweep(args):
     from oracle import oracle as ora
     ora.lib()
     rows = []
-    for n, m in [(512, 1), (512, 64), (1024, 64), (2048, 64), (4096, 64)]:
-        dt = _cpu_sample((n, m, 7))
-        rows.append({"n": n, "nrhs": m, "seconds": dt, "solves_per_s": 1.0 / dt,
-                     "gflops": flops_solve(n, m) / dt / 1e9})
+    with OneCore():
+        for n, m in [(512, 1), (512, 64), (1024, 64), (2048, 64), (4096, 64)]:
+            dt = _cpu_sample((n, m, 7))
+            rows.append({"n": n, "nrhs": m, "seconds": dt, "solves_per_s": 1.0 / dt,
+                         "gflops": flops_solve(n, m) / dt / 1e9})
     # n^3 fit of the largest timed size, for the sizes not timed directly
     big = rows[-1]
     extrap = {str(n): big["seconds"] * flops_solve(n, NRHS_DEFAULT) / flops_solve(big["n"], 64)
@@ -140,32 +149,42 @@ def run_cpu_sweep(args):
 
 
 def run_reference(args):
+    """The reference's CPU algorithm (the oracle: a loop-for-loop C restatement
+    of linfa-linalg's solvec, single-threaded like the reference), pinned to one
+    host core.  Each timed step is one complete solve of an n = 4096, 64-RHS
+    SPD system, the largest sample that keeps the run within a few minutes; the
+    n = 16384 rate is extrapolated from it by the flop model and marked so."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from oracle import oracle as ora
     ora.lib()  # builds the oracle if needed
-    workers = os.cpu_count() or 1
-    n_s = args.ref_sample_n
-    m = NRHS_DEFAULT
-    for _ in range(args.warmup):
-        cpu_rate(n_s, m, workers)
-    rates, secs = [], []
-    for _ in range(args.steps):
-        r, dt = cpu_rate(n_s, m, workers)
-        rates.append(r)
-        secs.append(dt)
-    value = statistics.median(rates)
+    n_s, m = args.ref_sample_n, NRHS_DEFAULT
+    for i in range(args.warmup):  # the C code has no JIT; a short solve pages it in
+        _cpu_sample((min(n_s, 1024), m, 100 + i))
+    secs = [cpu_rate(n_s, m, seed=1 + i)[0] for i in range(args.steps)]
+    sec = statistics.median(secs)
+    scale = flops_solve(n_s, m) / flops_solve(N_DEFAULT, NRHS_DEFAULT)
+    value = scale / sec
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * statistics.median(secs), "higher_is_better": True,
+        "ms_per_step": 1000.0 * sec, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "extrapolated": True,
         "config": {"workload": f"single SPD solve n={N_DEFAULT} nrhs={NRHS_DEFAULT} kappa=1e6",
-                   "sample": f"solvec n={n_s} nrhs={m} per process, A = G G^T/n + I"},
-        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": workers, "kind": "port",
-                         "sample": f"{workers} concurrent oracle solvec n={n_s} m={m}, "
-                                   f"scaled by (n^3/3+2n^2m) to n={N_DEFAULT}"},
+                   "sample": f"one solvec of n={n_s} nrhs={m} per step (A = G G^T/n + I), 1 core; "
+                             f"warm-up steps at n={min(n_s, 1024)}"},
+        "measured": {"n": n_s, "nrhs": m, "seconds_median": sec, "seconds": secs,
+                     "solves_per_s": 1.0 / sec, "gflops": flops_solve(n_s, m) / sec / 1e9},
+        "extrapolation": f"solves/s at n={N_DEFAULT}, m={NRHS_DEFAULT} = measured rate at n={n_s} x "
+                         f"(n^3/3 + 2 n^2 m at n={n_s}) / (the same at n={N_DEFAULT}) = x{scale:.3e}",
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": 1, "kind": "port",
+                         "extrapolated": True,
+                         "sample": f"oracle solvec n={n_s} m={m} on 1 pinned core, median of "
+                                   f"{args.steps}; n^3 fit to n={N_DEFAULT}",
+                         "cpu": platform.processor() or platform.machine(),
+                         "host_cores": os.cpu_count()},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -258,6 +277,82 @@ def backward_error(torch, A, X, B):
     return float((num / den).max())
 
 
+def roofline_of(kern, prof, args, n, m, hbm, bf16, fp64_peak, ffma_peak, peak_note, ms_step):
+    """Roofline of one kernel of the headline solve from its live CUDA-event time
+    and its ALGORITHMIC work per launch (the flops and bytes the operation needs,
+    not what the implementation executes).  The bound is the roofline whose floor
+    (work / peak) is the larger for that work; `frac` = that floor / the measured
+    time.  Executed-work figures (term products on the tensor pipe) are reported
+    beside it, never as `frac`."""
+    k_ms, k_n, k_work = prof[kern]
+    sec = k_ms * 1e-3
+    out = {"kernel": kern, "launches": k_n, "avg_launch_ms": k_ms / max(k_n, 1),
+           "share_of_step": k_ms / ms_step, "peak_source": peak_note}
+    if kern == "mixed_update":
+        # per solve: n^3/3 flops (one product per term, the algorithmic update) against
+        # the FP32 trailing matrix's read + write, m(m+1)/2 * 8 bytes per K = 256 pass
+        # of the panel-pair schedule: 64 flop/B, below the ridge (bf16 peak / HBM, about
+        # 280 flop/B), so HBM bounds the algorithmic work
+        upd_bytes, upd_launches = mixed_update_bytes(n)
+        solves = k_n / upd_launches
+        flops, byts = k_work, upd_bytes * solves
+        products = {"bf16": 1, "fp16": 1, "bf16x3": 3, "fp16x3": 3, "bf16x6": 6}.get(args.update, 1)
+        out.update({"tensor_pipe_tflops": products * flops / sec / 1e12,
+                    "tensor_pipe_frac": products * flops / sec / 1e12 / bf16,
+                    "tensor_products": products,
+                    "note": "frac: algorithmic bytes (FP32 trailing matrix read + write of the pair schedule) "
+                            "over the measured copy bandwidth; flop_frac: n^3/3 flops over the bf16 burst; "
+                            "tensor_pipe_frac: executed term products over the bf16 burst"})
+        fpeak, funit = bf16, "TFLOP/s (bf16 tensor)"
+    elif kern == "mixed_trsm":
+        # FP32 substitutions: n^2 m flops per launch against the lower triangle of the
+        # FP32 factor (2 n^2 bytes) and B (read + write, 8 n m): m/2 flop/B, above the
+        # FFMA ridge (FFMA peak / HBM, about 11 flop/B), so FP32 FFMA bounds them
+        nsub = max(1, k_n - 2 * args.steps)  # minus the per-factor inverse and coupling kernels
+        flops, byts = k_work, nsub * (2.0 * n * n + 16.0 * n * m)
+        fpeak, funit = ffma_peak, "TFLOP/s (FP32 FMA, measured live)"
+        out["note"] = "substitution launches only; flops n^2 m per launch"
+    elif kern == "residual":
+        # R = B - A X in FP64 accuracy: 2 n^2 m flops, the lower triangle of A (4 n^2 bytes)
+        flops, byts = k_work, k_n * (4.0 * n * n + 24.0 * n * m)
+        if args.residual == "slices":
+            fpeak, funit = bf16, "TFLOP/s (bf16 tensor; FP64-equivalent flops)"
+            out.update({"tensor_pipe_tflops": 36 * flops / sec / 1e12,
+                        "tensor_pipe_frac": 36 * flops / sec / 1e12 / bf16})
+        else:
+            fpeak, funit = fp64_peak, "TFLOP/s (FP64 tensor pipe, measured live)"
+    else:
+        flops, byts = k_work, None
+        fpeak, funit = ffma_peak, "TFLOP/s (FP32 FMA, measured live)"
+    t_flop = flops / (fpeak * 1e12) if fpeak and fpeak > 0 else 0.0
+    t_byte = byts / (hbm * 1e9) if byts else 0.0
+    if t_byte >= t_flop and byts:
+        out.update({"bound": "hbm", "achieved": byts / sec / 1e9, "peak": hbm, "unit": "GB/s",
+                    "frac": t_byte / sec, "algorithmic_bytes_per_launch": byts / k_n})
+    else:
+        out.update({"bound": "tensor" if "tensor" in funit else "fp32-fma", "achieved": flops / sec / 1e12,
+                    "peak": fpeak, "unit": funit.split(" (")[0], "peak_kind": funit, "frac": t_flop / sec})
+        if byts:
+            out["algorithmic_bytes_per_launch"] = byts / k_n
+    out["flop_frac"] = flops / sec / 1e12 / fpeak if fpeak and fpeak > 0 else None
+    out["flop_peak_kind"] = funit
+    if byts:
+        out["hbm_frac"] = byts / sec / 1e9 / hbm
+    # DRAM traffic of one ncu-captured launch, scaled to this workload's launches
+    tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    key = "residual_slices" if kern == "residual" and args.residual == "slices" else kern
+    t = json.load(open(tpath)).get(key) if os.path.exists(tpath) else None
+    out["traffic"], out["traffic_source"] = None, None
+    if t and "algorithmic_bytes" in t and out.get("algorithmic_bytes_per_launch"):
+        ratio = t["dram_bytes"] / t["algorithmic_bytes"]
+        out["traffic"] = ratio * out["algorithmic_bytes_per_launch"]
+        out["traffic_source"] = f"{t['source']} (DRAM/algorithmic = {ratio:.2f})"
+    elif t and "n_captured" in t:
+        out["traffic"] = t["dram_bytes"] * (n / t["n_captured"]) ** t["exponent"]
+        out["traffic_source"] = f"{t['source']}, scaled from n={t['n_captured']} by (n/{t['n_captured']})^{t['exponent']}"
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -266,7 +361,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--nrhs", type=int, default=NRHS_DEFAULT)
-    ap.add_argument("--ref-sample-n", type=int, default=2048)
+    ap.add_argument("--ref-sample-n", type=int, default=4096)
     ap.add_argument("--cpu-sample-n", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI leg")
@@ -282,7 +377,11 @@ def main():
     ap.add_argument("--batch-count", type=int, default=10000)
     ap.add_argument("--batch-dtype", default="f64", choices=["f64", "f32"])
     ap.add_argument("--serve-requests", type=int, default=400)
-    ap.add_argument("--serve-rates", default="25,50,100", help="Poisson arrival rates (requests/s)")
+    ap.add_argument("--serve-rates", default="100,200,400,800", help="Poisson arrival rates (requests/s)")
+    ap.add_argument("--serve-rate", type=float, default=200.0,
+                    help="arrival rate of the serving leg of the default run (requests/s)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched leg of the default run")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg of the default run")
     args = ap.parse_args()
     if args.workload == "cpu-sweep":
         run_cpu_sweep(args)
@@ -319,9 +418,9 @@ def main():
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as ora
         ora.lib()
-        rate, dt = cpu_rate(args.cpu_sample_n, m, 1)
-        cpu = {"value": rate, "unit": "solves/s", "cores": 1, "kind": "port",
-               "sample": f"oracle solvec n={args.cpu_sample_n} m={m} on 1 core took {dt:.2f} s; "
+        dt, rate = cpu_rate(args.cpu_sample_n, m)
+        cpu = {"value": rate, "unit": "solves/s", "cores": 1, "kind": "port", "extrapolated": True,
+               "sample": f"oracle solvec n={args.cpu_sample_n} m={m} on 1 pinned core took {dt:.2f} s; "
                          f"scaled by (n^3/3+2n^2m) to n={n}"}
 
     A0, B0 = make_system(torch, n, m, KAPPA_DEFAULT, SEED + rank, dev)
@@ -417,59 +516,12 @@ def main():
     hbm = peaks.get("hbm_gbs", 6800.0)
     bf16 = peaks.get("bf16_tflops", 1900.0)
     peak_note = "MEASURED_PEAKS.json" if peaks else "fallback (6.8 TB/s, 1.9 PF/s)"
+    ffma_peak = lla.measure_peak_tflops(2)
     dom = max(prof, key=lambda k: prof[k][0])
-    dom_ms, dom_n, dom_work = prof[dom]
-    sec = dom_ms * 1e-3
-    extra = {}
-    if dom == "mixed_update":
-        # Panels in pairs: per pair a narrow launch (K = 128, one 128-column block) and
-        # one K = 256 launch over the rest of the trailing matrix.  Per 128 x 128 tile the
-        # term products execute products * 2 * 128^2 * K tensor flops against 128 KB of
-        # FP32 read + write (384 flop/B for bf16x6 at K = 256, above the ridge point
-        # bf16 peak / HBM), so the tensor pipe is the roofline; the HBM side is reported
-        # beside it from the exact bytes of the pair schedule.
-        products = {"bf16": 1, "fp16": 1, "bf16x3": 3, "fp16x3": 3, "bf16x6": 6}.get(args.update, 1)
-        upd_bytes, upd_launches = mixed_update_bytes(n)
-        solves = dom_n / upd_launches
-        bound, unit, achieved, peak = "tensor", "TFLOP/s", products * dom_work / sec / 1e12, bf16
-        extra = {"algorithmic_bytes_per_launch": upd_bytes / upd_launches,
-                 "tensor_products": products,
-                 "hbm_gbs": upd_bytes * solves / sec / 1e9,
-                 "hbm_frac": upd_bytes * solves / sec / 1e9 / hbm,
-                 "note": "executed tensor flops (term products x 2 x lower-tile MACs) over the burst bf16 "
-                         "peak; clocks stayed at the maximum SM clock"}
-    elif dom == "mixed_trsm":
-        # two substitutions per iteration: each reads the FP32 factor's lower triangle once
-        nsub = max(1, dom_n - 2 * args.steps)  # minus the per-factor inverse and coupling kernels
-        alg = nsub * (2.0 * n * n + 16.0 * n * m)
-        bound, unit, achieved, peak = "hbm", "GB/s", alg / sec / 1e9, hbm
-        extra = {"algorithmic_bytes_per_launch": alg / nsub}
-    elif dom == "residual" and args.residual == "slices":
-        # 36 slice-pair products of 2 n^2 m each on the BF16 tensor cores; the eight
-        # BF16 slice planes of A (16 n^2 bytes) stream from HBM once per launch
-        bound, unit, achieved, peak = "tensor", "TFLOP/s", 36 * dom_work / sec / 1e12, bf16
-        extra = {"fp64_equivalent_tflops": dom_work / sec / 1e12,
-                 "algorithmic_bytes_per_launch": 16.0 * n * n}
-    else:
-        bound, unit, achieved, peak = "fp64-tensor", "TFLOP/s", dom_work / sec / 1e12, fp64_peak
-        peak_note = "measured live: 8 independent mma.sync m16n8k16 f64 per step on all SMs"
-    traffic, traffic_src = None, None
-    tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    if os.path.exists(tpath):
-        t = json.load(open(tpath)).get("residual_slices" if dom == "residual" and args.residual == "slices"
-                                        else dom)
-        if t and "algorithmic_bytes" in t and "algorithmic_bytes_per_launch" in extra:
-            # DRAM bytes / algorithmic bytes of one captured launch, applied to this workload's launches
-            traffic = t["dram_bytes"] / t["algorithmic_bytes"] * extra["algorithmic_bytes_per_launch"]
-            traffic_src = f"{t['source']} (DRAM/algorithmic = {t['dram_bytes'] / t['algorithmic_bytes']:.2f})"
-        elif t:
-            traffic = t["dram_bytes"] * (n / t["n_captured"]) ** t["exponent"]
-            traffic_src = f"{t['source']}, scaled from n={t['n_captured']} by (n/{t['n_captured']})^{t['exponent']}"
-    roofline = {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
-                "frac": achieved / peak if peak and peak > 0 else None,
-                "traffic": traffic, "traffic_source": traffic_src,
-                "share_of_step": dom_ms / ms_mixed, "avg_launch_ms": dom_ms / dom_n,
-                "peak_source": peak_note, **{k: v for k, v in extra.items() if v is not None}}
+    roofline = roofline_of(dom, prof, args, n, m, hbm, bf16, fp64_peak, ffma_peak, peak_note, ms_mixed)
+    roofline_others = {k: roofline_of(k, prof, args, n, m, hbm, bf16, fp64_peak, ffma_peak, peak_note, ms_mixed)
+                       for k in ("mixed_update", "mixed_trsm", "residual", "mixed_diag", "mixed_panel")
+                       if k in prof and k != dom}
 
     # end to end through the C ABI with host (pinned) buffers: lla_dposv_refined reads A
     # and overwrites B with X
@@ -492,6 +544,18 @@ def main():
         e2e = {"value": k_e2e / tot, "unit": "solves/s",
                "h2d_bytes_per_step": (n * n + n * m) * 8, "d2h_bytes_per_step": n * m * 8,
                "path": "lla_dposv_refined: pinned host row-major A (read) and B (overwritten by X)"}
+
+    # the batched and serving configurations, measured in the same run (rank 0)
+    batch = serve = None
+    if rank == 0 and not args.no_batch:
+        batch = {dtn: measure_batch(torch, lla, dev, args.batch_count, dtn, max(3, min(args.steps, 10)),
+                                    max(3, args.warmup), cpu_sample=0 if args.no_cpu else 200)
+                 for dtn in ("f64", "f32")}
+    if rank == 0 and not args.no_serve:
+        rng = np.random.default_rng(SEED)
+        pool, tri = serve_pools(torch, dev, rng)
+        serve = measure_serve(torch, lla, dev, pool, tri, rng, args.serve_rate, args.serve_requests)
+        del pool, tri
 
     if rank == 0:
         rep = timed_reports[-1]
@@ -517,9 +581,11 @@ def main():
             "mixed_over_plain": mixed_sps / plain_sps,
             "other_residual": alt,
             "gflops": flops_solve(n, m) * mixed_sps / 1e9,
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "roofline": roofline, "roofline_other_kernels": roofline_others,
+            "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": launches,
             "kernels": {k: {"ms": v[0], "launches": v[1], "work": v[2]} for k, v in prof.items()},
+            "batch": batch, "serve": serve,
         }
         print(json.dumps(out))
     if dist:
@@ -545,16 +611,27 @@ def make_batch(torch, count, seed, device, dtype):
     return n, m, As, Bs
 
 
-def run_batch(args):
-    import torch
-    import __graft_entry__
-    lla = __graft_entry__.load_package()
-    dev = torch.device("cuda", 0)
-    torch.cuda.set_device(dev)
-    dt = torch.float64 if args.batch_dtype == "f64" else torch.float32
-    count = args.batch_count
+def batch_backward_errors(torch, plan, n, m, As, Bs, dX, dt):
+    """Normwise backward error / (n eps) of EVERY system of the batch, computed
+    here in FP64 from the caller's copies of A_i and B_i."""
+    eps = float(torch.finfo(dt).eps)
+    vals = []
+    for i in range(len(n)):
+        x = dX[plan.b_off[i]:plan.b_off[i] + n[i] * m[i]].reshape(int(m[i]), int(n[i])).T.double()
+        a, b = As[i].double(), Bs[i].double()
+        r = b - a @ x
+        be = (r.abs().amax(0) / (a.abs().sum(1).amax() * x.abs().amax(0) + b.abs().amax(0))).amax()
+        vals.append(be / (float(n[i]) * eps))
+    return float(torch.stack(vals).max())
+
+
+def measure_batch(torch, lla, dev, count, dtname, steps, warmup, cpu_sample=0):
+    """The batched configuration: `count` systems, n log-uniform in [16, 256],
+    A = G G^T / n + 0.1 I, 1..8 RHS; one persistent launch replayed from a CUDA
+    graph per step (pools restored outside the events; pools > L2)."""
+    dt = torch.float64 if dtname == "f64" else torch.float32
     n, m, As, Bs = make_batch(torch, count, SEED, dev, dt)
-    plan = lla.BatchPlan(n, m, args.batch_dtype)
+    plan = lla.BatchPlan(n, m, dtname)
     A0 = torch.zeros(plan.a_elems, dtype=dt, device=dev)
     B0 = torch.zeros(plan.b_elems, dtype=dt, device=dev)
     for i in range(count):
@@ -564,71 +641,84 @@ def run_batch(args):
     info = torch.empty(count, dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream()
     tune_ms = plan.autotune(dA, dB, info, stream=stream)
-    # correctness: every system against its own FP64 backward error bound
+    # correctness: every system against the per-matrix FP64 class, 10 n eps
+    dA.copy_(A0)
+    dB.copy_(B0)
     plan.solve_graph(dA, dB, info, stream=stream)
     torch.cuda.synchronize()
     assert int((info != -1).sum()) == 0
-    eps = float(torch.finfo(dt).eps)
-    worst = 0.0
-    for i in range(0, count, max(1, count // 500)):
-        x = dB[plan.b_off[i]:plan.b_off[i] + n[i] * m[i]].reshape(int(m[i]), int(n[i])).T.double()
-        a, b = As[i].double(), Bs[i].double()
-        r = b - a @ x
-        be = float((r.abs().amax(0) / (a.abs().sum(1).amax() * x.abs().amax(0) + b.abs().amax(0))).max())
-        worst = max(worst, be / (n[i] * eps))
+    worst = batch_backward_errors(torch, plan, n, m, As, Bs, dB, dt)
     assert worst <= 10.0, worst
-    # timed: restore the pools (device copies, outside the events) and replay the graph
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     total = 0.0
     l0 = lla.kernel_launches()
     lla.profile_start()
-    with Clocks(0) as clk:
-        for it in range(args.warmup + args.steps):
+    with Clocks(dev.index or 0) as clk:
+        for it in range(warmup + steps):
             dA.copy_(A0)
             dB.copy_(B0)
             e0.record(stream)
             plan.solve_graph(dA, dB, info, stream=stream)
             e1.record(stream)
             torch.cuda.synchronize()
-            if it >= args.warmup:
+            if it >= warmup:
                 total += e0.elapsed_time(e1)
     prof = lla.profile_stop()
     launches = lla.kernel_launches() - l0
-    ms = total / args.steps
+    ms = total / steps
+    # the timed replays' results are checked too (the last one)
+    assert int((info != -1).sum()) == 0
+    worst_timed = batch_backward_errors(torch, plan, n, m, As, Bs, dB, dt)
+    assert worst_timed <= 10.0, worst_timed
     flops = plan.shape()["flops"]
-    fp64_peak = lla.measure_peak_tflops(0 if dt == torch.float64 else 2)
+    peak = lla.measure_peak_tflops(0 if dt == torch.float64 else 2)
     achieved = flops / (ms * 1e-3) / 1e12
-    # CPU baseline: the oracle on a sample of the systems, scaled by flops
     cpu = None
-    if not args.no_cpu:
+    if cpu_sample:
         from oracle import oracle as ora
-        idx = np.random.default_rng(1).choice(count, size=min(count, 300), replace=False)
-        t0, fl = time.perf_counter(), 0.0
-        for i in idx:
-            a = As[i].cpu().numpy().astype(np.float64 if dt == torch.float64 else np.float32)
-            b = Bs[i].cpu().numpy().astype(a.dtype)
-            ora.solvec_inplace(a, b)
-            fl += n[i] ** 3 / 3.0 + 2.0 * n[i] ** 2 * m[i]
-        tcpu = time.perf_counter() - t0
+        idx = np.random.default_rng(1).choice(count, size=min(count, cpu_sample), replace=False)
+        fl = 0.0
+        with OneCore():
+            t0 = time.perf_counter()
+            for i in idx:
+                a = As[i].cpu().numpy().astype(np.float64 if dt == torch.float64 else np.float32)
+                b = Bs[i].cpu().numpy().astype(a.dtype)
+                ora.solvec_inplace(a, b)
+                fl += n[i] ** 3 / 3.0 + 2.0 * n[i] ** 2 * m[i]
+            tcpu = time.perf_counter() - t0
         cpu = {"value": (fl / tcpu) / flops * count, "unit": "solves/s", "cores": 1, "kind": "port",
-               "sample": f"oracle solvec on {len(idx)} random systems of the batch, scaled by flops"}
-    out = {
-        "metric": "batched SPD solves/s (10,000 uneven systems, n 16-256, 1-8 RHS)",
-        "value": count / (ms * 1e-3), "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": args.batch_dtype, "data": "synthetic (seeded G G^T/n + 0.1 I)",
-        "config": {"workload": f"batch count={count} n=16..256 log-uniform m=1..8 {args.batch_dtype}",
+               "sample": f"oracle solvec on {len(idx)} random systems of the batch (1 pinned core), "
+                         f"scaled by flops to the whole batch"}
+    return {
+        "metric": f"batched SPD solves/s ({count} uneven systems, n 16-256, 1-8 RHS, {dtname})",
+        "value": count / (ms * 1e-3), "unit": "solves/s", "ms_per_step": ms, "steps": steps,
+        "warmup": warmup, "dtype": dtname,
+        "config": {"workload": f"batch count={count} n=16..256 log-uniform m=1..8 {dtname}",
                    "launch": "one persistent kernel replayed from a CUDA graph",
                    "shape": plan.shape(), "autotune_ms": tune_ms,
                    "l2": "pools %.2f GB (> L2)" % (plan.a_elems * (8 if dt == torch.float64 else 4) / 1e9)},
-        "backward_error_over_n_eps": worst,
-        "roofline": {"kernel": "batch", "bound": "fp64" if dt == torch.float64 else "fp32",
-                     "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp64_peak if fp64_peak > 0 else None,
+        "backward_error_over_n_eps": max(worst, worst_timed),
+        "checked": f"all {count} systems, FP64 residual of the caller's copies",
+        "roofline": {"kernel": "batch", "bound": "fp64-tensor" if dt == torch.float64 else "fp32-fma",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak > 0 else None,
                      "peak_source": "measured live (FP64 tensor pipe / FFMA loop on all SMs)"},
-        "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches * args.steps // (args.warmup + args.steps),
+        "cpu_baseline": cpu, "clocks": clk.summary(),
+        "gpu_launches": launches * steps // (warmup + steps),
         "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
     }
+
+
+def run_batch(args):
+    import torch
+    import __graft_entry__
+    lla = __graft_entry__.load_package()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    out = measure_batch(torch, lla, dev, args.batch_count, args.batch_dtype, args.steps, args.warmup,
+                        cpu_sample=0 if args.no_cpu else 300)
+    out.update({"n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "data": "synthetic (seeded G G^T/n + 0.1 I)"})
     print(json.dumps(out))
 
 
@@ -678,126 +768,154 @@ def run_sweep(args):
                       "rows": rows}))
 
 
-def run_serve(args):
-    """Poisson arrivals of solve requests: n log-uniform in [32, 4096], kappa
-    log-uniform in [1e1, 1e6] (Q diag(s) Q^T), f64 at 1e-13 or f32 at 1e-6
-    (50/50), 20% repeat-RHS requests on kept factors, 10% triangular solves;
-    admitted against a 40 GB HBM budget.  Reports throughput and p50/p99
-    latency (submit -> done) per arrival rate."""
+def serve_pools(torch, dev, rng):
+    """Distinct systems the requests draw from, built once on the device: 48 SPD
+    systems with n log-uniform in [32, 4096] and kappa log-uniform in [1e1, 1e6]
+    (Q diag(s) Q^T), and 12 lower factors for the triangular-solve requests with
+    n log-uniform in [32, 8192]."""
+    pool, tri = [], []
+    for n in sorted(np.exp(rng.uniform(np.log(32), np.log(4096), 48)).astype(int)):
+        kappa = float(np.exp(rng.uniform(np.log(1e1), np.log(1e6))))
+        A, _ = make_system(torch, int(n), 1, kappa, int(rng.integers(1 << 30)), dev)
+        pool.append({"n": int(n), "A64": A.T.contiguous().T, "A32": A.float().T.contiguous().T})
+    for n in sorted(np.exp(rng.uniform(np.log(32), np.log(8192), 12)).astype(int)):
+        kappa = float(np.exp(rng.uniform(np.log(1e1), np.log(1e6))))
+        A, _ = make_system(torch, int(n), 1, kappa, int(rng.integers(1 << 30)), dev)
+        tri.append({"n": int(n), "L": torch.linalg.cholesky(A).T.contiguous().T})
+        del A
+    torch.cuda.synchronize()
+    return pool, tri
+
+
+def normwise_be(torch, M, X, B):
+    """max_j ||b_j - M x_j||_inf / (||M||_inf ||x_j||_inf + ||b_j||_inf), in FP64."""
+    M, X, B = M.double(), X.double(), B.double()
+    r = B - M @ X
+    return float((r.abs().amax(0) / (M.abs().sum(1).amax() * X.abs().amax(0) + B.abs().amax(0))).max())
+
+
+def measure_serve(torch, lla, dev, pool, tri, rng, rate, nreq):
+    """One Poisson arrival stream at `rate` requests/s: 70% solves (f64 at 1e-13 or
+    f32 at 1e-6, 50/50), 20% repeat right-hand sides on kept factors, 10%
+    triangular solves up to n = 8192; 40 GB admission budget.  Every result is
+    checked here, independently, by an FP64 residual of the caller's copies of
+    its inputs."""
     import threading
+    srv = lla.Server(hbm_budget_bytes=40e9)
+    for i in (0, len(pool) - 1):  # warm the slots (workspace allocation) once per path
+        p = pool[i]
+        srv.submit(lla.REQ_SOLVE, p["A64"], torch.randn(p["n"], 1, dtype=torch.float64,
+                                                         device=dev).T.contiguous().T, tag=10**9 + i)
+    srv.drain()
+    srv.poll()
+    reqs = []
+    for _ in range(nreq):
+        u = rng.random()
+        m = int(rng.integers(1, 9))
+        if u < 0.1:
+            reqs.append(("trsm", int(rng.integers(len(tri))), m, torch.float64))
+        elif u < 0.3:
+            reqs.append(("resolve", int(rng.integers(len(pool))), m, torch.float64))
+        else:
+            reqs.append(("solve", int(rng.integers(len(pool))), m,
+                         torch.float64 if rng.random() < 0.5 else torch.float32))
+    # inputs materialised before the clock starts; B0 keeps a copy of every input
+    Bs, B0 = [], []
+    for (kind, pi, m, dt) in reqs:
+        nn = tri[pi]["n"] if kind == "trsm" else pool[pi]["n"]
+        b = torch.randn(nn, m, dtype=dt, device=dev).T.contiguous().T
+        Bs.append(b)
+        B0.append(b.clone())
+    gaps = rng.exponential(1.0 / rate, len(reqs))
+    handles = {}
+    for (kind, pi, m, dt) in reqs:  # kept factors for the repeat-RHS requests
+        if kind == "resolve" and pi not in handles:
+            p = pool[pi]
+            srv.submit(lla.REQ_SOLVE, p["A64"], torch.randn(p["n"], 1, dtype=torch.float64,
+                                                             device=dev).T.contiguous().T,
+                       keep_factor=True, tag=2 * 10**9 + pi)
+            handles[pi] = None
+    srv.drain()
+    for r in srv.poll():
+        if r["user_tag"] >= 2 * 10**9:
+            handles[r["user_tag"] - 2 * 10**9] = r["factor_handle"]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+
+    def submitter():
+        nxt = t0
+        for tag, ((kind, pi, m, dt), B, gap) in enumerate(zip(reqs, Bs, gaps)):
+            nxt += gap
+            d = nxt - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            if kind == "trsm":
+                srv.submit(lla.REQ_TRSM, tri[pi]["L"], B, tag=tag)
+            elif kind == "resolve":
+                srv.submit(lla.REQ_RESOLVE, pool[pi]["A64"], B, handle=handles[pi], tag=tag)
+            else:
+                p = pool[pi]
+                srv.submit(lla.REQ_SOLVE, p["A64"] if dt == torch.float64 else p["A32"], B,
+                           tol=1e-13 if dt == torch.float64 else 1e-6, tag=tag)
+    th = threading.Thread(target=submitter)
+    th.start()
+    th.join()
+    srv.drain(1200.0)
+    res = [r for r in srv.poll() if r["user_tag"] < len(reqs)]
+    stats = srv.stats()
+    for h in handles.values():
+        srv.release(h)
+    srv.close()
+    assert len(res) == len(reqs) and all(r["status"] == 0 for r in res), \
+        [r for r in res if r["status"]][:3]
+    lat = np.array([(r["t_done_us"] - r["t_submit_us"]) / 1e3 for r in res])
+    span = (max(r["t_done_us"] for r in res) - min(r["t_submit_us"] for r in res)) / 1e6
+    # independent FP64 check of EVERY result: normwise backward error of the
+    # solution the server wrote, against the caller's copy of the inputs
+    worst, over_tol, paths = {}, 0, {}
+    for r in res:
+        kind, pi, m, dt = reqs[r["user_tag"]]
+        X, b0 = Bs[r["user_tag"]], B0[r["user_tag"]]
+        if kind == "trsm":
+            M, nn = torch.tril(tri[pi]["L"]), tri[pi]["n"]
+        else:
+            M, nn = (pool[pi]["A64"] if dt == torch.float64 else pool[pi]["A32"]), pool[pi]["n"]
+        be = normwise_be(torch, M, X, b0)
+        eps = float(torch.finfo(dt).eps)
+        tol = 1e-13 if dt == torch.float64 else 1e-6
+        key = f"{r['path']}:{'f64' if dt == torch.float64 else 'f32'}:{kind}"
+        worst[key] = max(worst.get(key, 0.0), be)
+        paths[key] = paths.get(key, 0) + 1
+        over_tol += be > tol
+        assert be <= max(tol, 10 * nn * eps), (key, nn, be)
+    return {"arrival_rate": rate, "requests": len(res), "throughput": len(res) / span,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "peak_hbm_gb": stats["bytes_peak"] / 1e9,
+            "results_by_path": paths, "worst_backward_error_by_path": worst,
+            "results_over_requested_tol": int(over_tol),
+            "checked": "every result: FP64 residual of the caller's input copies (normwise backward error)"}
+
+
+def run_serve(args):
+    """Poisson arrivals of solve requests (the serving configuration): throughput
+    and p50/p99 latency (submit -> done) per arrival rate."""
     import torch
     import __graft_entry__
     lla = __graft_entry__.load_package()
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     rng = np.random.default_rng(SEED)
-    # a pool of distinct systems, built once on the device
-    pool = []
-    for n in sorted(np.exp(rng.uniform(np.log(32), np.log(4096), 48)).astype(int)):
-        kappa = float(np.exp(rng.uniform(np.log(1e1), np.log(1e6))))
-        A, _ = make_system(torch, int(n), 1, kappa, int(rng.integers(1 << 30)), dev)
-        L = torch.linalg.cholesky(A)
-        pool.append({"n": int(n), "A64": A.T.contiguous().T, "A32": A.float().T.contiguous().T,
-                     "L": L.T.contiguous().T})
-    torch.cuda.synchronize()
-    results_by_rate = []
-    for rate in [float(r) for r in args.serve_rates.split(",")]:
-        srv = lla.Server(hbm_budget_bytes=40e9)
-        # warm the slots (workspace allocation) with one request per path
-        for i in (0, len(pool) - 1):
-            p = pool[i]
-            srv.submit(lla.REQ_SOLVE, p["A64"], torch.randn(p["n"], 1, dtype=torch.float64,
-                                                             device=dev).T.contiguous().T, tag=10**9 + i)
-        srv.drain()
-        srv.poll()
-        # requests (inputs materialised before the clock starts)
-        kept = []  # (handle, pool index)
-        reqs = []
-        for t in range(args.serve_requests):
-            u = rng.random()
-            p_i = int(rng.integers(len(pool)))
-            p = pool[p_i]
-            m = int(rng.integers(1, 9))
-            if u < 0.1:
-                reqs.append(("trsm", p_i, m, torch.float64))
-            elif u < 0.3:
-                reqs.append(("resolve", p_i, m, torch.float64))
-            else:
-                reqs.append(("solve", p_i, m, torch.float64 if rng.random() < 0.5 else torch.float32))
-        Bs = [torch.randn(pool[pi]["n"], m, dtype=dt, device=dev).T.contiguous().T
-              for (_, pi, m, dt) in reqs]
-        gaps = rng.exponential(1.0 / rate, len(reqs))
-        # kept factors for repeat-RHS requests: a solve with keep_factor per pool entry used
-        handles = {}
-        for (kind, pi, m, dt) in reqs:
-            if kind == "resolve" and pi not in handles:
-                p = pool[pi]
-                srv.submit(lla.REQ_SOLVE, p["A64"], torch.randn(p["n"], 1, dtype=torch.float64,
-                                                                 device=dev).T.contiguous().T,
-                           keep_factor=True, tag=2 * 10**9 + pi)
-                handles[pi] = None
-        srv.drain()
-        for r in srv.poll():
-            if r["user_tag"] >= 2 * 10**9:
-                handles[r["user_tag"] - 2 * 10**9] = r["factor_handle"]
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-
-        def submitter():
-            nxt = t0
-            for tag, ((kind, pi, m, dt), B, gap) in enumerate(zip(reqs, Bs, gaps)):
-                nxt += gap
-                d = nxt - time.perf_counter()
-                if d > 0:
-                    time.sleep(d)
-                p = pool[pi]
-                if kind == "trsm":
-                    srv.submit(lla.REQ_TRSM, p["L"], B, tag=tag)
-                elif kind == "resolve":
-                    srv.submit(lla.REQ_RESOLVE, p["A64"], B, handle=handles[pi], tag=tag)
-                else:
-                    srv.submit(lla.REQ_SOLVE, p["A64"] if dt == torch.float64 else p["A32"], B,
-                               tol=1e-13 if dt == torch.float64 else 1e-6, tag=tag)
-        th = threading.Thread(target=submitter)
-        th.start()
-        th.join()
-        srv.drain(1200.0)
-        res = [r for r in srv.poll() if r["user_tag"] < len(reqs)]
-        stats = srv.stats()
-        for h in handles.values():
-            srv.release(h)
-        srv.close()
-        assert len(res) == len(reqs) and all(r["status"] == 0 for r in res), \
-            [r for r in res if r["status"]][:3]
-        lat = np.array([(r["t_done_us"] - r["t_submit_us"]) / 1e3 for r in res])
-        span = (max(r["t_done_us"] for r in res) - min(r["t_submit_us"] for r in res)) / 1e6
-        # every f64 result checked against 1e-13, f32 against 1e-6 (FP64 arithmetic here)
-        worst = 0.0
-        for r in res[:: max(1, len(res) // 60)]:
-            kind, pi, m, dt = reqs[r["user_tag"]]
-            if kind != "solve":
-                continue
-            p = pool[pi]
-            A = p["A64"] if dt == torch.float64 else p["A32"].double()
-            X = Bs[r["user_tag"]].double()
-            B0 = None  # inputs were overwritten; bound via the reported backward error
-            worst = max(worst, r["backward_error"] if r["path"] == "mixed" else 0.0)
-        paths = {}
-        for r in res:
-            paths[r["path"]] = paths.get(r["path"], 0) + 1
-        results_by_rate.append({
-            "arrival_rate": rate, "throughput": len(res) / span, "p50_ms": float(np.percentile(lat, 50)),
-            "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
-            "peak_hbm_gb": stats["bytes_peak"] / 1e9, "paths": paths,
-            "max_reported_backward_error": worst})
+    pool, tri = serve_pools(torch, dev, rng)
+    rates = [measure_serve(torch, lla, dev, pool, tri, rng, float(r), args.serve_requests)
+             for r in args.serve_rates.split(",")]
     out = {
         "metric": "serving: throughput and p50/p99 latency vs Poisson arrival rate",
-        "value": results_by_rate[-1]["throughput"], "unit": "requests/s", "n_gpus": 1,
+        "value": rates[-1]["throughput"], "unit": "requests/s", "n_gpus": 1,
         "higher_is_better": True, "dtype": "f64+f32", "data": "synthetic",
-        "config": {"workload": f"serve {args.serve_requests} requests per rate, n 32..4096 log-uniform, "
-                               "kappa 1e1..1e6, f64 1e-13 / f32 1e-6, 20% repeat-RHS, 10% TRSM, "
-                               "40 GB budget"},
-        "rates": results_by_rate,
+        "config": {"workload": f"serve {args.serve_requests} requests per rate, n 32..4096 log-uniform "
+                               "(triangular solves 32..8192), kappa 1e1..1e6, f64 1e-13 / f32 1e-6, "
+                               "20% repeat-RHS, 10% TRSM, 40 GB budget"},
+        "rates": rates,
     }
     print(json.dumps(out))
 

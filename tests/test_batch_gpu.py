@@ -127,3 +127,45 @@ def test_batch_autotune_keeps_results(gpu_lla, tmp_path, monkeypatch):
     # the pools still hold the inputs
     assert np.array_equal(dA.cpu().numpy(), ap) and np.array_equal(dB.cpu().numpy(), bp)
     assert (tmp_path / "tune.txt").read_text().strip()
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_batch_configuration_10000_systems(gpu_lla, dtype):
+    """The batched configuration at its own size: 10,000 systems, n log-uniform
+    in [16, 256], A = G G^T / n + 0.1 I, 1..8 RHS, one graph replay; EVERY
+    system within the per-matrix FP64 class (backward error <= 10 n eps)."""
+    torch = pytest.importorskip("torch")
+    lla = gpu_lla
+    count = 10000
+    rng = np.random.default_rng(10000)
+    n = np.clip(np.exp(rng.uniform(np.log(16), np.log(256), count)).round(), 16, 256).astype(np.int32)
+    m = rng.integers(1, 9, count).astype(np.int32)
+    dt = torch.float64 if dtype == "f64" else torch.float32
+    plan = lla.BatchPlan(n, m, dtype)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    A0 = torch.zeros(plan.a_elems, dtype=dt, device="cuda")
+    B0 = torch.zeros(plan.b_elems, dtype=dt, device="cuda")
+    As, Bs = [], []
+    for i in range(count):
+        G = torch.randn(int(n[i]), int(n[i]), dtype=torch.float64, device="cuda", generator=g)
+        a = (G @ G.T / int(n[i]) + 0.1 * torch.eye(int(n[i]), dtype=torch.float64, device="cuda")).to(dt)
+        b = torch.randn(int(n[i]), int(m[i]), dtype=torch.float64, device="cuda", generator=g).to(dt)
+        As.append(a)
+        Bs.append(b)
+        A0[plan.a_off[i]:plan.a_off[i] + n[i] * n[i]] = a.T.reshape(-1)
+        B0[plan.b_off[i]:plan.b_off[i] + n[i] * m[i]] = b.T.reshape(-1)
+    info = torch.full((count,), -7, dtype=torch.int32, device="cuda")
+    plan.solve_graph(A0, B0, info)
+    torch.cuda.synchronize()
+    assert int((info != -1).sum()) == 0
+    eps = float(torch.finfo(dt).eps)
+    worst = []
+    for i in range(count):
+        x = B0[plan.b_off[i]:plan.b_off[i] + n[i] * m[i]].reshape(int(m[i]), int(n[i])).T.double()
+        a, b = As[i].double(), Bs[i].double()
+        r = b - a @ x
+        be = (r.abs().amax(0) / (a.abs().sum(1).amax() * x.abs().amax(0) + b.abs().amax(0))).amax()
+        worst.append(be / (float(n[i]) * eps))
+    w = float(torch.stack(worst).max())
+    assert w <= 10.0, w

@@ -204,3 +204,73 @@ def test_refined_with_exact_slice_residual(gpu_lla):
     assert r2["converged"] == 1 and r2["fell_back"] == 0
     assert backward_error(a, x2, b) <= 2e-13
     assert abs(r1["iterations"] - r2["iterations"]) <= 1
+
+
+def device_qdq(torch, n, kappa, seed, diag_scale=0.0):
+    """A = D Q diag(s) Q^T D built on the device in FP64 (Q from the QR of a
+    seeded Gaussian, s log-uniform in [1, kappa], D = diag(10^U(-d, d)))."""
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    G = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=g)
+    Q, _ = torch.linalg.qr(G)
+    del G
+    s = torch.exp(torch.rand(n, dtype=torch.float64, device="cuda", generator=g) * np.log(kappa))
+    s[0], s[-1] = 1.0, kappa
+    A = (Q * s) @ Q.T
+    del Q
+    A = (A + A.T) * 0.5
+    if diag_scale:
+        d = 10.0 ** ((torch.rand(n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1) * diag_scale)
+        A = A * d[:, None] * d[None, :]
+    B = torch.randn(n, 64, dtype=torch.float64, device="cuda", generator=g)
+    return A, B
+
+
+def device_backward_error(torch, A, X, B):
+    R = B - A @ X
+    return float((R.abs().amax(0) / (A.abs().sum(1).amax() * X.abs().amax(0) + B.abs().amax(0))).max())
+
+
+@pytest.mark.parametrize("residual", ["slices", "fp64"])
+def test_precision_sweep_size_kappa_1e8_diag_scaled(gpu_lla, residual):
+    """The precision-sweep configuration at its own size: n = 8192, 16 RHS,
+    kappa = 1e8, diagonal scaled by 10^U(-3, 3); the bf16x6 form must reach the
+    1e-13 backward error without falling back (equilibration removes D)."""
+    torch = pytest.importorskip("torch")
+    lla = gpu_lla
+    n, m = 8192, 16
+    A, B = device_qdq(torch, n, 1e8, 8192, diag_scale=3.0)
+    B = B[:, :m].T.contiguous().T
+    X = torch.empty_like(B.T.contiguous()).T
+    rep = lla.posv_refined_device(A.T, B, X, update="bf16x6", residual=residual)
+    torch.cuda.synchronize()
+    assert rep["converged"] == 1 and rep["fell_back"] == 0, rep
+    be = device_backward_error(torch, A, X, B)
+    assert be <= 1e-13, (be, rep)
+
+
+def test_headline_size_n16384_kappa_1e6(gpu_lla):
+    """The headline configuration under the test suite: n = 16384, 64 RHS,
+    kappa = 1e6, bf16x6 updates with the exact-slice residual, checked by an
+    independent FP64 product; and it agrees with the plain FP64 path's solution
+    to the forward error the conditioning allows."""
+    torch = pytest.importorskip("torch")
+    lla = gpu_lla
+    n = 16384
+    A, B = device_qdq(torch, n, 1e6, 16384)
+    B = B.T.contiguous().T
+    X = torch.empty_like(B.T.contiguous()).T
+    rep = lla.posv_refined_device(A.T, B, X, update="bf16x6", residual="slices")
+    torch.cuda.synchronize()
+    assert rep["converged"] == 1 and rep["fell_back"] == 0, rep
+    be = device_backward_error(torch, A, X, B)
+    assert be <= 1e-13, (be, rep)
+    W = A.clone()
+    info = lla.potrf_device(W.T, algo=lla.ALGO_FAST)
+    Xp = B.clone()
+    lla.trsm_device(W.T, Xp, 0)
+    lla.trsm_device(W.T, Xp, 1)
+    lla.device_status()
+    assert int(info.item()) == -1
+    fe = float((X - Xp).abs().max() / Xp.abs().max())
+    assert fe <= 1e6 * 1e-13 * 10, fe
