@@ -376,6 +376,8 @@ def main():
                     help="single: the n=16384 system (the headline); batch: 10,000 uneven small systems")
     ap.add_argument("--batch-count", type=int, default=10000)
     ap.add_argument("--batch-dtype", default="f64", choices=["f64", "f32"])
+    ap.add_argument("--batch-refined", action="store_true",
+                    help="f64 batch through an FP32 factor with per-system FP64 refinement")
     ap.add_argument("--serve-requests", type=int, default=400)
     ap.add_argument("--serve-rates", default="100,200,400,800", help="Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-rate", type=float, default=200.0,
@@ -548,9 +550,11 @@ def main():
     # the batched and serving configurations, measured in the same run (rank 0)
     batch = serve = None
     if rank == 0 and not args.no_batch:
-        batch = {dtn: measure_batch(torch, lla, dev, args.batch_count, dtn, max(3, min(args.steps, 10)),
-                                    max(3, args.warmup), cpu_sample=0 if args.no_cpu else 200)
+        kb, wb = max(3, min(args.steps, 10)), max(3, args.warmup)
+        batch = {dtn: measure_batch(torch, lla, dev, args.batch_count, dtn, kb, wb,
+                                    cpu_sample=0 if args.no_cpu else 200)
                  for dtn in ("f64", "f32")}
+        batch["f64_refined"] = measure_batch(torch, lla, dev, args.batch_count, "f64", kb, wb, refined=True)
     if rank == 0 and not args.no_serve:
         rng = np.random.default_rng(SEED)
         pool, tri = serve_pools(torch, dev, rng)
@@ -625,13 +629,16 @@ def batch_backward_errors(torch, plan, n, m, As, Bs, dX, dt):
     return float(torch.stack(vals).max())
 
 
-def measure_batch(torch, lla, dev, count, dtname, steps, warmup, cpu_sample=0):
+def measure_batch(torch, lla, dev, count, dtname, steps, warmup, cpu_sample=0, refined=False):
     """The batched configuration: `count` systems, n log-uniform in [16, 256],
     A = G G^T / n + 0.1 I, 1..8 RHS; one persistent launch replayed from a CUDA
-    graph per step (pools restored outside the events; pools > L2)."""
+    graph per step (pools restored outside the events; pools > L2).  refined:
+    f64 systems through an FP32 factorisation with per-system FP64 refinement."""
     dt = torch.float64 if dtname == "f64" else torch.float32
     n, m, As, Bs = make_batch(torch, count, SEED, dev, dt)
     plan = lla.BatchPlan(n, m, dtname)
+    if refined:
+        plan.set_refined(True)
     A0 = torch.zeros(plan.a_elems, dtype=dt, device=dev)
     B0 = torch.zeros(plan.b_elems, dtype=dt, device=dev)
     for i in range(count):
@@ -690,7 +697,10 @@ def measure_batch(torch, lla, dev, count, dtname, steps, warmup, cpu_sample=0):
                "sample": f"oracle solvec on {len(idx)} random systems of the batch (1 pinned core), "
                          f"scaled by flops to the whole batch"}
     return {
-        "metric": f"batched SPD solves/s ({count} uneven systems, n 16-256, 1-8 RHS, {dtname})",
+        "metric": f"batched SPD solves/s ({count} uneven systems, n 16-256, 1-8 RHS, {dtname}"
+                  f"{', FP32 factor + FP64 refinement per system' if refined else ''})",
+        "path": "FP32 factorisation + per-system FP64 refinement (plain FP64 fallback)" if refined
+                else f"plain {dtname} factorisation",
         "value": count / (ms * 1e-3), "unit": "solves/s", "ms_per_step": ms, "steps": steps,
         "warmup": warmup, "dtype": dtname,
         "config": {"workload": f"batch count={count} n=16..256 log-uniform m=1..8 {dtname}",
@@ -716,7 +726,7 @@ def run_batch(args):
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     out = measure_batch(torch, lla, dev, args.batch_count, args.batch_dtype, args.steps, args.warmup,
-                        cpu_sample=0 if args.no_cpu else 300)
+                        cpu_sample=0 if args.no_cpu else 300, refined=args.batch_refined)
     out.update({"n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "data": "synthetic (seeded G G^T/n + 0.1 I)"})
     print(json.dumps(out))

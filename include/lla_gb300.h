@@ -217,6 +217,23 @@ int lla_dtrsm_device(const double *dL, int64_t n, int64_t ld, int trans, double 
 int lla_strsm_device(const float *dL, int64_t n, int64_t ld, int trans, float *dB, int64_t m,
                      int64_t ldb, int algo, void *stream, lla_error *err);
 
+/* IntoTriangular::triangular_inplace (src/triangular.rs:37-53) on a
+ * device-resident column-major matrix (rows x cols, ld): uplo = LLA_UPPER
+ * zeroes the strict lower part, LLA_LOWER the strict upper part.  Errors:
+ * NotSquare{rows, cols} (src/lib.rs:64-71).  Asynchronous on `stream`. */
+int lla_dtriangular_device(double *dA, int64_t rows, int64_t cols, int64_t ld, int uplo, void *stream,
+                           lla_error *err);
+int lla_striangular_device(float *dA, int64_t rows, int64_t cols, int64_t ld, int uplo, void *stream,
+                           lla_error *err);
+/* Triangular::is_triangular (src/triangular.rs:67-90) on a device-resident
+ * column-major matrix: *d_result (device int) receives 1 when every entry
+ * outside the uplo triangle is zero, else 0; a non-square matrix gives 0 (not
+ * an error, as in the reference).  Asynchronous on `stream`. */
+int lla_dis_triangular_device(const double *dA, int64_t rows, int64_t cols, int64_t ld, int uplo,
+                              int *d_result, void *stream, lla_error *err);
+int lla_sis_triangular_device(const float *dA, int64_t rows, int64_t cols, int64_t ld, int uplo,
+                              int *d_result, void *stream, lla_error *err);
+
 /* Synchronises `stream` and reports whether a bounded device wait of an
  * asynchronous call made on this host thread (lla_?trsm_device) gave up since
  * the last query: LLA_ERR_TIMEOUT (the X of such a call is not valid) or
@@ -282,7 +299,8 @@ typedef struct lla_refine_opts {
     int32_t fallback;    /* 1: plain FP64 on breakdown or stall (default); 0: LLA_ERR_NOT_CONVERGED */
     int32_t nb;          /* panel width (0: default) */
     int32_t residual;    /* lla_residual (default LLA_RESIDUAL_FP64) */
-    int32_t reserved[2];
+    int32_t sub_ctas_per_sm; /* CTAs per SM of the FP32 substitutions: 1 or 2 (0: default) */
+    int32_t update_kchunk;   /* K-chunk of the tensor-core update's operand stages: 64 or 32 (0: default) */
 } lla_refine_opts;
 
 typedef struct lla_refine_report {
@@ -351,6 +369,14 @@ void lla_batch_plan_destroy(lla_batch_plan *plan);
 int lla_batch_plan_info(const lla_batch_plan *plan, int64_t *a_elems, int64_t *b_elems,
                         int64_t *a_off, int64_t *b_off, int *ctas_per_sm, int *threads,
                         double *flops);
+/* f64 plans: refined = 1 solves every system through an FP32 factorisation
+ * with FP64 iterative refinement inside the same persistent launch (one CTA
+ * per system; A_i is then READ ONLY and B_i receives X_i; a system whose FP32
+ * factorisation breaks down or whose backward error stays above 10 n eps is
+ * solved again by the plain FP64 routine, whose failing row d_info[i]
+ * reports); refined = 0 restores the plain FP64 solve (A factored in place).
+ * LLA_ERR_INVALID_ARG for f32 plans. */
+int lla_batch_set_refined(lla_batch_plan *plan, int refined, lla_error *err);
 /* Overrides the launch shape (CTAs per SM 1..8, threads 128 or 256). */
 int lla_batch_set_shape(lla_batch_plan *plan, int ctas_per_sm, int threads);
 /* One persistent launch on `stream` (asynchronous). */
@@ -370,13 +396,18 @@ int lla_batch_autotune(lla_batch_plan *plan, void *dA, void *dB, int32_t *d_info
 
 /* ---- serving loop (no counterpart in the reference) ----------------------
  * Requests arrive while others run.  Each is admitted against an HBM budget
- * (first come, first served), small systems (n <= small_n, <= 8 RHS) are
- * gathered for up to batch_window_us into one batched launch, large ones run
- * concurrently on `slots` streams (mixed-precision refined solve for f64,
- * FP32 factor + FP64 refinement for f32, plain FP64 factor when the factor is
- * to be kept), factors can stay on the device for repeat right-hand sides,
- * and every request records submit / admit / start / done times.  All data is
- * device-resident (column-major); B is overwritten with X. */
+ * (first come, first served).  Small systems (n <= small_n, <= 8 RHS) go, as
+ * soon as they are admitted, to a device-resident loop: persistent CTAs that
+ * claim requests from a ring in mapped host memory and solve each one in
+ * place (one CTA per request, the batched kernel's arithmetic), so requests
+ * that arrive while others are on the GPU join the running loop; its CTAs
+ * return after batch_window_us without work and the host relaunches it on the
+ * next request.  Large requests run concurrently on `slots` streams
+ * (mixed-precision refined solve for f64, FP32 factor + FP64 refinement for
+ * f32, plain FP64 factor when the factor is to be kept); factors can stay on
+ * the device for repeat right-hand sides; every request records submit /
+ * admit / start / done times.  All data is device-resident (column-major); B
+ * is overwritten with X. */
 enum lla_request_kind {
     LLA_REQ_SOLVE = 0,   /* A X = B for SPD A (lower triangle read) */
     LLA_REQ_RESOLVE = 1, /* repeat right-hand sides on a kept factor (factor_handle) */
@@ -390,10 +421,10 @@ enum lla_result_path {
 typedef struct lla_serve_opts {
     double hbm_budget_bytes; /* admission budget (default 40e9) */
     int32_t slots;           /* concurrent large-request streams (default 6) */
-    int32_t small_n;         /* largest order sent to the batched kernel (default 256) */
-    int32_t batch_max;       /* most requests per batched launch (default 512) */
-    int32_t reserved;
-    double batch_window_us;  /* how long the batcher waits for more small requests (200) */
+    int32_t small_n;         /* largest order sent to the device-resident loop (default 256) */
+    int32_t batch_max;       /* most small requests in flight in the loop's ring (default and limit 1024) */
+    int32_t device_ctas;     /* persistent CTAs of the device loop (0: half the SMs) */
+    double batch_window_us;  /* idle time after which the loop's CTAs return (default 2000) */
 } lla_serve_opts;
 
 typedef struct lla_request {
@@ -425,6 +456,7 @@ typedef struct lla_result {
 typedef struct lla_server_stats {
     double bytes_in_use, bytes_peak;
     int64_t queued, running, submitted, completed, kept_factors;
+    int64_t device_loop_launches; /* launches of the device-resident loop so far */
 } lla_server_stats;
 
 typedef struct lla_server lla_server;

@@ -66,7 +66,8 @@ class Error(ctypes.Structure):
 class RefineOpts(ctypes.Structure):
     _fields_ = [("update", ctypes.c_int32), ("max_iters", ctypes.c_int32), ("tol", ctypes.c_double),
                 ("equilibrate", ctypes.c_int32), ("fallback", ctypes.c_int32), ("nb", ctypes.c_int32),
-                ("residual", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
+                ("residual", ctypes.c_int32), ("sub_ctas_per_sm", ctypes.c_int32),
+                ("update_kchunk", ctypes.c_int32)]
 
 
 class RefineReport(ctypes.Structure):
@@ -123,6 +124,7 @@ EXPORTS = {
                              ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                              ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
     "lla_batch_set_shape": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "lla_batch_set_refined": ([ctypes.c_void_p, ctypes.c_int, _E], ctypes.c_int),
     "lla_dbatch_posv_device": ([ctypes.c_void_p] * 5 + [_E], ctypes.c_int),
     "lla_sbatch_posv_device": ([ctypes.c_void_p] * 5 + [_E], ctypes.c_int),
     "lla_batch_posv_graph": ([ctypes.c_void_p] * 5 + [_E], ctypes.c_int),
@@ -157,6 +159,10 @@ for _p in "ds":
         f"lla_{_p}apply_constraints": (_V + _V + _V + [_E], ctypes.c_int),
         f"lla_{_p}potrf_device": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
                                    ctypes.c_void_p, ctypes.c_void_p, _E], ctypes.c_int),
+        f"lla_{_p}triangular_device": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                        ctypes.c_int, ctypes.c_void_p, _E], ctypes.c_int),
+        f"lla_{_p}is_triangular_device": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                           ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, _E], ctypes.c_int),
         f"lla_{_p}trsm_device": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
                                   ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
                                   ctypes.c_void_p, _E], ctypes.c_int),
@@ -487,6 +493,37 @@ def trsm_device(L, B, trans, algo=ALGO_FAST, stream=None):
     return B
 
 
+def triangular_device(A, uplo, stream=None):
+    """IntoTriangular::triangular_inplace on a column-major CUDA tensor in place
+    (src/triangular.rs:37-53); NotSquare for a non-square tensor."""
+    import torch
+    assert A.is_cuda and A.dim() == 2 and (A.stride(0) == 1 or A.numel() == 0)
+    e = Error()
+    p = "d" if A.dtype == torch.float64 else "s"
+    getattr(lib, f"lla_{p}triangular_device")(ctypes.c_void_p(A.data_ptr()), A.shape[0], A.shape[1],
+                                              max(1, _ld(A) if A.shape[1] > 0 else A.shape[0]), _uplo(uplo),
+                                              _stream_ptr(stream), ctypes.byref(e))
+    _raise(e)
+    return A
+
+
+def is_triangular_device(A, uplo, result=None, stream=None):
+    """Triangular::is_triangular on a column-major CUDA tensor (src/triangular.rs:67-90):
+    returns a device int32 tensor holding 1 or 0 (no host round trip)."""
+    import torch
+    assert A.is_cuda and A.dim() == 2 and (A.stride(0) == 1 or A.numel() == 0)
+    if result is None:
+        result = torch.empty(1, dtype=torch.int32, device=A.device)
+    e = Error()
+    p = "d" if A.dtype == torch.float64 else "s"
+    getattr(lib, f"lla_{p}is_triangular_device")(ctypes.c_void_p(A.data_ptr()), A.shape[0], A.shape[1],
+                                                 max(1, _ld(A) if A.shape[1] > 0 else A.shape[0]),
+                                                 _uplo(uplo), ctypes.c_void_p(result.data_ptr()),
+                                                 _stream_ptr(stream), ctypes.byref(e))
+    _raise(e)
+    return result
+
+
 def device_status(stream=None):
     """Synchronises `stream` and raises DeviceError(LLA_ERR_TIMEOUT) when a
     bounded wait of an asynchronous device call of this thread gave up since
@@ -507,9 +544,10 @@ def debug_inject_lost_handoff(spin_limit=1000):
 # ---- mixed-precision refined solve (no counterpart in the reference) --------
 
 def refine_opts(update="bf16x6", max_iters=30, tol=1e-13, equilibrate=True, fallback=True, nb=0,
-                residual="fp64"):
+                residual="fp64", sub_ctas_per_sm=0, update_kchunk=0):
     o = RefineOpts()
     lib.lla_refine_opts_default(ctypes.byref(o))
+    o.sub_ctas_per_sm, o.update_kchunk = sub_ctas_per_sm, update_kchunk
     o.update = UPDATE_NAMES[update] if isinstance(update, str) else int(update)
     o.residual = RESIDUAL_NAMES[residual] if isinstance(residual, str) else int(residual)
     o.max_iters, o.tol = max_iters, tol
@@ -600,6 +638,13 @@ class BatchPlan:
         if lib.lla_batch_set_shape(self.h, ctas_per_sm, threads):
             raise ValueError((ctas_per_sm, threads))
 
+    def set_refined(self, refined=True):
+        """f64 plans: solve through an FP32 factorisation with per-system FP64
+        refinement (A read only, B receives X), or back to plain FP64."""
+        e = Error()
+        lib.lla_batch_set_refined(self.h, int(bool(refined)), ctypes.byref(e))
+        _raise(e)
+
     def pack(self, As, Bs):
         """Host pools (numpy) holding the column-major A_i and B_i."""
         ap = np.zeros(self.a_elems, dtype=self.np_dtype)
@@ -655,7 +700,7 @@ PATH_NAMES = {1: "batched", 2: "mixed", 3: "fp64", 4: "kept_factor", 5: "trsm"}
 class ServeOpts(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_double), ("slots", ctypes.c_int32),
                 ("small_n", ctypes.c_int32), ("batch_max", ctypes.c_int32),
-                ("reserved", ctypes.c_int32), ("batch_window_us", ctypes.c_double)]
+                ("device_ctas", ctypes.c_int32), ("batch_window_us", ctypes.c_double)]
 
 
 class Request(ctypes.Structure):
@@ -683,19 +728,21 @@ class ServerStats(ctypes.Structure):
     _fields_ = [("bytes_in_use", ctypes.c_double), ("bytes_peak", ctypes.c_double),
                 ("queued", ctypes.c_int64), ("running", ctypes.c_int64),
                 ("submitted", ctypes.c_int64), ("completed", ctypes.c_int64),
-                ("kept_factors", ctypes.c_int64)]
+                ("kept_factors", ctypes.c_int64), ("device_loop_launches", ctypes.c_int64)]
 
 
 class Server:
     """Continuous-batching solve server over device-resident (column-major)
-    CUDA tensors.  submit() returns immediately; poll()/drain() collect results."""
+    CUDA tensors: small systems are served by a device-resident loop of
+    persistent CTAs, large ones by concurrent streams.  submit() returns
+    immediately; poll()/drain() collect results."""
 
-    def __init__(self, hbm_budget_bytes=40e9, slots=6, small_n=256, batch_max=512,
-                 batch_window_us=200.0):
+    def __init__(self, hbm_budget_bytes=40e9, slots=6, small_n=256, batch_max=1024,
+                 batch_window_us=2000.0, device_ctas=0):
         o = ServeOpts()
         lib.lla_serve_opts_default(ctypes.byref(o))
         o.hbm_budget_bytes, o.slots, o.small_n = hbm_budget_bytes, slots, small_n
-        o.batch_max, o.batch_window_us = batch_max, batch_window_us
+        o.batch_max, o.batch_window_us, o.device_ctas = batch_max, batch_window_us, device_ctas
         h, e = ctypes.c_void_p(), Error()
         lib.lla_server_create(ctypes.byref(o), ctypes.byref(h), ctypes.byref(e))
         _raise(e)

@@ -159,6 +159,8 @@ HostBuf::~HostBuf() {
 }
 
 Ctx::~Ctx() {
+    for (auto &e : mixed.ev)
+        if (e) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -852,9 +854,59 @@ static int trsm_device_impl(const T *dL, int64_t n, int64_t ld, int trans, T *dB
     return LLA_OK;
 }
 
+// triangular_inplace / is_triangular on device-resident column-major matrices
+// (src/triangular.rs:37-53, 67-90): no host round trip, so a factor produced by
+// lla_?potrf_device can be masked or tested where it lies.
+template <typename T>
+static int triangular_device_impl(T *dA, int64_t rows, int64_t cols, int64_t ld, int uplo, void *stream,
+                                  lla_error *err) {
+    if (rows < 0 || cols < 0 || ld < std::max<int64_t>(1, rows) || (rows * cols > 0 && !dA) ||
+        (uplo != LLA_UPPER && uplo != LLA_LOWER))
+        return lla__set_status(err, LLA_ERR_INVALID_ARG);
+    if (rows != cols) return not_square(err, rows, cols);  // check_square (src/lib.rs:64-71)
+    lla__set_status(err, LLA_OK);
+    if (rows == 0) return LLA_OK;
+    if (!get_ctx(err)) return err ? err->code : LLA_ERR_NO_DEVICE;
+    LLA_TRY_CUDA(launch_status(mask_launch<T>(dA, 1, ld, rows, uplo, (cudaStream_t)stream)));
+    return LLA_OK;
+}
+
+template <typename T>
+static int is_triangular_device_impl(const T *dA, int64_t rows, int64_t cols, int64_t ld, int uplo,
+                                     int *d_result, void *stream, lla_error *err) {
+    if (rows < 0 || cols < 0 || ld < std::max<int64_t>(1, rows) || (rows * cols > 0 && !dA) || !d_result ||
+        (uplo != LLA_UPPER && uplo != LLA_LOWER))
+        return lla__set_status(err, LLA_ERR_INVALID_ARG);
+    lla__set_status(err, LLA_OK);
+    if (!get_ctx(err)) return err ? err->code : LLA_ERR_NO_DEVICE;
+    cudaStream_t st = (cudaStream_t)stream;
+    // a non-square matrix is not triangular (no error, as in the reference)
+    LLA_TRY_CUDA(launch_status(fill_int_launch(d_result, rows == cols ? 1 : 0, st)));
+    if (rows == cols && rows > 0)
+        LLA_TRY_CUDA(launch_status(is_triangular_launch<T>(dA, 1, ld, rows, uplo, d_result, st)));
+    return LLA_OK;
+}
+
 #define LLA_VIEW_ARGS(T) T *a, int64_t rows, int64_t cols, int64_t rs, int64_t cs
 
 extern "C" {
+
+int lla_dtriangular_device(double *dA, int64_t rows, int64_t cols, int64_t ld, int uplo, void *stream,
+                           lla_error *err) {
+    return triangular_device_impl<double>(dA, rows, cols, ld, uplo, stream, err);
+}
+int lla_striangular_device(float *dA, int64_t rows, int64_t cols, int64_t ld, int uplo, void *stream,
+                           lla_error *err) {
+    return triangular_device_impl<float>(dA, rows, cols, ld, uplo, stream, err);
+}
+int lla_dis_triangular_device(const double *dA, int64_t rows, int64_t cols, int64_t ld, int uplo,
+                              int *d_result, void *stream, lla_error *err) {
+    return is_triangular_device_impl<double>(dA, rows, cols, ld, uplo, d_result, stream, err);
+}
+int lla_sis_triangular_device(const float *dA, int64_t rows, int64_t cols, int64_t ld, int uplo,
+                              int *d_result, void *stream, lla_error *err) {
+    return is_triangular_device_impl<float>(dA, rows, cols, ld, uplo, d_result, stream, err);
+}
 
 int lla_device_status(void *stream, lla_error *err) {
     lla__set_status(err, LLA_OK);

@@ -39,6 +39,7 @@ struct MixedWs {
     DevBuf F, fdiag, S;                       // plain FP64 fallback (S: exact-order verdict scratch)
     DevBuf opA, opB;                          // tensor-core operand planes of one panel
     DevBuf tcerr;                             // tensor-core update status word
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // start, factor done, refinement done
     DevBuf pinv;                              // inverted 32 x 32 diagonal blocks of one panel
     HostBuf words_host;
 };

@@ -81,6 +81,151 @@ __device__ int warp_potrf32(T *sD, int bs, int lane) {
     return fail;
 }
 
+// Factor-and-solve of one system by the whole CTA: A (n x n, column-major,
+// ld = n) is factored in place (L in the lower triangle), B (n x m, leading
+// dimension ldb) is overwritten with X.  sD: [32][33], sP: [kBMaxN][33] shared
+// scratch.  Returns the first failing row (non-positive pivot) or -1; every
+// thread returns the same value.
+template <typename T>
+__device__ int batch_factor(T *A, int n, T *sD, T *sP, int *s_fail) {
+    const int tid = threadIdx.x, nthr = blockDim.x, warp = tid >> 5, lane = tid & 31;
+    const int nwarps = nthr >> 5;
+    if (tid == 0) *s_fail = -1;
+    __syncthreads();
+    // ---- factor: right-looking, 32-column blocks ----
+    for (int kb = 0; kb < n; kb += kBNb) {
+        const int bs = min(kBNb, n - kb);
+        for (int e = tid; e < 32 * 32; e += nthr) {
+            const int r = e % 32, c = e / 32;
+            if (r < bs && c <= r) sD[r * 33 + c] = A[(kb + r) + (int64_t)(kb + c) * n];
+        }
+        __syncthreads();
+        if (warp == 0) {
+            const int f = warp_potrf32(sD, bs, lane);
+            if (lane == 0 && f >= 0) *s_fail = kb + f;
+        }
+        __syncthreads();
+        if (*s_fail >= 0) break;
+        for (int e = tid; e < 32 * 32; e += nthr) {
+            const int r = e % 32, c = e / 32;
+            if (r < bs && c <= r) A[(kb + r) + (int64_t)(kb + c) * n] = sD[r * 33 + c];
+        }
+        // panel: each row below the block solves against L_kk
+        const int q = kb + bs, rows = n - q;
+        for (int rr = tid; rr < rows; rr += nthr) {
+            const int r = q + rr;
+            T v[32];
+#pragma unroll
+            for (int c = 0; c < 32; ++c) v[c] = (c < bs) ? A[r + (int64_t)(kb + c) * n] : T(0);
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+                if (c < bs) {
+                    v[c] = v[c] / sD[c * 33 + c];
+#pragma unroll
+                    for (int c2 = c + 1; c2 < 32; ++c2)
+                        if (c2 < bs) v[c2] = fma(-v[c], sD[c2 * 33 + c], v[c2]);
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+                if (c < bs) {
+                    sP[rr * 33 + c] = v[c];
+                    A[r + (int64_t)(kb + c) * n] = v[c];
+                }
+            }
+        }
+        __syncthreads();
+        // trailing lower triangle, one column per warp, lanes over rows:
+        // A[i,j] -= sum_t P[i][t] P[j][t]
+        for (int j = warp; j < rows; j += nwarps) {
+            for (int i = j + lane; i < rows; i += 32) {
+                T acc = A[(q + i) + (int64_t)(q + j) * n];
+#pragma unroll 8
+                for (int t = 0; t < bs; ++t) acc = fma(-sP[i * 33 + t], sP[j * 33 + t], acc);
+                A[(q + i) + (int64_t)(q + j) * n] = acc;
+            }
+        }
+        __syncthreads();
+    }
+    const int fail = *s_fail;
+    __syncthreads();
+    return fail;
+}
+
+// L L^T X = B in place for the factor in the lower triangle of A (ld = n).
+template <typename T>
+__device__ void batch_trsolve(const T *A, int n, T *B, int64_t ldb, int m, T *sD, T *sP) {
+    const int tid = threadIdx.x, nthr = blockDim.x, warp = tid >> 5, lane = tid & 31;
+    const int nwarps = nthr >> 5;
+    // ---- solve L y = b (forward), then L^T x = y (backward), 32-row blocks ----
+    for (int pass = 0; pass < 2; ++pass) {
+        const bool fwd = pass == 0;
+        const int nblk = (n + kBNb - 1) / kBNb;
+        for (int bi = 0; bi < nblk; ++bi) {
+            const int kb = (fwd ? bi : nblk - 1 - bi) * kBNb;
+            const int bs = min(kBNb, n - kb);
+            for (int e = tid; e < 32 * 32; e += nthr) {
+                const int r = e % 32, c = e / 32;
+                if (r < bs && c <= r) sD[r * 33 + c] = A[(kb + r) + (int64_t)(kb + c) * n];
+            }
+            __syncthreads();
+            // warp k solves right-hand side k on this block (lane = row)
+            for (int k = warp; k < m; k += nwarps) {
+                T x = (lane < bs) ? B[(kb + lane) + (int64_t)k * ldb] : T(0);
+                if (fwd) {
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) {
+                        if (c < bs) {
+                            const T xc = shfl(x, c) / sD[c * 33 + c];
+                            if (lane == c) x = xc;
+                            if (lane > c && lane < bs) x = fma(-xc, sD[lane * 33 + c], x);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int cc = 31; cc >= 0; --cc) {
+                        if (cc < bs) {
+                            const T xc = shfl(x, cc) / sD[cc * 33 + cc];
+                            if (lane == cc) x = xc;
+                            if (lane < cc) x = fma(-xc, sD[cc * 33 + lane], x);
+                        }
+                    }
+                }
+                if (lane < bs) B[(kb + lane) + (int64_t)k * ldb] = x;
+            }
+            // stage the block's coupling to the remaining rows: forward needs
+            // L[r][kb+t] for r >= kb+bs, backward L[kb+t][r] for r < kb
+            const int q = fwd ? kb + bs : 0, rows = fwd ? n - kb - bs : kb;
+            for (int e = tid; e < rows * bs; e += nthr) {
+                if (fwd) {
+                    const int rr = e % rows, t = e / rows;  // consecutive rr: contiguous column
+                    sP[rr * 33 + t] = A[(q + rr) + (int64_t)(kb + t) * n];
+                } else {
+                    const int t = e % bs, rr = e / bs;  // consecutive t: contiguous column rr
+                    sP[rr * 33 + t] = A[(kb + t) + (int64_t)rr * n];
+                }
+            }
+            __syncthreads();
+            for (int e = tid; e < rows * m; e += nthr) {
+                const int rr = e % rows, k = e / rows;
+                T acc = B[(q + rr) + (int64_t)k * ldb];
+#pragma unroll 8
+                for (int t = 0; t < bs; ++t) acc = fma(-sP[rr * 33 + t], B[(kb + t) + (int64_t)k * ldb], acc);
+                B[(q + rr) + (int64_t)k * ldb] = acc;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+template <typename T>
+__device__ int batch_solve_one(T *A, int n, T *B, int64_t ldb, int m, T *sD, T *sP, int *s_fail) {
+    const int f = batch_factor<T>(A, n, sD, sP, s_fail);
+    if (f >= 0) return f;
+    batch_trsolve<T>(A, n, B, ldb, m, sD, sP);
+    return -1;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256, 2) batch_posv_kernel(const BatchItem *__restrict__ items, int64_t count, T *Apool,
                                   T *Bpool, int32_t *info, int *counter) {
@@ -88,8 +233,128 @@ __global__ void __launch_bounds__(256, 2) batch_posv_kernel(const BatchItem *__r
     T *sD = (T *)smem_raw;  // [32][33] diagonal block
     T *sP = sD + 32 * 33;   // [kBMaxN][33] panel / block rows (row r at sP[r * 33])
     __shared__ int s_item, s_fail;
-    const int tid = threadIdx.x, nthr = blockDim.x, warp = tid >> 5, lane = tid & 31;
-    const int nwarps = nthr >> 5;
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(counter, 1);
+        __syncthreads();
+        const int64_t it = s_item;
+        if (it >= count) break;
+        const BatchItem w = items[it];
+        const int f = batch_solve_one<T>(Apool + w.a_off, w.n, Bpool + w.b_off, w.n, w.m, sD, sP, &s_fail);
+        if (tid == 0) info[w.idx] = f;
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// f64 systems through an FP32 factorisation with FP64 refinement, per system
+//
+// One CTA per system, as above: the lower triangle of A (FP64, read only) is
+// copied to FP32 scratch and factored there; x = 0, r = b; each iteration
+// solves L L^T d = fp32(r) in FP32, adds d to x in FP64 and forms
+// r = b - A x in FP64 from the lower triangle of A (row sums for k <= i by
+// one thread per row, the mirrored part k > i by one warp per column, both
+// coalesced).  It stops when the normwise backward error
+// max_j ||r_j|| / (||A|| ||x_j|| + ||b_j||) reaches kBRefTol, or stops
+// improving.  A system whose FP32 factorisation breaks down, or that ends
+// above 10 n eps, is solved again by the plain FP64 routine (whose verdict
+// stands) from a working copy of A.  FP64 arithmetic is the scarce resource
+// on this GPU: the factorisation (n^3/3) moves to the FP32 pipe and only
+// 2 n^2 m per iteration stays in FP64.
+constexpr int kBRefIters = 6;
+constexpr double kBRefTol = 4.0 * 2.220446049250313e-16;
+constexpr size_t kBRefScratch = (size_t)kBMaxN * kBMaxN * 8 + (size_t)kBMaxN * kBMaxRhs * (4 + 8);
+
+__device__ __forceinline__ double block_max_double(double v, double *red) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, red[w]);
+    return r;
+}
+
+// out[i + j n] (+)= sign * sum_k A_sym(i, k) X[k][j] for the lower triangle of A
+// (ld n); X in shared memory, sX[k * kBMaxRhs + j].  mode 0: out = B - A X;
+// mode 1: out = sum_k |A_sym(i, k)| (row sums, m = 1, X unused).
+__device__ void sym_rows(const double *A, int n, const double *sX, int m, const double *B, double *out,
+                         bool rowsum) {
+    const int tid = threadIdx.x, nthr = blockDim.x, warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
+    // k <= i: one thread per row, consecutive rows read consecutive addresses
+    for (int i = tid; i < n; i += nthr) {
+        double acc[kBMaxRhs];
+#pragma unroll
+        for (int j = 0; j < kBMaxRhs; ++j) acc[j] = 0.0;
+        for (int k = 0; k <= i; ++k) {
+            const double a = A[i + (int64_t)k * n];
+            if (rowsum) {
+                acc[0] += fabs(a);
+            } else {
+#pragma unroll
+                for (int j = 0; j < kBMaxRhs; ++j)
+                    if (j < m) acc[j] = fma(a, sX[k * kBMaxRhs + j], acc[j]);
+            }
+        }
+        if (rowsum) {
+            out[i] = acc[0];
+        } else {
+#pragma unroll
+            for (int j = 0; j < kBMaxRhs; ++j)
+                if (j < m) out[i + (int64_t)j * n] = B[i + (int64_t)j * n] - acc[j];
+        }
+    }
+    __syncthreads();
+    // k > i: A(k, i) is column i of the lower triangle; one warp per column
+    for (int i = warp; i < n; i += nwarps) {
+        double acc[kBMaxRhs];
+#pragma unroll
+        for (int j = 0; j < kBMaxRhs; ++j) acc[j] = 0.0;
+        for (int k = i + 1 + lane; k < n; k += 32) {
+            const double a = A[k + (int64_t)i * n];
+            if (rowsum) {
+                acc[0] += fabs(a);
+            } else {
+#pragma unroll
+                for (int j = 0; j < kBMaxRhs; ++j)
+                    if (j < m) acc[j] = fma(a, sX[k * kBMaxRhs + j], acc[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kBMaxRhs; ++j)
+#pragma unroll
+            for (int o = 16; o; o >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
+        if (lane == 0) {
+            if (rowsum) {
+                out[i] += acc[0];
+            } else {
+#pragma unroll
+                for (int j = 0; j < kBMaxRhs; ++j)
+                    if (j < m) out[i + (int64_t)j * n] -= acc[j];
+            }
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256, 2) batch_posv_refined_kernel(const BatchItem *__restrict__ items, int64_t count,
+                                                                   const double *Apool, double *Bpool,
+                                                                   int32_t *info, int *counter, char *scratch) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *sDd = (double *)smem_raw;  // FP64 fallback: [32][33] + [kBMaxN][33]
+    float *sDf = (float *)smem_raw;    // FP32 factor and solves (same space)
+    double *sX = (double *)(smem_raw + sizeof(double) * (32 * 33 + kBMaxN * 33));  // [kBMaxN][kBMaxRhs]
+    __shared__ int s_item, s_fail;
+    __shared__ double red[8];
+    __shared__ double s_cx[kBMaxRhs], s_cr[kBMaxRhs], s_cb[kBMaxRhs];
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    char *base = scratch + (size_t)blockIdx.x * kBRefScratch;
+    float *W = (float *)base;  // FP32 factor (ld n); the FP64 fallback's working copy uses the same space
+    double *Wd = (double *)base;
+    float *R32 = (float *)(base + (size_t)kBMaxN * kBMaxN * 8);
+    double *R = (double *)(R32 + kBMaxN * kBMaxRhs);
     for (;;) {
         if (tid == 0) s_item = atomicAdd(counter, 1);
         __syncthreads();
@@ -97,132 +362,205 @@ __global__ void __launch_bounds__(256, 2) batch_posv_kernel(const BatchItem *__r
         if (it >= count) break;
         const BatchItem w = items[it];
         const int n = w.n, m = w.m;
-        T *A = Apool + w.a_off;
-        T *B = Bpool + w.b_off;
-        if (tid == 0) s_fail = -1;
-        // ---- factor: right-looking, 32-column blocks ----
-        for (int kb = 0; kb < n; kb += kBNb) {
-            const int bs = min(kBNb, n - kb);
-            for (int e = tid; e < 32 * 32; e += nthr) {
-                const int r = e % 32, c = e / 32;
-                if (r < bs && c <= r) sD[r * 33 + c] = A[(kb + r) + (int64_t)(kb + c) * n];
-            }
-            __syncthreads();
-            if (warp == 0) {
-                const int f = warp_potrf32(sD, bs, lane);
-                if (lane == 0 && f >= 0) s_fail = kb + f;
-            }
-            __syncthreads();
-            if (s_fail >= 0) break;
-            for (int e = tid; e < 32 * 32; e += nthr) {
-                const int r = e % 32, c = e / 32;
-                if (r < bs && c <= r) A[(kb + r) + (int64_t)(kb + c) * n] = sD[r * 33 + c];
-            }
-            // panel: each row below the block solves against L_kk
-            const int q = kb + bs, rows = n - q;
-            for (int rr = tid; rr < rows; rr += nthr) {
-                const int r = q + rr;
-                T v[32];
-#pragma unroll
-                for (int c = 0; c < 32; ++c) v[c] = (c < bs) ? A[r + (int64_t)(kb + c) * n] : T(0);
-#pragma unroll
-                for (int c = 0; c < 32; ++c) {
-                    if (c < bs) {
-                        v[c] = v[c] / sD[c * 33 + c];
-#pragma unroll
-                        for (int c2 = c + 1; c2 < 32; ++c2)
-                            if (c2 < bs) v[c2] = fma(-v[c], sD[c2 * 33 + c], v[c2]);
-                    }
-                }
-#pragma unroll
-                for (int c = 0; c < 32; ++c) {
-                    if (c < bs) {
-                        sP[rr * 33 + c] = v[c];
-                        A[r + (int64_t)(kb + c) * n] = v[c];
-                    }
-                }
-            }
-            __syncthreads();
-            // trailing lower triangle, one column per warp, lanes over rows:
-            // A[i,j] -= sum_t P[i][t] P[j][t]
-            for (int j = warp; j < rows; j += nwarps) {
-                for (int i = j + lane; i < rows; i += 32) {
-                    T acc = A[(q + i) + (int64_t)(q + j) * n];
-#pragma unroll 8
-                    for (int t = 0; t < bs; ++t) acc = fma(-sP[i * 33 + t], sP[j * 33 + t], acc);
-                    A[(q + i) + (int64_t)(q + j) * n] = acc;
-                }
-            }
-            __syncthreads();
+        const double *A = Apool + w.a_off;
+        double *B = Bpool + w.b_off;
+        for (int64_t e = tid; e < (int64_t)n * n; e += nthr) {
+            const int i = (int)(e % n), k = (int)(e / n);
+            if (i >= k) W[e] = (float)A[e];
         }
-        if (s_fail >= 0) {
-            if (tid == 0) info[w.idx] = s_fail;
-            __syncthreads();
-            continue;
+        // ||A||_inf and ||b_j||_inf
+        sym_rows(A, n, nullptr, 1, nullptr, R, true);
+        double an = 0.0;
+        for (int i = tid; i < n; i += nthr) an = fmax(an, R[i]);
+        an = block_max_double(an, red);
+        for (int j = 0; j < m; ++j) {
+            double v = 0.0;
+            for (int i = tid; i < n; i += nthr) v = fmax(v, fabs(B[i + (int64_t)j * n]));
+            v = block_max_double(v, red);
+            if (tid == 0) s_cb[j] = v;
         }
-        // ---- solve L y = b (forward), then L^T x = y (backward), 32-row blocks ----
-        for (int pass = 0; pass < 2; ++pass) {
-            const bool fwd = pass == 0;
-            const int nblk = (n + kBNb - 1) / kBNb;
-            for (int bi = 0; bi < nblk; ++bi) {
-                const int kb = (fwd ? bi : nblk - 1 - bi) * kBNb;
-                const int bs = min(kBNb, n - kb);
-                for (int e = tid; e < 32 * 32; e += nthr) {
-                    const int r = e % 32, c = e / 32;
-                    if (r < bs && c <= r) sD[r * 33 + c] = A[(kb + r) + (int64_t)(kb + c) * n];
+        __syncthreads();
+        int f = batch_factor<float>(W, n, sDf, sDf + 32 * 33, &s_fail);
+        bool ok = f < 0;
+        if (ok) {
+            for (int e = tid; e < n * kBMaxRhs; e += nthr) sX[e] = 0.0;
+            for (int64_t e = tid; e < (int64_t)n * m; e += nthr) R[e] = B[e];
+            __syncthreads();
+            double eta = INFINITY, eta_prev = INFINITY;
+            for (int itr = 0; itr < kBRefIters; ++itr) {
+                for (int64_t e = tid; e < (int64_t)n * m; e += nthr) R32[e] = (float)R[e];
+                __syncthreads();
+                batch_trsolve<float>(W, n, R32, n, m, sDf, sDf + 32 * 33);
+                for (int64_t e = tid; e < (int64_t)n * m; e += nthr) {
+                    const int i = (int)(e % n), j = (int)(e / n);
+                    sX[i * kBMaxRhs + j] += (double)R32[e];
                 }
                 __syncthreads();
-                // warp k solves right-hand side k on this block (lane = row)
-                for (int k = warp; k < m; k += nwarps) {
-                    T x = (lane < bs) ? B[(kb + lane) + (int64_t)k * n] : T(0);
-                    if (fwd) {
-#pragma unroll
-                        for (int c = 0; c < 32; ++c) {
-                            if (c < bs) {
-                                const T xc = shfl(x, c) / sD[c * 33 + c];
-                                if (lane == c) x = xc;
-                                if (lane > c && lane < bs) x = fma(-xc, sD[lane * 33 + c], x);
-                            }
-                        }
-                    } else {
-#pragma unroll
-                        for (int cc = 31; cc >= 0; --cc) {
-                            if (cc < bs) {
-                                const T xc = shfl(x, cc) / sD[cc * 33 + cc];
-                                if (lane == cc) x = xc;
-                                if (lane < cc) x = fma(-xc, sD[cc * 33 + lane], x);
-                            }
-                        }
+                sym_rows(A, n, sX, m, B, R, false);
+                double e_max = 0.0;
+                for (int j = 0; j < m; ++j) {
+                    double vx = 0.0, vr = 0.0;
+                    for (int i = tid; i < n; i += nthr) {
+                        vx = fmax(vx, fabs(sX[i * kBMaxRhs + j]));
+                        vr = fmax(vr, fabs(R[i + (int64_t)j * n]));
                     }
-                    if (lane < bs) B[(kb + lane) + (int64_t)k * n] = x;
+                    vx = block_max_double(vx, red);
+                    vr = block_max_double(vr, red);
+                    const double den = an * vx + s_cb[j];
+                    double ej = den > 0 ? vr / den : (vr > 0 ? INFINITY : 0.0);
+                    if (ej != ej) ej = INFINITY;
+                    e_max = fmax(e_max, ej);
                 }
-                // stage the block's coupling to the remaining rows: forward needs
-                // L[r][kb+t] for r >= kb+bs, backward L[kb+t][r] for r < kb
-                const int q = fwd ? kb + bs : 0, rows = fwd ? n - kb - bs : kb;
-                for (int e = tid; e < rows * bs; e += nthr) {
-                    if (fwd) {
-                        const int rr = e % rows, t = e / rows;  // consecutive rr: contiguous column
-                        sP[rr * 33 + t] = A[(q + rr) + (int64_t)(kb + t) * n];
-                    } else {
-                        const int t = e % bs, rr = e / bs;  // consecutive t: contiguous column rr
-                        sP[rr * 33 + t] = A[(kb + t) + (int64_t)rr * n];
-                    }
+                eta = e_max;  // uniform across the CTA
+                if (eta <= kBRefTol || !(eta < INFINITY) || (itr >= 2 && eta > 0.5 * eta_prev)) break;
+                eta_prev = eta;
+            }
+            ok = eta <= 10.0 * n * 2.220446049250313e-16;
+            if (ok) {
+                for (int64_t e = tid; e < (int64_t)n * m; e += nthr) {
+                    const int i = (int)(e % n), j = (int)(e / n);
+                    B[e] = sX[i * kBMaxRhs + j];
                 }
-                __syncthreads();
-                for (int e = tid; e < rows * m; e += nthr) {
-                    const int rr = e % rows, k = e / rows;
-                    T acc = B[(q + rr) + (int64_t)k * n];
-#pragma unroll 8
-                    for (int t = 0; t < bs; ++t)
-                        acc = fma(-sP[rr * 33 + t], B[(kb + t) + (int64_t)k * n], acc);
-                    B[(q + rr) + (int64_t)k * n] = acc;
-                }
-                __syncthreads();
             }
         }
-        if (tid == 0) info[w.idx] = -1;
+        if (!ok) {  // plain FP64 from a working copy of A (B still holds b)
+            __syncthreads();
+            for (int64_t e = tid; e < (int64_t)n * n; e += nthr) {
+                const int i = (int)(e % n), k = (int)(e / n);
+                if (i >= k) Wd[e] = A[e];
+            }
+            __syncthreads();
+            f = batch_solve_one<double>(Wd, n, B, n, m, sDd, sDd + 32 * 33, &s_fail);
+        } else {
+            f = -1;
+        }
+        if (tid == 0) info[w.idx] = f;
         __syncthreads();
     }
+}
+
+size_t batch_refined_smem() { return sizeof(double) * (32 * 33 + kBMaxN * 33 + kBMaxN * kBMaxRhs); }
+size_t batch_refined_scratch_bytes(int ctas) { return (size_t)ctas * kBRefScratch; }
+
+// ---------------------------------------------------------------------------
+// device-resident serving loop
+
+__device__ __forceinline__ unsigned long long ld_acquire_sys_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_sys_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Persistent CTAs of 256 threads.  Thread 0 claims the next published ticket
+// (compare-and-swap on the device counter, so a ticket is claimed at most once
+// and only after the host published it), the CTA copies the lower triangle of
+// A into its scratch (ld = n) and solves in place with the batched routine;
+// thread 0 then publishes the outcome.  Every wait is bounded: an idle CTA
+// returns after idle_ns without work (the host relaunches the loop when new
+// requests arrive), at once when ring->stop is set.
+__global__ void __launch_bounds__(256) serve_loop_kernel(ServeRing *ring, unsigned long long *next,
+                                                        double *scratch, unsigned long long idle_ns) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ long long s_ticket;
+    __shared__ int s_fail;
+    __shared__ ServeReq s_req;
+    const int tid = threadIdx.x;
+    double *myA = scratch + (size_t)blockIdx.x * kBMaxN * kBMaxN;
+    for (;;) {
+        if (tid == 0) {
+            long long claim = -1;
+            const unsigned long long t_idle = globaltimer_ns();
+            unsigned sleep_ns = 64;
+            for (;;) {
+                const unsigned long long cur = atomicAdd(next, 0ull);
+                const unsigned long long pub = ld_acquire_sys_u64(&ring->published);
+                if (cur < pub) {
+                    if (atomicCAS(next, cur, cur + 1) == cur) {
+                        claim = (long long)cur;
+                        break;
+                    }
+                    continue;
+                }
+                if (*(volatile int *)&ring->stop) break;
+                if (globaltimer_ns() - t_idle > idle_ns) break;
+                __nanosleep(sleep_ns);
+                if (sleep_ns < 2048) sleep_ns *= 2;
+            }
+            s_ticket = claim;
+            if (claim >= 0) {
+                // the host wrote the slot before it raised `published` (acquired above)
+                const ServeReq *q = &ring->req[claim % kServeRing];
+                s_req.A = *(void *const volatile *)&q->A;
+                s_req.B = *(void *volatile *)&q->B;
+                s_req.lda = *(volatile const int64_t *)&q->lda;
+                s_req.ldb = *(volatile const int64_t *)&q->ldb;
+                s_req.n = *(volatile const int32_t *)&q->n;
+                s_req.m = *(volatile const int32_t *)&q->m;
+                s_req.dtype = *(volatile const int32_t *)&q->dtype;
+            }
+        }
+        __syncthreads();
+        const long long t = s_ticket;
+        if (t < 0) break;
+        const ServeReq q = s_req;
+        const int n = q.n;
+        int f;
+        if (q.dtype == 8) {
+            double *W = myA;
+            const double *A = (const double *)q.A;
+            for (int64_t e = tid; e < (int64_t)n * n; e += blockDim.x) {
+                const int i = (int)(e % n), j = (int)(e / n);
+                if (i >= j) W[e] = A[i + (int64_t)j * q.lda];
+            }
+            __syncthreads();
+            double *sD = (double *)smem_raw;
+            f = batch_solve_one<double>(W, n, (double *)q.B, q.ldb, q.m, sD, sD + 32 * 33, &s_fail);
+        } else {
+            float *W = (float *)myA;
+            const float *A = (const float *)q.A;
+            for (int64_t e = tid; e < (int64_t)n * n; e += blockDim.x) {
+                const int i = (int)(e % n), j = (int)(e / n);
+                if (i >= j) W[e] = A[i + (int64_t)j * q.lda];
+            }
+            __syncthreads();
+            float *sD = (float *)smem_raw;
+            f = batch_solve_one<float>(W, n, (float *)q.B, q.ldb, q.m, sD, sD + 32 * 33, &s_fail);
+        }
+        __syncthreads();  // every thread's writes of X precede the publication
+        if (tid == 0) {
+            const int slot = (int)(t % kServeRing);
+            __threadfence_system();
+            *(volatile int32_t *)&ring->status[slot] = f >= 0 ? 1 : 0;
+            *(volatile int64_t *)&ring->fail_row[slot] = f;
+            st_release_sys_u64(&ring->done_seq[slot], (unsigned long long)t + 1);
+        }
+    }
+}
+
+size_t serve_loop_scratch_bytes(int ctas) { return (size_t)ctas * kBMaxN * kBMaxN * sizeof(double); }
+
+int serve_loop_launch(ServeRing *ring_dev, unsigned long long *d_next, double *scratch, int ctas,
+                      double idle_us, cudaStream_t st) {
+    const size_t smem = sizeof(double) * (32 * 33 + kBMaxN * 33);
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(serve_loop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return -1;
+        attr = true;
+    }
+    LaunchScope ls(K_BATCH, st);
+    serve_loop_kernel<<<(unsigned)ctas, 256, smem, st>>>(ring_dev, d_next, scratch,
+                                                         (unsigned long long)(idle_us * 1e3));
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 }  // namespace lla
@@ -243,6 +581,8 @@ struct lla_batch_plan {
     int *d_counter = nullptr;
     int ctas_per_sm = 2, threads = 256;
     bool tuned = false;
+    bool refined = false;   // f64 systems through an FP32 factor + FP64 refinement (A read only)
+    char *d_scratch = nullptr;  // per-CTA scratch of the refined mode
     std::string key;
     // graph replay cache
     cudaGraphExec_t gexec = nullptr;
@@ -333,8 +673,20 @@ template int batch_launch_raw<float>(const BatchItem *, int64_t, float *, float 
 
 }  // namespace lla
 
+// The refined mode's CTAs per SM are limited by its shared memory (two fit).
+static int refined_ctas_per_sm(int cps) { return std::min(cps, 2); }
+
 template <typename T>
 static cudaError_t batch_launch(lla_batch_plan *p, T *dA, T *dB, int32_t *d_info, cudaStream_t st) {
+    if (p->refined && sizeof(T) == 8) {
+        if (cudaMemsetAsync(p->d_counter, 0, sizeof(int), st) != cudaSuccess) return cudaGetLastError();
+        const int cps = refined_ctas_per_sm(p->ctas_per_sm);
+        const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(p->count, (int64_t)cps * sm_count()));
+        LaunchScope ls(K_BATCH, st, p->flops);
+        batch_posv_refined_kernel<<<grid, p->threads, batch_refined_smem(), st>>>(
+            p->d_items, p->count, (const double *)dA, (double *)dB, d_info, p->d_counter, p->d_scratch);
+        return cudaGetLastError();
+    }
     if (batch_launch_raw<T>(p->d_items, p->count, dA, dB, d_info, p->d_counter, p->ctas_per_sm,
                             p->threads, p->flops, st) == 0)
         return cudaSuccess;
@@ -422,6 +774,7 @@ int lla_batch_plan_create(int64_t count, const int32_t *n, const int32_t *m, int
 void lla_batch_plan_destroy(lla_batch_plan *p) {
     if (!p) return;
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    if (p->d_scratch) cudaFree(p->d_scratch);
     cudaFree(p->d_items);
     cudaFree(p->d_counter);
     delete p;
@@ -449,6 +802,46 @@ int lla_batch_set_shape(lla_batch_plan *p, int ctas_per_sm, int threads) {
         if (p->gexec) {
             cudaGraphExecDestroy(p->gexec);
             p->gexec = nullptr;
+        }
+    }
+    return LLA_OK;
+}
+
+// Switches an f64 plan between the plain FP64 solve (A factored in place) and
+// the FP32 factorisation with per-system FP64 refinement (A read only).
+int lla_batch_set_refined(lla_batch_plan *p, int refined, lla_error *err) {
+    if (!p || (refined && p->dtype != 8)) return lla__set_status(err, LLA_ERR_INVALID_ARG);
+    lla__set_status(err, LLA_OK);
+    const bool want = refined != 0;
+    if (want && !p->d_scratch) {
+        static bool attr = false;
+        if (!attr) {
+            const cudaError_t e = cudaFuncSetAttribute(batch_posv_refined_kernel,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       (int)batch_refined_smem());
+            if (e != cudaSuccess) return lla__set_cuda_error(err, e);
+            attr = true;
+        }
+        const cudaError_t e = cudaMalloc(&p->d_scratch, batch_refined_scratch_bytes(2 * sm_count()));
+        if (e != cudaSuccess) {
+            p->d_scratch = nullptr;
+            return lla__set_cuda_error(err, e);
+        }
+    }
+    if (p->refined != want) {
+        p->refined = want;
+        if (p->gexec) {
+            cudaGraphExecDestroy(p->gexec);
+            p->gexec = nullptr;
+        }
+        // the launch shape is cached per mode
+        p->key += want ? ":r" : "";
+        if (!want && p->key.size() > 2 && p->key.compare(p->key.size() - 2, 2, ":r") == 0)
+            p->key.resize(p->key.size() - 2);
+        int cps, thr;
+        if (cache_lookup(p->key, cps, thr)) {
+            p->ctas_per_sm = cps;
+            p->threads = thr;
         }
     }
     return LLA_OK;
@@ -549,6 +942,7 @@ int lla_batch_autotune(lla_batch_plan *p, void *dA, void *dB, int32_t *d_info, v
     for (const auto &c : cands) {
         if (e != cudaSuccess) break;
         if (smem * c[0] > 227 * 1024) continue;  // does not fit on one SM
+        if (p->refined && c[0] > 2) continue;      // the refined kernel fits two CTAs per SM
         p->ctas_per_sm = c[0];
         p->threads = c[1];
         float tbest = 1e30f;

@@ -44,6 +44,37 @@ template <typename T>
 int batch_launch_raw(const BatchItem *d_items, int64_t count, T *dA, T *dB, int32_t *d_info,
                      int *d_counter, int ctas_per_sm, int threads, double flops, cudaStream_t st);
 
+// Device-resident serving loop (lla_batch.cu, driven by lla_serve.cpp).
+// The request ring lives in pinned host memory mapped into the device's
+// address space: the host writes a request into slot t % kServeRing and then
+// raises `published` to t + 1 (release); persistent CTAs claim tickets from a
+// device counter, solve the request in place (A copied into per-CTA scratch,
+// B overwritten with X) and publish status, failing row and done_seq = t + 1
+// (system-scope release).  A slot is reused only after its ticket completed.
+constexpr int kServeRing = 1024;
+struct ServeReq {
+    const void *A;
+    void *B;
+    int64_t lda, ldb;
+    int32_t n, m, dtype, pad;
+};
+struct ServeRing {
+    unsigned long long published;  // host: tickets [0, published) are written
+    int stop;                      // host: idle CTAs return at once
+    int pad;
+    ServeReq req[kServeRing];
+    int32_t status[kServeRing];         // device: 0 solved, 1 not positive definite
+    int64_t fail_row[kServeRing];       // device: first failing row, or -1
+    unsigned long long done_seq[kServeRing];  // device: ticket + 1 once finished
+};
+// Persistent loop of `ctas` CTAs on `st`: each claims tickets (device counter
+// *d_next) and solves them; a CTA returns after about idle_us microseconds
+// without work, or at once when ring->stop is set.  scratch: ctas x 256^2
+// doubles for the working copies of A.
+int serve_loop_launch(ServeRing *ring_dev, unsigned long long *d_next, double *scratch, int ctas,
+                      double idle_us, cudaStream_t st);
+size_t serve_loop_scratch_bytes(int ctas);
+
 // Layout kernels (lla_layout.cu).
 enum ExportMode { EXPORT_FULL = 0, EXPORT_LOWER = 1, EXPORT_LOWER_ZERO_UPPER = 2, EXPORT_FAIL = 3 };
 // W[i + j*ld] = R[i*rs + j*cs] for i < rows, j < cols.
@@ -62,6 +93,8 @@ int mask_launch(T *R, int64_t rs, int64_t cs, int64_t n, int uplo, cudaStream_t 
 template <typename T>
 int is_triangular_launch(const T *R, int64_t rs, int64_t cs, int64_t n, int uplo, int *d_flag,
                          cudaStream_t st);
+// *p = v (one device int).
+int fill_int_launch(int *p, int v, cudaStream_t st);
 // W = identity (n x n, ld).
 template <typename T>
 int eye_launch(T *W, int64_t ld, int64_t n, cudaStream_t st);

@@ -94,6 +94,14 @@ __global__ void eye_kernel(T *W, int64_t ld, int64_t n) {
     for (int64_t j = blockIdx.y; j < n; j += gridDim.y) W[i + j * ld] = (i == j) ? T(1) : T(0);
 }
 
+__global__ void fill_int_kernel(int *p, int v) { *p = v; }
+
+int fill_int_launch(int *p, int v, cudaStream_t st) {
+    LaunchScope ls(K_MISC, st);
+    fill_int_kernel<<<1, 1, 0, st>>>(p, v);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 static dim3 tiles2d(int64_t rows, int64_t cols) {
     return dim3((unsigned)ceil_div(rows, 32), (unsigned)ceil_div(cols, 32));
 }

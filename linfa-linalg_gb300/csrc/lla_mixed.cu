@@ -45,13 +45,16 @@ __device__ __forceinline__ double warp_max(double v) {
 // s_i = 2^-floor(log2(a_ii)/2); a non-positive or non-finite diagonal marks
 // the matrix as not factorable in low precision (the FP64 path decides).
 __global__ void equil_scale_kernel(const double *A, int64_t lda, int64_t n, int scale, double *s,
-                                   int *bad) {
+                                   int *bad, int64_t *info) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double a = A[i + i * lda];
     if (!(a > 0.0) || !isfinite(a)) {
         s[i] = 1.0;
         atomicExch(bad, 1);
+        // the low-precision factorisation is skipped (its kernels return at once
+        // once *info >= 0) and the FP64 fallback decides
+        if (info) atomicExch((unsigned long long *)info, 0ull);
         return;
     }
     if (!scale) {
@@ -197,7 +200,8 @@ __global__ void colmax_kernel(const double *M, int64_t ld, int64_t n, int64_t m,
 
 // Y = fp32(s .* R)   (n x m, column-major; ld of Y = n)
 __global__ void scale_to_f32_kernel(const double *R, int64_t ldr, const double *s, int64_t n,
-                                    int64_t m, float *Y) {
+                                    int64_t m, float *Y, const int *state) {
+    if (refine_done(state)) return;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t j = blockIdx.y;
     if (i < n && j < m) Y[i + j * n] = (float)(s[i] * R[i + j * ldr]);
@@ -205,7 +209,8 @@ __global__ void scale_to_f32_kernel(const double *R, int64_t ldr, const double *
 
 // X += s .* Y (FP64), and colmax_x[j] = max_i |X[i,j]|
 __global__ void update_x_kernel(double *X, int64_t ldx, const double *s, const float *Y, int64_t n,
-                                int64_t m, double *colmax_x) {
+                                int64_t m, double *colmax_x, const int *state) {
+    if (refine_done(state)) return;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t j = blockIdx.y;
     double v = 0.0;
@@ -233,7 +238,8 @@ __global__ void __launch_bounds__(128) residual_dmma_kernel(const double *__rest
                                                             int64_t ldx, const double *__restrict__ B,
                                                             int64_t ldb, double *R, int64_t ldr,
                                                             int64_t m, double *colmax_r, int splits,
-                                                            double *P) {
+                                                            double *P, const int *state) {
+    if (refine_done(state)) return;
     __shared__ double As[kResK][kResRows + 4];  // [k][row], stride 36 = 4 (mod 16)
     __shared__ double Xs[kResK][kResCols + 4];  // [k][col], stride 68 = 4 (mod 16)
     const int64_t i0 = (int64_t)blockIdx.x * kResRows;
@@ -335,7 +341,8 @@ __global__ void __launch_bounds__(128) residual_dmma_kernel(const double *__rest
 // R = B - (P[0] + P[1] + ...), summed in split order; and column maxima of |R|.
 __global__ void residual_combine_kernel(const double *__restrict__ P, int splits, const double *B,
                                         int64_t ldb, double *R, int64_t ldr, int64_t n, int64_t m,
-                                        double *colmax_r) {
+                                        double *colmax_r, const int *state) {
+    if (refine_done(state)) return;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t j = blockIdx.y;
     double v = 0.0;
@@ -357,10 +364,10 @@ static unsigned gx(int64_t n, int b) { return (unsigned)ceil_div(n, b); }
 
 int equilibrate_launch(const double *A, int64_t lda, int64_t n, bool scale, double *s, float *W,
                        int64_t ldw, double *rowsum, double *anorm, double *rowmax, double *part, int *bad,
-                       cudaStream_t st) {
+                       cudaStream_t st, int64_t *info) {
     {
         LaunchScope ls(K_MIXED_CONVERT, st, 8.0 * n);
-        equil_scale_kernel<<<gx(n, 256), 256, 0, st>>>(A, lda, n, scale ? 1 : 0, s, bad);
+        equil_scale_kernel<<<gx(n, 256), 256, 0, st>>>(A, lda, n, scale ? 1 : 0, s, bad, info);
     }
     const int64_t R = (n + kSymT - 1) / kSymT;
     if (R > 65535) return -1;
@@ -392,16 +399,85 @@ int colmax_launch(const double *M, int64_t ld, int64_t n, int64_t m, double *col
 }
 
 int scale_to_f32_launch(const double *R, int64_t ldr, const double *s, int64_t n, int64_t m, float *Y,
-                        cudaStream_t st) {
+                        cudaStream_t st, const int *state) {
     LaunchScope ls(K_REFINE, st, 12.0 * n * m);
-    scale_to_f32_kernel<<<dim3(gx(n, 256), (unsigned)m), 256, 0, st>>>(R, ldr, s, n, m, Y);
+    scale_to_f32_kernel<<<dim3(gx(n, 256), (unsigned)m), 256, 0, st>>>(R, ldr, s, n, m, Y, state);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 int update_x_launch(double *X, int64_t ldx, const double *s, const float *Y, int64_t n, int64_t m,
-                    double *colmax_x, cudaStream_t st) {
+                    double *colmax_x, cudaStream_t st, const int *state) {
     LaunchScope ls(K_REFINE, st, 20.0 * n * m);
-    update_x_kernel<<<dim3(gx(n, 256), (unsigned)m), 256, 0, st>>>(X, ldx, s, Y, n, m, colmax_x);
+    update_x_kernel<<<dim3(gx(n, 256), (unsigned)m), 256, 0, st>>>(X, ldx, s, Y, n, m, colmax_x, state);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+// Refinement control on the device.  Control words (as doubles): [0] ||A||_inf,
+// [2] int64 info of the low-precision factor, [4] int state | int iterations,
+// [5] eta, [6] eta of the previous iteration, [7] eta after the first solve,
+// [8 ..) column maxima of |r|, |x| and |b|.  state: 0 refining, 1 converged,
+// 2 stalled or out of iterations, 3 the low-precision factorisation failed.
+// Every per-iteration kernel returns at once when state != 0, so the host can
+// enqueue several iterations ahead and synchronise once per group.
+__global__ void refine_begin_kernel(double *words) {
+    int *st = (int *)(words + 4);
+    st[0] = (*(const int64_t *)(words + 2) >= 0) ? 3 : 0;
+    st[1] = 0;
+}
+
+// eta = max_j ||r_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf); converged when
+// eta <= tol; stalled when eta is not finite, or does not halve over an
+// iteration after the second, or max_iters ran out.  While refining, the
+// column maxima of |r| and |x| are cleared for the next iteration.
+__global__ void __launch_bounds__(256) refine_check_kernel(double *words, int64_t m, double tol, int max_iters) {
+    int *st = (int *)(words + 4);
+    if (*(volatile int *)st != 0) return;
+    __shared__ double red[8];
+    __shared__ int s_go;
+    const int tid = threadIdx.x;
+    const double an = words[0];
+    const double *cr = words + 8, *cx = cr + m, *cb = cx + m;
+    double e = 0.0;
+    for (int64_t j = tid; j < m; j += blockDim.x) {
+        const double den = an * cx[j] + cb[j];
+        double ej = den > 0 ? cr[j] / den : (cr[j] > 0 ? INFINITY : 0.0);
+        if (ej != ej) ej = INFINITY;
+        e = fmax(e, ej);
+    }
+    e = warp_max(e);
+    if ((tid & 31) == 0) red[tid >> 5] = e;
+    __syncthreads();
+    if (tid == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) e = fmax(e, red[w]);
+        const int it = st[1] + 1;
+        st[1] = it;
+        words[5] = e;
+        if (it == 1) words[7] = e;
+        int state = 0;
+        if (e <= tol)
+            state = 1;
+        else if (!isfinite(e) || (it >= 3 && e > 0.5 * words[6]) || it >= max_iters)
+            state = 2;
+        if (state == 0) words[6] = e;
+        st[0] = state;
+        s_go = state == 0;
+    }
+    __syncthreads();
+    if (s_go) {
+        double *c = words + 8;
+        for (int64_t j = tid; j < 2 * m; j += blockDim.x) c[j] = 0.0;
+    }
+}
+
+int refine_begin_launch(double *words, cudaStream_t st) {
+    LaunchScope ls(K_MISC, st);
+    refine_begin_kernel<<<1, 1, 0, st>>>(words);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int refine_check_launch(double *words, int64_t m, double tol, int max_iters, cudaStream_t st) {
+    LaunchScope ls(K_MISC, st);
+    refine_check_kernel<<<1, 256, 0, st>>>(words, m, tol, max_iters);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -422,18 +498,18 @@ int residual_splits(int64_t n, int64_t m) {
 
 int residual_launch(const double *A, int64_t lda, int64_t n, const double *X, int64_t ldx,
                     const double *B, int64_t ldb, double *R, int64_t ldr, int64_t m, double *colmax_r,
-                    double *P, cudaStream_t st) {
+                    double *P, cudaStream_t st, const int *state) {
     const int splits = P ? residual_splits(n, m) : 1;
     {
         // algorithmic work: 2 n^2 m flops
         LaunchScope ls(K_RESIDUAL, st, 2.0 * n * n * m);
         residual_dmma_kernel<<<dim3(gx(n, kResRows), gx(m, kResCols), splits), 128, 0, st>>>(
-            A, lda, n, X, ldx, B, ldb, R, ldr, m, colmax_r, splits, P);
+            A, lda, n, X, ldx, B, ldb, R, ldr, m, colmax_r, splits, P, state);
     }
     if (splits > 1) {
         LaunchScope ls(K_REFINE, st, 8.0 * n * m * (splits + 2));
         residual_combine_kernel<<<dim3(gx(n, 256), (unsigned)m), 256, 0, st>>>(P, splits, B, ldb, R, ldr,
-                                                                             n, m, colmax_r);
+                                                                             n, m, colmax_r, state);
     }
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
@@ -462,6 +538,9 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 // Smallest pivot_k / a_kk that the FMA-order fallback factorisation accepts
 // without the exact-order re-run (the host-view entry points use the same guard).
 constexpr double kFallbackPivotGuard = 1e-10;
+// Refinement iterations enqueued before the first synchronisation (the usual
+// count for an FP32-accurate factor at kappa ~ 1e6), and per later group.
+constexpr int kRefineGroup = 4, kRefineGroupNext = 2;
 
 extern "C" void lla_refine_opts_default(lla_refine_opts *o) {
     if (!o) return;
@@ -566,7 +645,11 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
         MX_TRY(cudaMemcpyAsync(words, hw, sizeof(init), cudaMemcpyHostToDevice, st));
         MX_TRY(cudaMemsetAsync(colmax_r, 0, sizeof(double) * 3 * m, st));
     }
-    // 1. equilibrate (and ||A||_inf, ||b_j||_inf)
+    for (auto &e : w.ev)
+        if (!e) MX_TRY(cudaEventCreate(&e));
+    MX_TRY(cudaEventRecord(w.ev[0], st));
+    // 1. equilibrate (and ||A||_inf, ||b_j||_inf); a non-positive diagonal marks
+    // the low-precision factorisation as failed on the device (info >= 0)
     auto t0 = std::chrono::steady_clock::now();
     const bool slices = opts.residual == LLA_RESIDUAL_EXACT_SLICES;
     MX_TRY(w.sympart.ensure(sizeof(double) * sym_part_doubles(n)));
@@ -576,77 +659,74 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
         oz_rm = oz_rowmax(w.oz.p, n, m);
     }
     MX_TRY(last_err(equilibrate_launch(dA, lda, n, opts.equilibrate != 0, s, L, n,
-                                       (double *)w.rowsum.p, anorm, oz_rm, (double *)w.sympart.p, bad, st)));
+                                       (double *)w.rowsum.p, anorm, oz_rm, (double *)w.sympart.p, bad, st, info)));
     MX_TRY(last_err(colmax_launch(dB, ldb, n, m, colmax_b, st)));
-    // 2. low-precision factorisation
-    bool lowp_ok = true;
-    MX_TRY(read_words(4));
-    if (((int *)(hw + 3))[0] != 0) lowp_ok = false;
-    if (lowp_ok) {
-        int rc = lowp_factor_launch(L, n, n, opts, info, (float *)w.diag0.p, min_ratio, c, st);
-        MX_TRY(last_err(rc));
-        MX_TRY(read_words(4));
-        int64_t finfo;
-        std::memcpy(&finfo, hw + 2, sizeof(int64_t));
-        if (finfo >= 0) lowp_ok = false;
-    }
-    if (lowp_ok)  // inverses of the 64 x 64 diagonal blocks, reused by every substitution
-        MX_TRY(last_err(diag_inverse_launch(L, n, n, (float *)w.winv.p, st)));
-    if (lowp_ok && slices)  // slices of A, once per solve
+    // 2. low-precision factorisation (its kernels return at once after a breakdown)
+    MX_TRY(last_err(lowp_factor_launch(L, n, n, opts, info, (float *)w.diag0.p, min_ratio, c, st)));
+    // inverses of the 64 x 64 diagonal blocks, reused by every substitution
+    MX_TRY(last_err(diag_inverse_launch(L, n, n, (float *)w.winv.p, st)));
+    if (slices)  // slices of A, once per solve
         MX_TRY(last_err(oz_prepare(dA, lda, n, m, w.oz.p, true, st)));
-    r.ms_factor = ms_since(t0);
-    r.factor_failed = lowp_ok ? 0 : 1;
-    // 3. refinement
-    t0 = std::chrono::steady_clock::now();
-    double eta = INFINITY, eta_prev = INFINITY;
-    bool converged = false;
-    if (lowp_ok) {
-        for (int64_t j = 0; j < m; ++j)
-            MX_TRY(cudaMemsetAsync(dX + j * ldx, 0, sizeof(double) * n, st));
-        const double *rhs = dB;
-        int64_t ldrhs = ldb;
-        for (int it = 1; it <= opts.max_iters; ++it) {
-            // correction d = S L^-T L^-1 S r  (FP32), x += d
-            MX_TRY(last_err(scale_to_f32_launch(rhs, ldrhs, s, n, m, Y, st)));
-            MX_TRY(cudaMemsetAsync(err_word, 0, sizeof(int), st));
-            const float *Wi = (const float *)w.winv.p;
+    // 3. refinement, controlled on the device: every iteration ends with a check
+    // kernel that sets the state word; the host enqueues iterations in groups and
+    // synchronises once per group (all kernels of an iteration return at once
+    // when the state is no longer "refining")
+    MX_TRY(cudaEventRecord(w.ev[1], st));
+    int *state = (int *)(words + 4);
+    MX_TRY(last_err(refine_begin_launch(words, st)));
+    for (int64_t j = 0; j < m; ++j)
+        MX_TRY(cudaMemsetAsync(dX + j * ldx, 0, sizeof(double) * n, st));
+    MX_TRY(cudaMemsetAsync(err_word, 0, sizeof(int), st));
+    const float *Wi = (const float *)w.winv.p;
+    const int sub_cps = opts.sub_ctas_per_sm == 1 ? 1 : 2;
+    double eta = INFINITY;
+    bool converged = false, lowp_ok = true;
+    int enqueued = 0, group = kRefineGroup;
+    for (;;) {
+        for (int g = 0; g < group && enqueued < opts.max_iters; ++g, ++enqueued) {
+            // correction d = S L^-T L^-1 S r  (FP32), x += d; the first iteration solves with b
+            const double *rhs = enqueued == 0 ? dB : R;
+            const int64_t ldrhs = enqueued == 0 ? ldb : n;
+            MX_TRY(last_err(scale_to_f32_launch(rhs, ldrhs, s, n, m, Y, st, state)));
             MX_TRY(next_epoch());
-            MX_TRY(last_err(trsm_inv_launch(L, n, Wi, n, Y, n, m, 0, stage, w.stage_epoch, tws, err_word, st)));
+            MX_TRY(last_err(trsm_inv_launch(L, n, Wi, n, Y, n, m, 0, stage, w.stage_epoch, tws, err_word, st, state,
+                                            sub_cps)));
             MX_TRY(next_epoch());
-            MX_TRY(last_err(trsm_inv_launch(L, n, Wi, n, Y, n, m, 1, stage, w.stage_epoch, tws, err_word, st)));
-            MX_TRY(cudaMemsetAsync(colmax_r, 0, sizeof(double) * 2 * m, st));
-            MX_TRY(last_err(update_x_launch(dX, ldx, s, Y, n, m, colmax_x, st)));
-            // r = b - A x  (FP64)
+            MX_TRY(last_err(trsm_inv_launch(L, n, Wi, n, Y, n, m, 1, stage, w.stage_epoch, tws, err_word, st, state,
+                                            sub_cps)));
+            MX_TRY(last_err(update_x_launch(dX, ldx, s, Y, n, m, colmax_x, st, state)));
+            // r = b - A x  (FP64 accuracy)
             if (slices)
                 MX_TRY(last_err(oz_residual_launch(dX, ldx, dB, ldb, R, n, n, m, colmax_x, colmax_r,
-                                                   w.oz.p, err_word, st)));
+                                                   w.oz.p, err_word, st, state)));
             else
                 MX_TRY(last_err(residual_launch(dA, lda, n, dX, ldx, dB, ldb, R, n, m, colmax_r,
-                                                (double *)w.P.p, st)));
-            rhs = R;
-            ldrhs = n;
-            MX_TRY(read_words(8 + 3 * m));
-            if (((int *)(hw + 3))[1] != 0) return lla__set_status(err, LLA_ERR_TIMEOUT);
-            const double an = hw[0];
-            double e = 0.0;
-            for (int64_t j = 0; j < m; ++j) {
-                const double den = an * hw[8 + m + j] + hw[8 + 2 * m + j];
-                const double ej = den > 0 ? hw[8 + j] / den : (hw[8 + j] > 0 ? INFINITY : 0.0);
-                e = std::isnan(ej) ? INFINITY : std::max(e, ej);
-            }
-            eta = e;
-            r.iterations = it;
-            if (it == 1) r.backward_error0 = eta;
-            if (eta <= opts.tol) {
-                converged = true;
-                break;
-            }
-            // stall: no halving of the backward error over an iteration (after two)
-            if (!std::isfinite(eta) || (it >= 3 && eta > 0.5 * eta_prev)) break;
-            eta_prev = eta;
+                                                (double *)w.P.p, st, state)));
+            MX_TRY(last_err(refine_check_launch(words, m, opts.tol, opts.max_iters, st)));
         }
+        MX_TRY(cudaEventRecord(w.ev[2], st));
+        MX_TRY(read_words(8));
+        if (((int *)(hw + 3))[1] != 0) return lla__set_status(err, LLA_ERR_TIMEOUT);
+        const int stv = ((int *)(hw + 4))[0];
+        if (stv != 0 || enqueued >= opts.max_iters) {
+            lowp_ok = stv != 3;
+            converged = stv == 1;
+            r.iterations = ((int *)(hw + 4))[1];
+            eta = lowp_ok ? hw[5] : INFINITY;
+            r.backward_error0 = lowp_ok ? hw[7] : 0.0;
+            break;
+        }
+        group = kRefineGroupNext;
     }
-    r.ms_refine = ms_since(t0);
+    r.factor_failed = lowp_ok ? 0 : 1;
+    {
+        float f = 0.f, g = 0.f;
+        MX_TRY(cudaEventElapsedTime(&f, w.ev[0], w.ev[1]));
+        MX_TRY(cudaEventElapsedTime(&g, w.ev[1], w.ev[2]));
+        r.ms_factor = f;  // device time: equilibration, factorisation, block inverses, slices of A
+        r.ms_refine = g;  // device time of the refinement iterations (including the enqueued extras)
+    }
+    (void)t0;
     r.backward_error = eta;
     r.converged = converged ? 1 : 0;
     if (!converged) {

@@ -22,14 +22,20 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
 size_t sym_part_doubles(int64_t n);
 int equilibrate_launch(const double *A, int64_t lda, int64_t n, bool scale, double *s, float *W,
                        int64_t ldw, double *rowsum, double *anorm, double *rowmax, double *part, int *bad,
-                       cudaStream_t st);
+                       cudaStream_t st, int64_t *info = nullptr);
+
+// Refinement control (lla_mixed.cu): kernels that take `state` return at once
+// when it is non-NULL and nonzero (the refinement has finished or failed).
+__device__ __forceinline__ bool refine_done(const int *state) {
+    return state != nullptr && *(volatile const int *)state != 0;
+}
 int colmax_launch(const double *M, int64_t ld, int64_t n, int64_t m, double *colmax, cudaStream_t st);
 // R = B - A_sym X in FP64; P: workspace of residual_splits(n, m) * n * m
 // doubles for the split-K partials (NULL: no split).
 int residual_splits(int64_t n, int64_t m);
 int residual_launch(const double *A, int64_t lda, int64_t n, const double *X, int64_t ldx,
                     const double *B, int64_t ldb, double *R, int64_t ldr, int64_t m, double *colmax_r,
-                    double *P, cudaStream_t st);
+                    double *P, cudaStream_t st, const int *state = nullptr);
 
 // FP32 substitutions with inverted 64 x 64 diagonal blocks (lla_trsm_inv.cu).
 // W: diag_inverse_floats(n) floats (inverses and the four coupling sets);
@@ -41,7 +47,7 @@ size_t trsm_inv_stage_words(int64_t n, int64_t m);
 int diag_inverse_launch(const float *L, int64_t ld, int64_t n, float *W, cudaStream_t st);
 int trsm_inv_launch(const float *L, int64_t ld, const float *W, int64_t n, float *B, int64_t ldb,
                     int64_t m, int trans, unsigned long long *stage, unsigned epoch, int *ws, int *err_word,
-                    cudaStream_t st);
+                    cudaStream_t st, const int *state = nullptr, int ctas_per_sm = 2);
 
 // Exact-slice (tensor-core) residual: workspace size, once-per-solve slicing
 // of A, and the per-iteration residual (colmax_x: column maxima of |X|).
@@ -52,6 +58,6 @@ double *oz_rowmax(void *ws, int64_t n, int64_t m);
 int oz_prepare(const double *A, int64_t lda, int64_t n, int64_t m, void *ws, bool rowmax_ready, cudaStream_t st);
 int oz_residual_launch(const double *X, int64_t ldx, const double *B, int64_t ldb, double *R, int64_t ldr,
                        int64_t n, int64_t m, const double *colmax_x, double *colmax_r, void *ws,
-                       int *err_word, cudaStream_t st);
+                       int *err_word, cudaStream_t st, const int *state = nullptr);
 
 }  // namespace lla

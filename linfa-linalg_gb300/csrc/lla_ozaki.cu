@@ -173,7 +173,8 @@ __global__ void __launch_bounds__(256) oz_slice_a_kernel(const double *__restric
 // Slices of X^T, planes [q][j][k] (m_pad = 64 rows, zero for j >= m or k >= n).
 __global__ void oz_slice_x_kernel(const double *__restrict__ X, int64_t ldx, int64_t n, int64_t m,
                                   int64_t ldp, const double *__restrict__ colmax,
-                                  __nv_bfloat16 *planes, int64_t plane_stride) {
+                                  __nv_bfloat16 *planes, int64_t plane_stride, const int *state) {
+    if (refine_done(state)) return;
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t j = blockIdx.y;
     if (k >= ldp) return;
@@ -203,7 +204,9 @@ __global__ void oz_slice_x_kernel(const double *__restrict__ X, int64_t ldx, int
 // is read out.
 __global__ void __launch_bounds__(kOzThreads, 1) oz_residual_kernel(
     const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmX, int64_t n,
-    int64_t m, int kchunks, int splits, double *F, int *err_word) {
+    int64_t m, int kchunks, int splits, double *F, int *err_word, const int *state) {
+    // uniform for the CTA: nothing below (barriers, tensor memory) is touched
+    if (refine_done(state)) return;
     extern __shared__ uint8_t smem_raw[];
     __shared__ int s_abort;
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -384,7 +387,9 @@ __global__ void __launch_bounds__(kOzThreads, 1) oz_residual_kernel(
 // as a stall.
 __global__ void oz_combine_kernel(const double *__restrict__ F, int splits, const double *B, int64_t ldb,
                                   const double *__restrict__ rowmax, const double *__restrict__ colmax_x,
-                                  double *R, int64_t ldr, int64_t n, int64_t m, double *colmax_r) {
+                                  double *R, int64_t ldr, int64_t n, int64_t m, double *colmax_r,
+                                  const int *state) {
+    if (refine_done(state)) return;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t j = blockIdx.y;
     double v = 0.0;
@@ -489,7 +494,7 @@ int oz_prepare(const double *A, int64_t lda, int64_t n, int64_t m, void *ws, boo
 // Every iteration: R = B - A_sym X for up to 64 columns at a time.
 int oz_residual_launch(const double *X, int64_t ldx, const double *B, int64_t ldb, double *R, int64_t ldr,
                        int64_t n, int64_t m, const double *colmax_x, double *colmax_r, void *ws,
-                       int *err_word, cudaStream_t st) {
+                       int *err_word, cudaStream_t st, const int *state) {
     static bool attr = false;
     if (!attr) {
         if (cudaFuncSetAttribute(oz_residual_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kOzSmem) !=
@@ -526,19 +531,19 @@ int oz_residual_launch(const double *X, int64_t ldx, const double *B, int64_t ld
         {
             LaunchScope ls(K_OZ_SLICE, st, 8.0 * n * mc + 2.0 * kOzS * kOzN * o.ldp);
             oz_slice_x_kernel<<<dim3((unsigned)((o.ldp + 255) / 256), kOzN), 256, 0, st>>>(
-                X + c0 * ldx, ldx, n, mc, o.ldp, colmax_x + c0, o.X, kOzN * o.ldp);
+                X + c0 * ldx, ldx, n, mc, o.ldp, colmax_x + c0, o.X, kOzN * o.ldp, state);
         }
         {
             // algorithmic work: 2 n^2 mc flops of the FP64 product it replaces
             LaunchScope ls(K_RESIDUAL, st, 2.0 * n * n * mc);
             oz_residual_kernel<<<dim3((unsigned)((n + kOzM - 1) / kOzM), (unsigned)o.splits), kOzThreads,
-                                 kOzSmem, st>>>(o.tmA, o.tmX, n, mc, kchunks, o.splits, o.F, err_word);
+                                 kOzSmem, st>>>(o.tmA, o.tmX, n, mc, kchunks, o.splits, o.F, err_word, state);
         }
         {
             LaunchScope ls(K_REFINE, st, 8.0 * n * mc * (o.splits + 2));
             oz_combine_kernel<<<dim3((unsigned)((n + 255) / 256), (unsigned)mc), 256, 0, st>>>(
                 o.F, o.splits, B + c0 * ldb, ldb, o.rowmax, colmax_x + c0, R + c0 * ldr, ldr, n, mc,
-                colmax_r + c0);
+                colmax_r + c0, state);
         }
     }
     return cudaGetLastError() == cudaSuccess ? 0 : -1;

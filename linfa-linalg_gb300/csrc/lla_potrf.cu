@@ -15,7 +15,9 @@
 //
 // FAST mode is LAPACK-style right-looking (A22 -= L21 L21^T in place) with
 // fused multiply-add; the FP64 trailing update runs on the FP64 tensor pipe
-// (mma.sync m16n8k16 .f64), measured on GB300 at twice the DFMA rate.
+// (mma.sync m16n8k16 .f64), measured on GB300 at 1.05-1.10 TFLOP/s with
+// GEMM-like operand use, about the DFMA rate (1.02 TFLOP/s): FP64 is the
+// scarce resource on this GPU either way.
 #include "lla_common.cuh"
 #include "lla_kernels.h"
 #include "lla_prof.h"

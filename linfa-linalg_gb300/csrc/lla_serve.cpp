@@ -5,16 +5,18 @@
 // repeat right-hand sides, and every request records its queueing and service
 // times (p50/p99 are computed from these by the caller).
 //
-// Threads (all host-side; the GPU work is the library's kernels):
+// Threads (host side; the small requests are served by a device-resident loop):
 //   * slot workers (opts.slots of them): each owns a CUDA stream and the
 //     library's per-thread workspace, takes the next admitted large request
 //     and runs it to completion (mixed-precision refined solve, plain FP64
 //     factor-and-solve when the factor is to be kept, FP32 solve with FP64
 //     refinement for single-precision requests, triangular solve, or a solve
 //     with a kept factor);
-//   * a batcher: gathers admitted small requests (n <= opts.small_n) for up
-//     to opts.batch_window_us or opts.batch_max requests, copies them into
-//     pools, solves them in one persistent launch and scatters the results.
+//   * a device pump: small requests (n <= opts.small_n) go to a
+//     device-resident loop -- persistent CTAs that claim requests from a ring
+//     in mapped host memory and solve each in place, one CTA per request --
+//     as soon as they are admitted; the pump relaunches the loop when its
+//     CTAs have returned after an idle limit, and reaps completions.
 // Requests run on independent data with fixed kernels, so a request's result
 // does not depend on what it shares the device with.
 #include <cuda_runtime.h>
@@ -71,7 +73,7 @@ struct lla_server {
     std::map<int64_t, Factor> factors;
     int64_t next_handle = 1;
     size_t in_use = 0, peak = 0;
-    int64_t submitted = 0, completed = 0, running = 0;
+    int64_t submitted = 0, completed = 0, running = 0, loop_launches = 0;
     bool stop = false;
     std::vector<std::thread> threads;
 };
@@ -139,16 +141,12 @@ int run_big(lla_server *s, Pending *p, cudaStream_t st, std::vector<void *> &scr
     };
     if (r.kind == LLA_REQ_TRSM) {  // L X = B with the lower factor given in A
         p->res.path = LLA_PATH_TRSM;
-        if (r.dtype == 4)
-            return lla_strsm_device((const float *)r.A, n, r.lda, 0, (float *)r.B, m, r.ldb,
-                                    LLA_ALGO_FAST, st, &err) ||
-                           cudaStreamSynchronize(st) != cudaSuccess
-                       ? LLA_ERR_CUDA
-                       : LLA_OK;
-        int rc = lla_dtrsm_device((const double *)r.A, n, r.lda, 0, (double *)r.B, m, r.ldb,
-                                  LLA_ALGO_FAST, st, &err);
+        int rc = r.dtype == 4 ? lla_strsm_device((const float *)r.A, n, r.lda, 0, (float *)r.B, m, r.ldb,
+                                                 LLA_ALGO_FAST, st, &err)
+                              : lla_dtrsm_device((const double *)r.A, n, r.lda, 0, (double *)r.B, m, r.ldb,
+                                                 LLA_ALGO_FAST, st, &err);
         if (rc) return rc;
-        return cudaStreamSynchronize(st) == cudaSuccess ? LLA_OK : LLA_ERR_CUDA;
+        return lla_device_status(st, &err);  // synchronises; LLA_ERR_TIMEOUT if a wait gave up
     }
     if (r.kind == LLA_REQ_RESOLVE) {
         Factor f;
@@ -162,7 +160,8 @@ int run_big(lla_server *s, Pending *p, cudaStream_t st, std::vector<void *> &scr
         }
         int rc = lla_dtrsm_device(f.L, n, n, 0, (double *)r.B, m, r.ldb, LLA_ALGO_FAST, st, &err);
         if (!rc) rc = lla_dtrsm_device(f.L, n, n, 1, (double *)r.B, m, r.ldb, LLA_ALGO_FAST, st, &err);
-        if (cudaStreamSynchronize(st) != cudaSuccess && !rc) rc = LLA_ERR_CUDA;
+        const int sc = lla_device_status(st, &err);  // synchronises the stream
+        if (!rc) rc = sc;
         {
             std::lock_guard<std::mutex> lk(s->mu);
             auto it = s->factors.find(r.factor_handle);
@@ -195,7 +194,7 @@ int run_big(lla_server *s, Pending *p, cudaStream_t st, std::vector<void *> &scr
         if (!rc && hinfo >= 0) rc = LLA_NOT_POSITIVE_DEFINITE;
         if (!rc) rc = lla_dtrsm_device(L, n, n, 0, (double *)r.B, m, r.ldb, LLA_ALGO_FAST, st, &err);
         if (!rc) rc = lla_dtrsm_device(L, n, n, 1, (double *)r.B, m, r.ldb, LLA_ALGO_FAST, st, &err);
-        if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = LLA_ERR_CUDA;
+        if (!rc) rc = lla_device_status(st, &err);  // synchronises the stream
         if (rc) {
             cudaFreeAsync(L, st);
             return rc;
@@ -263,104 +262,98 @@ void slot_worker(lla_server *s) {
     cudaStreamDestroy(st);
 }
 
-void batcher(lla_server *s) {
+// Small requests go to the device-resident loop (serve_loop_kernel): this
+// thread publishes each admitted small request into the request ring as soon
+// as it is admitted (no batching window: requests that arrive while others are
+// on the GPU join the running loop), relaunches the loop when its CTAs have
+// returned after their idle limit, and reaps completions in any order.
+void device_pump(lla_server *s) {
+    using lla::kServeRing;
     cudaStream_t st;
     cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
-    lla::DevBuf poolA, poolB, ditems, dinfo;
-    lla::HostBuf hitems;
+    lla::ServeRing *ring = nullptr, *ring_dev = nullptr;
+    unsigned long long *d_next = nullptr;
+    double *scratch = nullptr;
+    const int ctas = s->opts.device_ctas;
+    bool ok = cudaHostAlloc((void **)&ring, sizeof(lla::ServeRing), cudaHostAllocMapped) == cudaSuccess;
+    if (ok) {
+        std::memset((void *)ring, 0, sizeof(lla::ServeRing));
+        ok = cudaHostGetDevicePointer((void **)&ring_dev, ring, 0) == cudaSuccess &&
+             cudaMalloc((void **)&d_next, sizeof(unsigned long long)) == cudaSuccess &&
+             cudaMemset(d_next, 0, sizeof(unsigned long long)) == cudaSuccess &&
+             cudaMalloc((void **)&scratch, lla::serve_loop_scratch_bytes(ctas)) == cudaSuccess;
+    }
+    std::vector<std::unique_ptr<Pending>> owned(kServeRing);
+    unsigned long long published = 0, low = 0;  // low: the oldest ticket not yet reaped
+    bool launched = false;
+    auto reap = [&]() {
+        for (unsigned long long t = low; t < published; ++t) {
+            const int slot = (int)(t % kServeRing);
+            if (!owned[slot] || __atomic_load_n(&ring->done_seq[slot], __ATOMIC_ACQUIRE) != t + 1) continue;
+            const int status = __atomic_load_n(&ring->status[slot], __ATOMIC_RELAXED);
+            finish(s, owned[slot].get(), status ? LLA_NOT_POSITIVE_DEFINITE : LLA_OK);
+            owned[slot].reset();
+        }
+        while (low < published && !owned[low % kServeRing]) ++low;
+    };
     for (;;) {
-        std::vector<std::unique_ptr<Pending>> group;
+        std::vector<std::unique_ptr<Pending>> take;
         {
             std::unique_lock<std::mutex> lk(s->mu);
-            s->cv_small.wait(lk, [&] { return s->stop || !s->small.empty(); });
-            if (s->stop && s->small.empty()) break;
-            // continuous batching: wait up to the window for more small requests
-            const auto deadline = Clock::now() + std::chrono::microseconds((int64_t)s->opts.batch_window_us);
-            s->cv_small.wait_until(lk, deadline, [&] {
-                return s->stop || (int)s->small.size() >= s->opts.batch_max;
-            });
-            while (!s->small.empty() && (int)group.size() < s->opts.batch_max) {
-                group.push_back(std::move(s->small.front()));
+            if (low == published)  // nothing in flight: sleep until work arrives
+                s->cv_small.wait(lk, [&] { return s->stop || !s->small.empty(); });
+            if (s->stop && s->small.empty() && low == published) break;
+            while (!s->small.empty() && published + take.size() - low < (unsigned long long)s->opts.batch_max) {
+                take.push_back(std::move(s->small.front()));
                 s->small.pop_front();
             }
         }
-        const double t_start = now_us(s->t0);
-        // one batched launch per element type; pools and work list are grow-only
-        for (int elem : {8, 4}) {
-            std::vector<Pending *> g;
-            for (auto &p : group)
-                if (p->req.dtype == elem) g.push_back(p.get());
-            if (g.empty()) continue;
-            // largest systems first
-            std::stable_sort(g.begin(), g.end(), [](const Pending *a, const Pending *b) {
-                return a->req.n * a->req.n * (a->req.n + 6 * a->req.m) >
-                       b->req.n * b->req.n * (b->req.n + 6 * b->req.m);
-            });
-            const int64_t k = (int64_t)g.size();
-            std::vector<lla::BatchItem> items(k);
-            int64_t ae = 0, be = 0;
-            double flops = 0;
-            for (int64_t i = 0; i < k; ++i) {
-                const lla_request &r = g[i]->req;
-                items[i] = lla::BatchItem{(int32_t)r.n, (int32_t)r.m, (int32_t)i, 0, ae, be};
-                ae += (r.n * r.n + 1) / 2 * 2;
-                be += (r.n * r.m + 1) / 2 * 2;
-                flops += (double)r.n * r.n * r.n / 3.0 + 2.0 * r.n * r.n * r.m;
-            }
-            int rc = 0;
-            if (poolA.ensure(elem * std::max<int64_t>(ae, 1)) != cudaSuccess ||
-                poolB.ensure(elem * std::max<int64_t>(be, 1)) != cudaSuccess ||
-                ditems.ensure(sizeof(lla::BatchItem) * k) != cudaSuccess ||
-                dinfo.ensure(sizeof(int32_t) * k + sizeof(int)) != cudaSuccess ||
-                hitems.ensure(sizeof(lla::BatchItem) * k + sizeof(int32_t) * k) != cudaSuccess)
-                rc = LLA_ERR_NO_MEMORY;
-            int32_t *hinfo = nullptr;
-            if (!rc) {
-                std::memcpy(hitems.p, items.data(), sizeof(lla::BatchItem) * k);
-                hinfo = (int32_t *)((char *)hitems.p + sizeof(lla::BatchItem) * k);
-                if (cudaMemcpyAsync(ditems.p, hitems.p, sizeof(lla::BatchItem) * k, cudaMemcpyHostToDevice,
-                                    st) != cudaSuccess)
-                    rc = LLA_ERR_CUDA;
-            }
-            for (int64_t i = 0; !rc && i < k; ++i) {
-                const lla_request &r = g[i]->req;
-                if (cudaMemcpy2DAsync((char *)poolA.p + elem * items[i].a_off, elem * r.n, r.A, elem * r.lda,
-                                      elem * r.n, r.n, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
-                    (r.m > 0 && cudaMemcpy2DAsync((char *)poolB.p + elem * items[i].b_off, elem * r.n, r.B,
-                                                  elem * r.ldb, elem * r.n, r.m, cudaMemcpyDeviceToDevice,
-                                                  st) != cudaSuccess))
-                    rc = LLA_ERR_CUDA;
-            }
-            int32_t *dinf = (int32_t *)dinfo.p;
-            int *dcounter = (int *)((char *)dinfo.p + sizeof(int32_t) * k);
-            if (!rc) {
-                const int lr =
-                    elem == 8 ? lla::batch_launch_raw<double>((const lla::BatchItem *)ditems.p, k,
-                                                              (double *)poolA.p, (double *)poolB.p, dinf,
-                                                              dcounter, 2, 256, flops, st)
-                              : lla::batch_launch_raw<float>((const lla::BatchItem *)ditems.p, k,
-                                                             (float *)poolA.p, (float *)poolB.p, dinf,
-                                                             dcounter, 3, 128, flops, st);
-                if (lr) rc = LLA_ERR_CUDA;
-            }
-            for (int64_t i = 0; !rc && i < k; ++i) {
-                const lla_request &r = g[i]->req;
-                if (r.m > 0 && cudaMemcpy2DAsync(r.B, elem * r.ldb, (char *)poolB.p + elem * items[i].b_off,
-                                                 elem * r.n, elem * r.n, r.m, cudaMemcpyDeviceToDevice,
-                                                 st) != cudaSuccess)
-                    rc = LLA_ERR_CUDA;
-            }
-            if (!rc && (cudaMemcpyAsync(hinfo, dinf, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, st) !=
-                            cudaSuccess ||
-                        cudaStreamSynchronize(st) != cudaSuccess))
-                rc = LLA_ERR_CUDA;
-            for (int64_t i = 0; i < k; ++i) {
-                g[i]->res.t_start_us = t_start;
-                g[i]->res.path = LLA_PATH_BATCHED;
-                finish(s, g[i], rc ? rc : (hinfo[i] >= 0 ? LLA_NOT_POSITIVE_DEFINITE : LLA_OK));
+        if (!ok) {  // the loop's resources could not be set up: fail these requests
+            for (auto &p : take) finish(s, p.get(), LLA_ERR_NO_MEMORY);
+            continue;
+        }
+        for (auto &p : take) {
+            const lla_request &r = p->req;
+            const int slot = (int)(published % kServeRing);
+            lla::ServeReq &q = ring->req[slot];
+            q.A = r.A;
+            q.B = r.B;
+            q.lda = r.lda;
+            q.ldb = r.ldb;
+            q.n = (int32_t)r.n;
+            q.m = (int32_t)r.m;
+            q.dtype = r.dtype;
+            p->res.path = LLA_PATH_BATCHED;
+            p->res.t_start_us = now_us(s->t0);
+            owned[slot] = std::move(p);
+            ++published;
+            __atomic_store_n(&ring->published, published, __ATOMIC_RELEASE);
+        }
+        reap();
+        if (low < published && (!launched || cudaStreamQuery(st) == cudaSuccess)) {
+            // the loop's CTAs returned after their idle limit (or were never
+            // started): whatever they claimed is finished, the rest waits
+            reap();
+            if (low < published) {
+                if (lla::serve_loop_launch(ring_dev, d_next, scratch, ctas, s->opts.batch_window_us, st) != 0) {
+                    for (unsigned long long t = low; t < published; ++t)
+                        if (owned[t % kServeRing]) finish(s, owned[t % kServeRing].get(), LLA_ERR_CUDA);
+                    for (auto &o : owned) o.reset();
+                    low = published;
+                } else {
+                    launched = true;
+                    std::lock_guard<std::mutex> lk(s->mu);
+                    s->loop_launches++;
+                }
             }
         }
+        if (low < published && take.empty()) std::this_thread::sleep_for(std::chrono::microseconds(10));
     }
+    if (ring) __atomic_store_n(&ring->stop, 1, __ATOMIC_RELEASE);
+    cudaStreamSynchronize(st);
+    if (scratch) cudaFree(scratch);
+    if (d_next) cudaFree(d_next);
+    if (ring) cudaFreeHost(ring);
     cudaStreamDestroy(st);
 }
 
@@ -399,8 +392,9 @@ void lla_serve_opts_default(lla_serve_opts *o) {
     o->hbm_budget_bytes = 40e9;
     o->slots = 6;
     o->small_n = 256;
-    o->batch_max = 512;
-    o->batch_window_us = 200.0;
+    o->batch_max = 1024;
+    o->batch_window_us = 2000.0;
+    o->device_ctas = 0;
 }
 
 int lla_server_create(const lla_serve_opts *opts, lla_server **out, lla_error *err) {
@@ -412,11 +406,17 @@ int lla_server_create(const lla_serve_opts *opts, lla_server **out, lla_error *e
     else
         lla_serve_opts_default(&s->opts);
     if (s->opts.slots <= 0) s->opts.slots = 1;
-    if (s->opts.batch_max <= 0) s->opts.batch_max = 512;
+    if (s->opts.batch_max <= 0 || s->opts.batch_max > lla::kServeRing) s->opts.batch_max = lla::kServeRing;
     if (s->opts.small_n > 256) s->opts.small_n = 256;
+    if (!(s->opts.batch_window_us > 0)) s->opts.batch_window_us = 2000.0;
     s->t0 = Clock::now();
     int dev = 0;
     cudaGetDevice(&dev);
+    if (s->opts.device_ctas <= 0) {  // default: one CTA on every other SM
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        s->opts.device_ctas = std::max(1, sms / 2);
+    }
     auto bind = [dev](void (*fn)(lla_server *), lla_server *srv) {
         return std::thread([dev, fn, srv] {
             cudaSetDevice(dev);
@@ -424,7 +424,7 @@ int lla_server_create(const lla_serve_opts *opts, lla_server **out, lla_error *e
         });
     };
     s->threads.push_back(bind(admitter, s));
-    s->threads.push_back(bind(batcher, s));
+    s->threads.push_back(bind(device_pump, s));
     for (int i = 0; i < s->opts.slots; ++i) s->threads.push_back(bind(slot_worker, s));
     *out = s;
     return lla__set_status(err, LLA_OK);
@@ -500,6 +500,7 @@ int lla_server_get_stats(lla_server *s, lla_server_stats *out) {
     out->submitted = s->submitted;
     out->completed = s->completed;
     out->kept_factors = (int64_t)s->factors.size();
+    out->device_loop_launches = s->loop_launches;
     return LLA_OK;
 }
 

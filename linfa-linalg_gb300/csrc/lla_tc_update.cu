@@ -14,8 +14,8 @@
 //   * eight epilogue warps read a finished accumulator from tensor memory
 //     (tcgen05.ld 32x32b, two warps per 32-lane quarter) and subtract it from
 //     the FP32 tile in HBM (coalesced: a warp covers 32 consecutive rows of a
-//     column-major column) while the next tile's MMAs run; diagonal tiles write
-//     their lower half only.
+//     column-major column) while the next tile's MMAs run; diagonal tiles
+//     write their lower half only.
 // Every wait is bounded: on expiry the CTA records LLA_ERR_TIMEOUT, skips its
 // writes, frees its tensor memory and returns.
 #include <cuda.h>
@@ -28,17 +28,31 @@
 
 namespace lla {
 
-constexpr int kTcM = 128, kTcN = 128, kTcK = 64;  // tile and K-chunk
-constexpr int kTcTileBytes = kTcM * kTcK * 2;      // 16 KiB: one term plane of one operand
-constexpr int kTcRingBytes = 12 * kTcTileBytes;    // 192 KiB of operand stages
-constexpr int kTcMaxStages = 6;
+constexpr int kTcM = 128, kTcN = 128;            // tile
+constexpr int kTcRingBytes = 192 * 1024;          // operand stages
+constexpr int kTcMaxStages = 8;
 constexpr int kTcSmem = 1024 + kTcRingBytes + 256;
+// K-chunk KC of a stage: 64 (128-byte rows, 128-byte swizzle) or 32 (64-byte
+// rows, 64-byte swizzle: twice the stages in the same ring, so more loads are
+// in flight ahead of the MMAs).  One term plane of one operand: 128 x KC x 2 B.
+template <int KC>
+__host__ __device__ constexpr int tc_tile_bytes() { return kTcM * KC * 2; }
 // Stages of the ring: a stage holds every term plane of both operands for one
-// K-chunk (terms x 32 KiB), so each plane is loaded once per chunk and serves
-// all the term pairs that use it.
+// K-chunk, so each plane is loaded once per chunk and serves all the term
+// pairs that use it.
+template <int KC>
 __host__ __device__ constexpr int tc_stages(int terms) {
-    return (kTcRingBytes / (2 * terms * kTcTileBytes)) < kTcMaxStages ? kTcRingBytes / (2 * terms * kTcTileBytes)
-                                                                      : kTcMaxStages;
+    return (kTcRingBytes / (2 * terms * tc_tile_bytes<KC>())) < kTcMaxStages
+               ? kTcRingBytes / (2 * terms * tc_tile_bytes<KC>())
+               : kTcMaxStages;
+}
+// Shared-memory descriptor of a K-major tile stored with the KC-wide swizzle:
+// 8-row atoms of KC * 2 bytes per row stacked along M.
+template <int KC>
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+    if (KC == 64) return sw128_desc(saddr);
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(512 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)4 << 61);
 }
 constexpr uint32_t kTcCols = 128;  // tensor-memory columns of one FP32 128 x 128 accumulator
 // Two accumulators per tile: the leading product h0 h0^T, and the sum of the
@@ -84,7 +98,9 @@ __device__ __forceinline__ constexpr int tc_pb(int terms, int i) {
     return terms == 1 ? 0 : (terms == 2 ? (i == 0 ? 1 : 0) : (i == 0 ? 2 : (i == 1 || i == 3 ? 1 : 0)));
 }
 
-template <int TERMS>
+// 320 threads are 10 warps, so one SM sub-partition runs 3 of them from its
+// 16K registers: at most 170 registers a thread (168 allocated).
+template <int TERMS, int KC>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     const __grid_constant__ CUtensorMap tmap, float *C, int64_t ld, int64_t q, int64_t n, int kchunks,
     uint32_t idesc, int64_t ntiles, int narrow, const int64_t *info, int *err_word) {
@@ -97,8 +113,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     __syncthreads();
     if (s_skip) return;
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    const int S = tc_stages(terms);
-    const uint32_t opnd = (uint32_t)terms * kTcTileBytes;  // one operand's planes in a stage
+    constexpr int kTile = tc_tile_bytes<KC>();
+    const int S = tc_stages<KC>(terms);
+    const uint32_t opnd = (uint32_t)terms * kTile;  // one operand's planes in a stage
     uint8_t *ring = smem;                                   // stage s: A planes, then B planes
     uint64_t *bars = (uint64_t *)(smem + kTcRingBytes);
     // bars: full[S], empty[S], tmem_full[2], tmem_empty[2]
@@ -145,8 +162,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
                     }
                     const uint32_t st_a = smem_u32(ring + (size_t)s * 2 * opnd);
                     mbar_expect_tx(full0 + 8 * s, (I == J ? 1u : 2u) * opnd);
-                    tma_load_3d(st_a, &tmap, kc * kTcK, (int)(I * kTcM), 0, full0 + 8 * s);
-                    if (I != J) tma_load_3d(st_a + opnd, &tmap, kc * kTcK, (int)(J * kTcN), 0, full0 + 8 * s);
+                    tma_load_3d(st_a, &tmap, kc * KC, (int)(I * kTcM), 0, full0 + 8 * s);
+                    if (I != J) tma_load_3d(st_a + opnd, &tmap, kc * KC, (int)(J * kTcN), 0, full0 + 8 * s);
                 }
             }
         }
@@ -173,17 +190,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
                     tc_fence_after();
                     const uint32_t st_a = smem_u32(ring + (size_t)s * 2 * opnd);
                     const uint32_t st_b = (I == J) ? st_a : st_a + opnd;  // a diagonal tile uses its rows twice
-                    const uint64_t ad0 = sw128_desc(st_a), bd0 = sw128_desc(st_b);
+                    const uint64_t ad0 = tc_desc<KC>(st_a), bd0 = tc_desc<KC>(st_b);
 #pragma unroll
                     for (int pr = 0; pr < NP; ++pr) {
                         const bool lead = pr == NP - 1;  // (0, 0)
                         const uint32_t d = lead ? dt : dt + kTcCols;
                         const bool fresh = kc == 0 && (lead || pr == 0);
-                        // descriptors address 16-byte units: a plane is kTcTileBytes / 16 further
-                        const uint64_t ad = ad0 + (uint64_t)(tc_pa(TERMS, pr) * (kTcTileBytes >> 4));
-                        const uint64_t bd = bd0 + (uint64_t)(tc_pb(TERMS, pr) * (kTcTileBytes >> 4));
+                        // descriptors address 16-byte units: a plane is kTile / 16 further
+                        const uint64_t ad = ad0 + (uint64_t)(tc_pa(TERMS, pr) * (kTile >> 4));
+                        const uint64_t bd = bd0 + (uint64_t)(tc_pb(TERMS, pr) * (kTile >> 4));
 #pragma unroll
-                        for (int k = 0; k < kTcK / 16; ++k)  // +32 bytes along K per step
+                        for (int k = 0; k < KC / 16; ++k)  // +32 bytes along K per step
                             tc_mma(d, ad + 2 * k, bd + 2 * k, idesc, (fresh && k == 0) ? 0u : 1u);
                     }
                     tc_commit(empty0 + 8 * s);  // frees the stage once these MMAs are done
@@ -277,22 +294,26 @@ PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
     return g_encode;
 }
 
+template <int KC>
+static bool tc_set_attrs() {
+    return cudaFuncSetAttribute(tc_update_kernel<1, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) ==
+               cudaSuccess &&
+           cudaFuncSetAttribute(tc_update_kernel<2, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) ==
+               cudaSuccess &&
+           cudaFuncSetAttribute(tc_update_kernel<3, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) ==
+               cudaSuccess;
+}
+
 int tc_update_prepare() {
     if (!tma_encoder()) return -1;
-    if (cudaFuncSetAttribute(tc_update_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(tc_update_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(tc_update_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) !=
-            cudaSuccess)
-        return -1;
-    return 0;
+    return tc_set_attrs<64>() && tc_set_attrs<32>() ? 0 : -1;
 }
 
 int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, int64_t plane_stride,
                      int64_t ldp, int64_t rows, int kext, int terms, bool fp16, const TcPairs &pairs,
-                     const int64_t *info, int *err_word, bool narrow, cudaStream_t st) {
-    if (!g_encode || rows <= 0 || kext % kTcK != 0 || kext > ldp || (ldp * 2) % 16 != 0 || terms < 1 ||
+                     const int64_t *info, int *err_word, bool narrow, cudaStream_t st, int kchunk) {
+    const int kc = kchunk == 32 ? 32 : 64;
+    if (!g_encode || rows <= 0 || kext % kc != 0 || kext > ldp || (ldp * 2) % 16 != 0 || terms < 1 ||
         terms > 3 || (reinterpret_cast<uintptr_t>(planes) & 15) != 0)
         return -1;
     const int64_t tr = (rows + kTcM - 1) / kTcM;
@@ -300,13 +321,13 @@ int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, i
     CUtensorMap map;
     const cuuint64_t dims[3] = {(cuuint64_t)kext, (cuuint64_t)rows, (cuuint64_t)terms};
     const cuuint64_t strides[2] = {(cuuint64_t)ldp * 2, (cuuint64_t)plane_stride * 2};
-    const cuuint32_t box[3] = {(cuuint32_t)kTcK, (cuuint32_t)kTcM, (cuuint32_t)terms};  // every term plane
+    const cuuint32_t box[3] = {(cuuint32_t)kc, (cuuint32_t)kTcM, (cuuint32_t)terms};  // every term plane
     const cuuint32_t estr[3] = {1, 1, 1};
     const CUresult r =
         g_encode(&map, fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
                  planes, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                 CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                 kc == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
+                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return -1;
     // instruction descriptor: D = F32 (bits 4-5), A/B = BF16 (1) or F16 (0) (bits 7-9, 10-12),
     // both K-major, N >> 3 at bit 17, M >> 4 at bit 24
@@ -325,8 +346,11 @@ int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, i
     if (pairs.n != (terms == 1 ? 1 : (terms == 2 ? 3 : 6)) || pairs.pa[pairs.n - 1] != 0 ||
         pairs.pb[pairs.n - 1] != 0)
         return -1;
-    auto kern = terms == 1 ? tc_update_kernel<1> : (terms == 2 ? tc_update_kernel<2> : tc_update_kernel<3>);
-    kern<<<grid, kTcThreads, kTcSmem, st>>>(map, C, ld, q, n, kext / kTcK, idesc, tiles, narrow ? 1 : 0, info,
+    auto kern = kc == 32 ? (terms == 1 ? tc_update_kernel<1, 32>
+                                       : (terms == 2 ? tc_update_kernel<2, 32> : tc_update_kernel<3, 32>))
+                         : (terms == 1 ? tc_update_kernel<1, 64>
+                                       : (terms == 2 ? tc_update_kernel<2, 64> : tc_update_kernel<3, 64>));
+    kern<<<grid, kTcThreads, kTcSmem, st>>>(map, C, ld, q, n, kext / kc, idesc, tiles, narrow ? 1 : 0, info,
                                             err_word);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

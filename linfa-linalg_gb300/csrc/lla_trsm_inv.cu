@@ -23,6 +23,8 @@
 // matches.  Every wait is bounded and reports LLA_ERR_TIMEOUT.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "lla_common.cuh"
 #include "lla_mixed.h"
 #include "lla_prof.h"
@@ -176,6 +178,7 @@ constexpr int64_t kIvHelperMin = 16;  // first position whose coupling terms are
 constexpr int kIvYd = kIvNb + 2;  // words per staged column (padded: 528-byte columns)
 constexpr size_t kIvSmem = sizeof(float) * ((size_t)kIvStages * kIvNb * kIvLd + 2ull * kIvStages * kIvCols * kIvYd +
                                             2ull * kIvNb * kIvCols + 2ull * kIvCols * kIvLd);
+constexpr size_t kIvSmemSolo = 120 * 1024;  // more than half of an SM's shared memory: one CTA per SM
 
 // TRANS = false: L Y = B (blocks ascending); TRANS = true: L^T X = B (descending).
 // 256 threads.  The coupling tiles and the solved words of earlier blocks
@@ -193,7 +196,9 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
                                                           const float *__restrict__ Wall, int64_t n,
                                                           float *B, int64_t ldb, int64_t m, int nchunks,
                                                           unsigned long long *ll, int64_t ldl, unsigned epoch,
-                                                          int *counter, int *err_word, int64_t hmin) {
+                                                          int *counter, int *err_word, int64_t hmin,
+                                                          const int *state) {
+    if (refine_done(state)) return;  // the refinement has finished: nothing to solve
     constexpr int C = kIvCols, LPT = kIvTile / 256, NS = kIvStages;
     constexpr int YCH = kIvNb * C / 2 / 256;  // 16-byte (two-word) copies per thread per stage
     extern __shared__ __align__(16) float iv_smem[];
@@ -540,13 +545,16 @@ int diag_inverse_launch(const float *L, int64_t ld, int64_t n, float *W, cudaStr
 
 int trsm_inv_launch(const float *L, int64_t ld, const float *W, int64_t n, float *B, int64_t ldb,
                     int64_t m, int trans, unsigned long long *stage, unsigned epoch, int *ws, int *err_word,
-                    cudaStream_t st) {
+                    cudaStream_t st, const int *state, int ctas_per_sm) {
     if (n == 0 || m == 0) return 0;
     if (epoch == 0) return -1;
     const int nchunks = (int)((m + kIvCols - 1) / kIvCols);
     const int64_t R = (n + kIvNb - 1) / kIvNb;
     auto kern = trans ? trsm_inv_kernel<true> : trsm_inv_kernel<false>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kIvSmem) != cudaSuccess)
+    // two CTAs share an SM by default; one CTA per SM (shared memory reserved
+    // beyond half an SM) gives each block's critical product the whole SM
+    const size_t smem = ctas_per_sm == 1 ? std::max<size_t>(kIvSmem, kIvSmemSolo) : kIvSmem;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return -1;
     if (cudaMemsetAsync(ws, 0, sizeof(int), st) != cudaSuccess) return -1;
     // algorithmic work: n^2 m flops
@@ -554,8 +562,8 @@ int trsm_inv_launch(const float *L, int64_t ld, const float *W, int64_t n, float
     // positions from kIvHelperMin on get a helper for the first half of their coupling terms
     const int64_t hmin = kIvHelperMin;
     const int64_t items = iv_items_before(R, R, hmin, nchunks);  // every group
-    kern<<<(unsigned)items, 256, kIvSmem, st>>>(L, ld, W, n, B, ldb, m, nchunks, stage, R * kIvNb, epoch, ws,
-                                               err_word, hmin);
+    kern<<<(unsigned)items, 256, smem, st>>>(L, ld, W, n, B, ldb, m, nchunks, stage, R * kIvNb, epoch, ws,
+                                            err_word, hmin, state);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -129,7 +129,7 @@ def test_batch_autotune_keeps_results(gpu_lla, tmp_path, monkeypatch):
     assert (tmp_path / "tune.txt").read_text().strip()
 
 
-@pytest.mark.parametrize("dtype", ["f64", "f32"])
+@pytest.mark.parametrize("dtype", ["f64", "f32", "f64-refined"])
 def test_batch_configuration_10000_systems(gpu_lla, dtype):
     """The batched configuration at its own size: 10,000 systems, n log-uniform
     in [16, 256], A = G G^T / n + 0.1 I, 1..8 RHS, one graph replay; EVERY
@@ -140,8 +140,10 @@ def test_batch_configuration_10000_systems(gpu_lla, dtype):
     rng = np.random.default_rng(10000)
     n = np.clip(np.exp(rng.uniform(np.log(16), np.log(256), count)).round(), 16, 256).astype(np.int32)
     m = rng.integers(1, 9, count).astype(np.int32)
-    dt = torch.float64 if dtype == "f64" else torch.float32
-    plan = lla.BatchPlan(n, m, dtype)
+    dt = torch.float32 if dtype == "f32" else torch.float64
+    plan = lla.BatchPlan(n, m, dtype[:3])
+    if dtype == "f64-refined":
+        plan.set_refined(True)
     g = torch.Generator(device="cuda")
     g.manual_seed(5)
     A0 = torch.zeros(plan.a_elems, dtype=dt, device="cuda")
@@ -169,3 +171,39 @@ def test_batch_configuration_10000_systems(gpu_lla, dtype):
         worst.append(be / (float(n[i]) * eps))
     w = float(torch.stack(worst).max())
     assert w <= 10.0, w
+
+
+def test_batch_refined_mode(gpu_lla):
+    """f64 systems through an FP32 factorisation with per-system FP64
+    refinement: every system at the per-matrix FP64 class (backward error
+    <= 10 n eps), A left untouched (read only), the graph replay identical to
+    the direct launch, and a non-SPD system reported at the row the plain FP64
+    batched solve reports (its fallback is that routine)."""
+    torch = pytest.importorskip("torch")
+    lla = gpu_lla
+    rng = np.random.default_rng(808)
+    n, m, As, Bs = make_batch(rng, 300, np.float64)
+    bad = [5, 77, 150]
+    for i in bad:
+        As[i] = As[i].copy()
+        As[i][min(3, n[i] - 1), min(3, n[i] - 1)] = -1.0
+    plan = lla.BatchPlan(n, m, "f64")
+    plan.set_refined(True)
+    X, info, a_after = run(lla, plan, As, Bs)
+    ap, _ = plan.pack(As, Bs)
+    assert np.array_equal(a_after, ap)  # A is read only in this mode
+    eps = np.finfo(np.float64).eps
+    for i in range(plan.count):
+        if i in bad:
+            continue
+        assert info[i] == -1, (i, info[i])
+        be = backward_error(As[i], X[i], Bs[i])
+        assert be <= 10 * n[i] * eps, (i, n[i], be)
+    X2, info2, _ = run(lla, plan, As, Bs, graph=True)
+    assert np.array_equal(info, info2) and all(np.array_equal(X[i], X2[i]) for i in range(plan.count))
+    plain = lla.BatchPlan(n, m, "f64")
+    _, info_p, _ = run(lla, plain, As, Bs)
+    for i in bad:
+        assert info[i] == info_p[i] and info[i] >= 0, (i, info[i], info_p[i])
+    with pytest.raises(lla.DeviceError):
+        lla.BatchPlan(n[:4], m[:4], "f32").set_refined(True)

@@ -274,3 +274,20 @@ def test_headline_size_n16384_kappa_1e6(gpu_lla):
     assert int(info.item()) == -1
     fe = float((X - Xp).abs().max() / Xp.abs().max())
     assert fe <= 1e6 * 1e-13 * 10, fe
+
+
+@pytest.mark.parametrize("update", ["bf16x6", "bf16x3", "fp16x3"])
+@pytest.mark.parametrize("kchunk", [32, 64])
+def test_update_kchunk_forms(gpu_lla, update, kchunk):
+    """The tensor-core update with 64-wide K-chunks (128-byte swizzle) and with
+    32-wide K-chunks (64-byte swizzle, twice the stages): both converge to the
+    FP64 target, and their factors agree to FP32 accuracy."""
+    lla = gpu_lla
+    rng = np.random.default_rng(3 + kchunk)
+    n = 1537
+    a = qdq(rng, n, 1e6)
+    b = rng.standard_normal((n, 9))
+    x = b.copy()
+    rep = lla.posv_refined(a, x, update=update, update_kchunk=kchunk)
+    assert rep["converged"] == 1 and rep["fell_back"] == 0, rep
+    assert backward_error(a, x, b) <= 2e-13

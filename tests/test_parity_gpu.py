@@ -160,6 +160,42 @@ def test_masks_and_predicate(gpu_lla):
             assert lla.is_triangular(g, other) == ora.is_triangular(r, other)
 
 
+def test_device_masks_and_predicate(gpu_lla):
+    """triangular_inplace / is_triangular on device-resident column-major
+    matrices (lla_?triangular_device, lla_?is_triangular_device) against the
+    oracle: the same entries zeroed, the same verdicts, -0.0 counts as zero and
+    NaN does not, a non-square matrix is NotSquare / not triangular."""
+    torch = pytest.importorskip("torch")
+    lla = gpu_lla
+    rng = np.random.default_rng(55)
+    for it in range(12):
+        n = int(rng.integers(1, 300)) if it else 1
+        dt = np.float64 if it % 2 == 0 else np.float32
+        a = rng.uniform(-100, 100, (n, n)).astype(dt)
+        for uplo in ("lower", "upper"):
+            g = torch.tensor(a, device="cuda").T.contiguous().T  # column-major
+            r = a.copy()
+            lla.triangular_device(g, uplo)
+            ora.triangular_inplace(r, uplo)
+            assert same_bits(g.cpu().numpy(), r)
+            other = "upper" if uplo == "lower" else "lower"
+            assert int(lla.is_triangular_device(g, uplo).item()) == int(ora.is_triangular(r, uplo)) == 1
+            want = ora.is_triangular(r, other)
+            assert int(lla.is_triangular_device(g, other).item()) == int(want)
+    # -0.0 is zero, NaN is not
+    z = np.tril(rng.standard_normal((40, 40)))
+    z[3, 20] = -0.0
+    assert int(lla.is_triangular_device(torch.tensor(z, device="cuda").T.contiguous().T, "lower").item()) == 1
+    z[3, 20] = np.nan
+    assert int(lla.is_triangular_device(torch.tensor(z, device="cuda").T.contiguous().T, "lower").item()) == 0
+    assert ora.is_triangular(z, "lower") is False or ora.is_triangular(z, "lower") == 0
+    # non-square: NotSquare for the mask, "not triangular" for the predicate
+    ns = torch.zeros(5, 7, dtype=torch.float64, device="cuda").T.contiguous().T
+    with pytest.raises(lla.NotSquare):
+        lla.triangular_device(ns, "lower")
+    assert int(lla.is_triangular_device(ns, "lower").item()) == 0
+
+
 @pytest.mark.parametrize("n", [33, 64, 100, 257, 512, 1000])
 def test_larger_n_bitwise(exact, n):
     """Multi-panel sizes (panels of 32, trailing tiles of 64, solve blocks of 32)."""

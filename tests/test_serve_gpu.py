@@ -165,3 +165,57 @@ def test_not_positive_definite_request(gpu_lla):
         assert res[2]["status"] == lla.NOT_POSITIVE_DEFINITE
     finally:
         srv.close()
+
+
+def test_device_loop_serves_requests_as_they_arrive(gpu_lla):
+    """Small requests go to the device-resident loop as soon as they are
+    admitted.  Requests submitted while the loop runs join it; a pause longer
+    than its idle limit lets its CTAs return, and the next request relaunches
+    it.  Each result is bit-identical to the batched kernel's solve of the same
+    system (the same per-CTA arithmetic), for f64 and f32."""
+    import time
+    torch = pytest.importorskip("torch")
+    lla = gpu_lla
+    rng = np.random.default_rng(99)
+    systems = []
+    for i in range(40):
+        n = int(rng.integers(16, 257))
+        m = int(rng.integers(1, 9))
+        dt = np.float64 if i % 3 else np.float32
+        g = rng.standard_normal((n, n))
+        systems.append(((g @ g.T / n + 0.1 * np.eye(n)).astype(dt), rng.standard_normal((n, m)).astype(dt)))
+    srv = lla.Server(batch_window_us=500.0, device_ctas=8)
+    outs = {}
+    try:
+        for tag, (a, b) in enumerate(systems):
+            tdt = torch.float64 if a.dtype == np.float64 else torch.float32
+            A, B = col(torch, a, tdt), col(torch, b, tdt)
+            torch.cuda.synchronize()
+            srv.submit(lla.REQ_SOLVE, A, B, tag=tag)
+            outs[tag] = B
+            if tag in (9, 19, 29):
+                time.sleep(0.02)  # longer than the idle limit: the loop's CTAs return
+        srv.drain()
+        res = {r["user_tag"]: r for r in srv.poll()}
+        stats = srv.stats()
+    finally:
+        srv.close()
+    assert stats["device_loop_launches"] >= 2, stats
+    for dt in (np.float64, np.float32):
+        idx = [i for i, (a, _) in enumerate(systems) if a.dtype == dt]
+        plan = lla.BatchPlan(np.array([systems[i][0].shape[0] for i in idx], np.int32),
+                             np.array([systems[i][1].shape[1] for i in idx], np.int32),
+                             "f64" if dt == np.float64 else "f32")
+        ap, bp = plan.pack([systems[i][0] for i in idx], [systems[i][1] for i in idx])
+        dA, dB = torch.from_numpy(ap).cuda(), torch.from_numpy(bp).cuda()
+        info = torch.full((plan.count,), -7, dtype=torch.int32, device="cuda")
+        plan.solve(dA, dB, info)
+        torch.cuda.synchronize()
+        xb = plan.unpack_x(dB.cpu().numpy())
+        for k, i in enumerate(idx):
+            r = res[i]
+            assert r["status"] == 0 and r["path"] == "batched", r
+            x = outs[i].cpu().numpy()
+            assert np.array_equal(x, xb[k]), (i, np.abs(x - xb[k]).max())
+            a, b = systems[i]
+            assert backward_error(a, x, b) <= 10 * a.shape[0] * np.finfo(dt).eps
