@@ -65,7 +65,7 @@ class Error(ctypes.Structure):
 
 class RefineOpts(ctypes.Structure):
     _fields_ = [("update", ctypes.c_int32), ("max_iters", ctypes.c_int32), ("tol", ctypes.c_double),
-                ("equilibrate", ctypes.c_int32), ("fallback", ctypes.c_int32), ("nb", ctypes.c_int32),
+                ("equilibrate", ctypes.c_int32), ("fallback", ctypes.c_int32), ("update_epilogue", ctypes.c_int32),
                 ("residual", ctypes.c_int32), ("sub_ctas_per_sm", ctypes.c_int32),
                 ("update_kchunk", ctypes.c_int32)]
 
@@ -543,7 +543,7 @@ def debug_inject_lost_handoff(spin_limit=1000):
 
 # ---- mixed-precision refined solve (no counterpart in the reference) --------
 
-def refine_opts(update="bf16x6", max_iters=30, tol=1e-13, equilibrate=True, fallback=True, nb=0,
+def refine_opts(update="bf16x6", max_iters=30, tol=1e-13, equilibrate=True, fallback=True, update_epilogue=0,
                 residual="fp64", sub_ctas_per_sm=0, update_kchunk=0):
     o = RefineOpts()
     lib.lla_refine_opts_default(ctypes.byref(o))
@@ -551,7 +551,8 @@ def refine_opts(update="bf16x6", max_iters=30, tol=1e-13, equilibrate=True, fall
     o.update = UPDATE_NAMES[update] if isinstance(update, str) else int(update)
     o.residual = RESIDUAL_NAMES[residual] if isinstance(residual, str) else int(residual)
     o.max_iters, o.tol = max_iters, tol
-    o.equilibrate, o.fallback, o.nb = int(bool(equilibrate)), int(bool(fallback)), nb
+    o.equilibrate, o.fallback = int(bool(equilibrate)), int(bool(fallback))
+    o.update_epilogue = update_epilogue
     return o
 
 

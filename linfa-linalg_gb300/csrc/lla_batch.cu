@@ -262,19 +262,40 @@ __global__ void __launch_bounds__(256, 2) batch_posv_kernel(const BatchItem *__r
 // on this GPU: the factorisation (n^3/3) moves to the FP32 pipe and only
 // 2 n^2 m per iteration stays in FP64.
 constexpr int kBRefIters = 6;
-constexpr double kBRefTol = 4.0 * 2.220446049250313e-16;
+// Stop at n eps / 16 (about what the plain FP64 batched solve reaches); a
+// system left above 10 n eps is re-solved in plain FP64.
+constexpr double kBRefTolPerN = 2.220446049250313e-16 / 16.0;
 constexpr size_t kBRefScratch = (size_t)kBMaxN * kBMaxN * 8 + (size_t)kBMaxN * kBMaxRhs * (4 + 8);
 
-__device__ __forceinline__ double block_max_double(double v, double *red) {
+// Column maxima of |X| and |R| (m <= kBMaxRhs columns each) over the CTA in one
+// reduction: vx, vr hold this thread's partial maxima; on return every thread
+// holds the CTA's.  red: 8 warps x 2 kBMaxRhs doubles of shared memory.
+__device__ __forceinline__ void block_max_cols(double (&vx)[kBMaxRhs], double (&vr)[kBMaxRhs], double *red) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
 #pragma unroll
-    for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int j = 0; j < kBMaxRhs; ++j)
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            vx[j] = fmax(vx[j], __shfl_xor_sync(0xffffffffu, vx[j], o));
+            vr[j] = fmax(vr[j], __shfl_xor_sync(0xffffffffu, vr[j], o));
+        }
     __syncthreads();
-    if (lane == 0) red[warp] = v;
+    if (lane == 0)
+#pragma unroll
+        for (int j = 0; j < kBMaxRhs; ++j) {
+            red[warp * 2 * kBMaxRhs + j] = vx[j];
+            red[warp * 2 * kBMaxRhs + kBMaxRhs + j] = vr[j];
+        }
     __syncthreads();
-    double r = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, red[w]);
-    return r;
+#pragma unroll
+    for (int j = 0; j < kBMaxRhs; ++j) {
+        vx[j] = 0.0;
+        vr[j] = 0.0;
+        for (int w = 0; w < nw; ++w) {
+            vx[j] = fmax(vx[j], red[w * 2 * kBMaxRhs + j]);
+            vr[j] = fmax(vr[j], red[w * 2 * kBMaxRhs + kBMaxRhs + j]);
+        }
+    }
 }
 
 // out[i + j n] (+)= sign * sum_k A_sym(i, k) X[k][j] for the lower triangle of A
@@ -347,8 +368,8 @@ __global__ void __launch_bounds__(256, 2) batch_posv_refined_kernel(const BatchI
     float *sDf = (float *)smem_raw;    // FP32 factor and solves (same space)
     double *sX = (double *)(smem_raw + sizeof(double) * (32 * 33 + kBMaxN * 33));  // [kBMaxN][kBMaxRhs]
     __shared__ int s_item, s_fail;
-    __shared__ double red[8];
-    __shared__ double s_cx[kBMaxRhs], s_cr[kBMaxRhs], s_cb[kBMaxRhs];
+    __shared__ double red[8 * 2 * kBMaxRhs];
+    __shared__ double s_cb[kBMaxRhs];
     const int tid = threadIdx.x, nthr = blockDim.x;
     char *base = scratch + (size_t)blockIdx.x * kBRefScratch;
     float *W = (float *)base;  // FP32 factor (ld n); the FP64 fallback's working copy uses the same space
@@ -371,15 +392,24 @@ __global__ void __launch_bounds__(256, 2) batch_posv_refined_kernel(const BatchI
         // ||A||_inf and ||b_j||_inf
         sym_rows(A, n, nullptr, 1, nullptr, R, true);
         double an = 0.0;
-        for (int i = tid; i < n; i += nthr) an = fmax(an, R[i]);
-        an = block_max_double(an, red);
-        for (int j = 0; j < m; ++j) {
-            double v = 0.0;
-            for (int i = tid; i < n; i += nthr) v = fmax(v, fabs(B[i + (int64_t)j * n]));
-            v = block_max_double(v, red);
-            if (tid == 0) s_cb[j] = v;
+        {
+            double vb[kBMaxRhs], va[kBMaxRhs];
+#pragma unroll
+            for (int j = 0; j < kBMaxRhs; ++j) vb[j] = va[j] = 0.0;
+            for (int i = tid; i < n; i += nthr) {
+                va[0] = fmax(va[0], R[i]);
+#pragma unroll
+                for (int j = 0; j < kBMaxRhs; ++j)
+                    if (j < m) vb[j] = fmax(vb[j], fabs(B[i + (int64_t)j * n]));
+            }
+            block_max_cols(vb, va, red);
+            an = va[0];
+#pragma unroll
+            for (int j = 0; j < kBMaxRhs; ++j)
+                if (tid == j) s_cb[j] = vb[j];
         }
         __syncthreads();
+        const double tol = kBRefTolPerN * n;
         int f = batch_factor<float>(W, n, sDf, sDf + 32 * 33, &s_fail);
         bool ok = f < 0;
         if (ok) {
@@ -397,22 +427,29 @@ __global__ void __launch_bounds__(256, 2) batch_posv_refined_kernel(const BatchI
                 }
                 __syncthreads();
                 sym_rows(A, n, sX, m, B, R, false);
+                double vx[kBMaxRhs], vr[kBMaxRhs];
+#pragma unroll
+                for (int j = 0; j < kBMaxRhs; ++j) vx[j] = vr[j] = 0.0;
+                for (int i = tid; i < n; i += nthr) {
+#pragma unroll
+                    for (int j = 0; j < kBMaxRhs; ++j)
+                        if (j < m) {
+                            vx[j] = fmax(vx[j], fabs(sX[i * kBMaxRhs + j]));
+                            vr[j] = fmax(vr[j], fabs(R[i + (int64_t)j * n]));
+                        }
+                }
+                block_max_cols(vx, vr, red);
                 double e_max = 0.0;
-                for (int j = 0; j < m; ++j) {
-                    double vx = 0.0, vr = 0.0;
-                    for (int i = tid; i < n; i += nthr) {
-                        vx = fmax(vx, fabs(sX[i * kBMaxRhs + j]));
-                        vr = fmax(vr, fabs(R[i + (int64_t)j * n]));
-                    }
-                    vx = block_max_double(vx, red);
-                    vr = block_max_double(vr, red);
-                    const double den = an * vx + s_cb[j];
-                    double ej = den > 0 ? vr / den : (vr > 0 ? INFINITY : 0.0);
+#pragma unroll
+                for (int j = 0; j < kBMaxRhs; ++j) {
+                    if (j >= m) continue;
+                    const double den = an * vx[j] + s_cb[j];
+                    double ej = den > 0 ? vr[j] / den : (vr[j] > 0 ? INFINITY : 0.0);
                     if (ej != ej) ej = INFINITY;
                     e_max = fmax(e_max, ej);
                 }
                 eta = e_max;  // uniform across the CTA
-                if (eta <= kBRefTol || !(eta < INFINITY) || (itr >= 2 && eta > 0.5 * eta_prev)) break;
+                if (eta <= tol || !(eta < INFINITY) || (itr >= 2 && eta > 0.5 * eta_prev)) break;
                 eta_prev = eta;
             }
             ok = eta <= 10.0 * n * 2.220446049250313e-16;

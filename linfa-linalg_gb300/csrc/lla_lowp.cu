@@ -428,7 +428,8 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
                        narrow ? (double)rows * cols * kext * 2.0 - (double)cols * (cols - 1) * kext
                               : (double)rows * (rows + 1) * kext);
         return tc_update_launch(L, ld, q, n, (char *)planes + (size_t)q * ldp * esz, plane_stride, ldp, rows,
-                                kext, terms, fp16, pairs, info, err_word, narrow, st, opts.update_kchunk);
+                                kext, terms, fp16, pairs, info, err_word, narrow, st, opts.update_kchunk,
+                                opts.update_epilogue);
     };
     // Panels in pairs: after panel p only the next panel's 128 columns are
     // updated (narrow); panel p + 128 is factored, and then both panels'

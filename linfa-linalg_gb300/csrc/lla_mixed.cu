@@ -550,7 +550,7 @@ extern "C" void lla_refine_opts_default(lla_refine_opts *o) {
     o->tol = 1e-13;
     o->equilibrate = 1;
     o->fallback = 1;
-    o->nb = 0;
+    o->update_epilogue = 0;
     o->residual = LLA_RESIDUAL_FP64;
 }
 
@@ -589,7 +589,10 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
     cudaStream_t st = (cudaStream_t)stream;
     MixedWs &w = c->mixed;
     // workspace
-    MX_TRY(w.L.ensure(sizeof(float) * n * n));
+    // FP32 factor, column-major; a leading dimension of whole 16-byte rows lets the
+    // tensor-core update stage its output tiles with TMA
+    const int64_t ldl = (n + 3) / 4 * 4;
+    MX_TRY(w.L.ensure(sizeof(float) * ldl * n));
     MX_TRY(w.s.ensure(sizeof(double) * n));
     MX_TRY(w.rowsum.ensure(sizeof(double) * n));
     MX_TRY(w.R.ensure(sizeof(double) * n * m));
@@ -658,13 +661,13 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
         MX_TRY(w.oz.ensure(oz_workspace_bytes(n, m)));
         oz_rm = oz_rowmax(w.oz.p, n, m);
     }
-    MX_TRY(last_err(equilibrate_launch(dA, lda, n, opts.equilibrate != 0, s, L, n,
+    MX_TRY(last_err(equilibrate_launch(dA, lda, n, opts.equilibrate != 0, s, L, ldl,
                                        (double *)w.rowsum.p, anorm, oz_rm, (double *)w.sympart.p, bad, st, info)));
     MX_TRY(last_err(colmax_launch(dB, ldb, n, m, colmax_b, st)));
     // 2. low-precision factorisation (its kernels return at once after a breakdown)
-    MX_TRY(last_err(lowp_factor_launch(L, n, n, opts, info, (float *)w.diag0.p, min_ratio, c, st)));
+    MX_TRY(last_err(lowp_factor_launch(L, n, ldl, opts, info, (float *)w.diag0.p, min_ratio, c, st)));
     // inverses of the 64 x 64 diagonal blocks, reused by every substitution
-    MX_TRY(last_err(diag_inverse_launch(L, n, n, (float *)w.winv.p, st)));
+    MX_TRY(last_err(diag_inverse_launch(L, ldl, n, (float *)w.winv.p, st)));
     if (slices)  // slices of A, once per solve
         MX_TRY(last_err(oz_prepare(dA, lda, n, m, w.oz.p, true, st)));
     // 3. refinement, controlled on the device: every iteration ends with a check
@@ -689,10 +692,10 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
             const int64_t ldrhs = enqueued == 0 ? ldb : n;
             MX_TRY(last_err(scale_to_f32_launch(rhs, ldrhs, s, n, m, Y, st, state)));
             MX_TRY(next_epoch());
-            MX_TRY(last_err(trsm_inv_launch(L, n, Wi, n, Y, n, m, 0, stage, w.stage_epoch, tws, err_word, st, state,
+            MX_TRY(last_err(trsm_inv_launch(L, ldl, Wi, n, Y, n, m, 0, stage, w.stage_epoch, tws, err_word, st, state,
                                             sub_cps)));
             MX_TRY(next_epoch());
-            MX_TRY(last_err(trsm_inv_launch(L, n, Wi, n, Y, n, m, 1, stage, w.stage_epoch, tws, err_word, st, state,
+            MX_TRY(last_err(trsm_inv_launch(L, ldl, Wi, n, Y, n, m, 1, stage, w.stage_epoch, tws, err_word, st, state,
                                             sub_cps)));
             MX_TRY(last_err(update_x_launch(dX, ldx, s, Y, n, m, colmax_x, st, state)));
             // r = b - A x  (FP64 accuracy)

@@ -28,6 +28,7 @@ int tc_update_prepare();
 // bounded waits record LLA_ERR_TIMEOUT in *err_word.
 int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, int64_t plane_stride,
                      int64_t ldp, int64_t rows, int kext, int terms, bool fp16, const TcPairs &pairs,
-                     const int64_t *info, int *err_word, bool narrow, cudaStream_t st, int kchunk = 64);
+                     const int64_t *info, int *err_word, bool narrow, cudaStream_t st, int kchunk = 64,
+                     int epilogue = 0);
 
 }  // namespace lla

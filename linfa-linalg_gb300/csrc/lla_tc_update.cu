@@ -22,6 +22,8 @@
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include "lla_common.cuh"
 #include "lla_tc.h"
 #include "lla_tcgen05.cuh"
@@ -29,9 +31,14 @@
 namespace lla {
 
 constexpr int kTcM = 128, kTcN = 128;            // tile
-constexpr int kTcRingBytes = 192 * 1024;          // operand stages
 constexpr int kTcMaxStages = 8;
-constexpr int kTcSmem = 1024 + kTcRingBytes + 256;
+// Shared memory: the operand ring, then (TMA-staged epilogue only) one FP32
+// 128 x 128 output tile, then the barriers.
+constexpr int kTcTileC = kTcM * kTcN * 4;  // 64 KiB
+__host__ __device__ constexpr int tc_ring_bytes(bool epi_tma) { return epi_tma ? 144 * 1024 : 192 * 1024; }
+__host__ __device__ constexpr int tc_smem_bytes(bool epi_tma) {
+    return 1024 + tc_ring_bytes(epi_tma) + (epi_tma ? kTcTileC : 0) + 256;
+}
 // K-chunk KC of a stage: 64 (128-byte rows, 128-byte swizzle) or 32 (64-byte
 // rows, 64-byte swizzle: twice the stages in the same ring, so more loads are
 // in flight ahead of the MMAs).  One term plane of one operand: 128 x KC x 2 B.
@@ -41,9 +48,9 @@ __host__ __device__ constexpr int tc_tile_bytes() { return kTcM * KC * 2; }
 // K-chunk, so each plane is loaded once per chunk and serves all the term
 // pairs that use it.
 template <int KC>
-__host__ __device__ constexpr int tc_stages(int terms) {
-    return (kTcRingBytes / (2 * terms * tc_tile_bytes<KC>())) < kTcMaxStages
-               ? kTcRingBytes / (2 * terms * tc_tile_bytes<KC>())
+__host__ __device__ constexpr int tc_stages(int terms, bool epi_tma) {
+    return (tc_ring_bytes(epi_tma) / (2 * terms * tc_tile_bytes<KC>())) < kTcMaxStages
+               ? tc_ring_bytes(epi_tma) / (2 * terms * tc_tile_bytes<KC>())
                : kTcMaxStages;
 }
 // Shared-memory descriptor of a K-major tile stored with the KC-wide swizzle:
@@ -100,13 +107,21 @@ __device__ __forceinline__ constexpr int tc_pb(int terms, int i) {
 
 // 320 threads are 10 warps, so one SM sub-partition runs 3 of them from its
 // 16K registers: at most 170 registers a thread (168 allocated).
-template <int TERMS, int KC>
+//
+// EPI_TMA: the epilogue stages the FP32 output tile in shared memory -- one
+// elected epilogue thread loads it with a TMA box while the tile's MMAs run
+// and stores it back with a TMA box -- so the tile's 64 KiB each way are in
+// flight without registers; the threads only read the accumulator, read and
+// write shared memory.  Diagonal tiles write back their upper part unchanged.
+// Needs a leading dimension that is a multiple of 4 floats (16-byte rows).
+template <int TERMS, int KC, bool EPI_TMA>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
-    const __grid_constant__ CUtensorMap tmap, float *C, int64_t ld, int64_t q, int64_t n, int kchunks,
-    uint32_t idesc, int64_t ntiles, int narrow, const int64_t *info, int *err_word) {
+    const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap cmap, float *C, int64_t ld,
+    int64_t q, int64_t n, int kchunks, uint32_t idesc, int64_t ntiles, int narrow, const int64_t *info,
+    int *err_word) {
     constexpr int terms = TERMS, NP = tc_npairs(TERMS);
     extern __shared__ uint8_t smem_raw[];
-    __shared__ int s_abort, s_skip;
+    __shared__ int s_abort, s_skip, s_epi_abort;
     // one reader decides for the whole CTA (another CTA may set err_word meanwhile)
     if (threadIdx.x == 0)
         s_skip = (*(volatile const int64_t *)info >= 0 || *(volatile const int *)err_word != 0);
@@ -114,15 +129,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     if (s_skip) return;
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     constexpr int kTile = tc_tile_bytes<KC>();
-    const int S = tc_stages<KC>(terms);
+    const int S = tc_stages<KC>(terms, EPI_TMA);
     const uint32_t opnd = (uint32_t)terms * kTile;  // one operand's planes in a stage
     uint8_t *ring = smem;                                   // stage s: A planes, then B planes
-    uint64_t *bars = (uint64_t *)(smem + kTcRingBytes);
-    // bars: full[S], empty[S], tmem_full[2], tmem_empty[2]
-    uint32_t *tslot = (uint32_t *)(bars + 2 * kTcMaxStages + 4);
+    float *sC = (float *)(smem + tc_ring_bytes(EPI_TMA));  // EPI_TMA: sC[c * 128 + r]
+    uint64_t *bars = (uint64_t *)(smem + tc_ring_bytes(EPI_TMA) + (EPI_TMA ? kTcTileC : 0));
+    // bars: full[S], empty[S], tmem_full[2], tmem_empty[2], c_full
+    uint32_t *tslot = (uint32_t *)(bars + 2 * kTcMaxStages + 5);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kTcMaxStages);
     const uint32_t tfull0 = smem_u32(bars + 2 * kTcMaxStages), tempty0 = tfull0 + 16;
+    const uint32_t cfull = tfull0 + 32;
     if (tid == 0) {
         for (int s = 0; s < S; ++s) {
             mbar_init(full0 + 8 * s, 1);
@@ -132,8 +149,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
             mbar_init(tfull0 + 8 * a, 1);
             mbar_init(tempty0 + 8 * a, kTcEpiThreads);  // every epilogue thread releases
         }
+        mbar_init(cfull, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
+        s_epi_abort = 0;
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -209,6 +228,66 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
                 tc_commit(tfull0 + 8 * a);  // accumulator a is complete
             }
         }
+    } else if (EPI_TMA) {  // warps 0-7: epilogue through the shared-memory tile
+        int64_t lt = 0;
+        const int qw = warp & 3, half = warp >> 2;
+        constexpr bool cross = NP > 1;
+        const int r = qw * 32 + lane;
+        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
+            const int a = (int)(lt & 1);
+            const int64_t use = lt >> 1;
+            int64_t I, J;
+            tc_tile(t, narrow, I, J);
+            if (tid == 0) {
+                // the previous tile's store has read the buffer: load this tile into it
+                asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                mbar_expect_tx(cfull, (uint32_t)kTcTileC);
+                tma_load_2d(smem_u32(sC), &cmap, (int)(q + I * kTcM), (int)(q + J * kTcN), cfull);
+            }
+            bool okc = mbar_wait(cfull, (uint32_t)(lt & 1), err_word);
+            bool ok = mbar_wait(tfull0 + 8 * a, (uint32_t)(use & 1), err_word) && okc;
+            ok = __all_sync(0xffffffffu, ok) && !*(volatile int *)&s_abort;
+            // one decision for all eight epilogue warps (they meet at named barrier 1)
+            if (!ok && lane == 0) s_epi_abort = 1;
+            asm volatile("bar.sync 1, %0;" ::"n"(kTcEpiThreads) : "memory");
+            if (*(volatile int *)&s_epi_abort) {
+                if (tid == 0) {
+                    s_abort = 1;
+                    // the tile load issued above must land before the CTA leaves (bounded)
+                    for (long long i = 0; !okc && i < kTcSpin; ++i) okc = mbar_try_wait(cfull, (uint32_t)(lt & 1));
+                }
+                break;
+            }
+            tc_fence_after();
+            const uint32_t ta = tmem + (uint32_t)(a * 2 * kTcCols) + ((uint32_t)(qw * 32) << 16);
+#pragma unroll
+            for (int sb = 0; sb < 4; ++sb) {  // 16 columns: leading and cross-term sums
+                uint32_t v[16], w[16];
+                const uint32_t col = (uint32_t)(half * 64 + sb * 16);
+                tc_ld16_nowait(ta + col, v);
+                if (cross) tc_ld16_nowait(ta + kTcCols + col, w);
+                tc_wait_ld();
+#pragma unroll
+                for (int c16 = 0; c16 < 16; ++c16) {
+                    const int cc = half * 64 + sb * 16 + c16;
+                    const float prod =
+                        cross ? __uint_as_float(v[c16]) + __uint_as_float(w[c16]) : __uint_as_float(v[c16]);
+                    // a diagonal tile keeps its upper part as loaded
+                    if (I != J || cc <= r) sC[cc * kTcM + r] -= prod;
+                }
+            }
+            // the accumulator is read: release it to the MMA warp
+            tc_fence_before();
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tempty0 + 8 * a) : "memory");
+            // the tile's shared-memory writes, then one thread stores it
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("bar.sync 1, %0;" ::"n"(kTcEpiThreads) : "memory");
+            if (tid == 0) {
+                tma_store_2d(&cmap, smem_u32(sC), (int)(q + I * kTcM), (int)(q + J * kTcN));
+                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            }
+        }
+        if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");  // stores complete
     } else {  // warps 0-7: epilogue; warp w drains lane quarter w % 4, columns 64 (w / 4) ..
         int64_t lt = 0;
         const int qw = warp & 3, half = warp >> 2;
@@ -294,25 +373,30 @@ PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
     return g_encode;
 }
 
-template <int KC>
+template <int KC, bool E>
 static bool tc_set_attrs() {
-    return cudaFuncSetAttribute(tc_update_kernel<1, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) ==
+    const int sm = tc_smem_bytes(E);
+    return cudaFuncSetAttribute(tc_update_kernel<1, KC, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) ==
                cudaSuccess &&
-           cudaFuncSetAttribute(tc_update_kernel<2, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) ==
+           cudaFuncSetAttribute(tc_update_kernel<2, KC, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) ==
                cudaSuccess &&
-           cudaFuncSetAttribute(tc_update_kernel<3, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) ==
+           cudaFuncSetAttribute(tc_update_kernel<3, KC, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) ==
                cudaSuccess;
 }
 
 int tc_update_prepare() {
     if (!tma_encoder()) return -1;
-    return tc_set_attrs<64>() && tc_set_attrs<32>() ? 0 : -1;
+    return tc_set_attrs<64, false>() && tc_set_attrs<32, false>() && tc_set_attrs<32, true>() ? 0 : -1;
 }
 
 int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, int64_t plane_stride,
                      int64_t ldp, int64_t rows, int kext, int terms, bool fp16, const TcPairs &pairs,
-                     const int64_t *info, int *err_word, bool narrow, cudaStream_t st, int kchunk) {
-    const int kc = kchunk == 32 ? 32 : 64;
+                     const int64_t *info, int *err_word, bool narrow, cudaStream_t st, int kchunk,
+                     int epilogue) {
+    // the TMA-staged epilogue (default) needs 16-byte rows of C and 32-wide K-chunks
+    const bool epi_tma = epilogue != 1 && ld % 4 == 0 && (reinterpret_cast<uintptr_t>(C) & 15) == 0 &&
+                         ld * 4 < (1ll << 40) && n < (1ll << 31);
+    const int kc = (epi_tma || kchunk == 32) ? 32 : 64;
     if (!g_encode || rows <= 0 || kext % kc != 0 || kext > ldp || (ldp * 2) % 16 != 0 || terms < 1 ||
         terms > 3 || (reinterpret_cast<uintptr_t>(planes) & 15) != 0)
         return -1;
@@ -329,6 +413,18 @@ int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, i
                  kc == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return -1;
+    CUtensorMap cmap;  // the FP32 matrix, column-major: rows are the inner dimension
+    std::memset(&cmap, 0, sizeof(cmap));
+    if (epi_tma) {
+        const cuuint64_t cdims[2] = {(cuuint64_t)n, (cuuint64_t)n};
+        const cuuint64_t cstrides[1] = {(cuuint64_t)ld * 4};
+        const cuuint32_t cbox[2] = {(cuuint32_t)kTcM, (cuuint32_t)kTcN};
+        const cuuint32_t cestr[2] = {1, 1};
+        if (g_encode(&cmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, C, cdims, cstrides, cbox, cestr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return -1;
+    }
     // instruction descriptor: D = F32 (bits 4-5), A/B = BF16 (1) or F16 (0) (bits 7-9, 10-12),
     // both K-major, N >> 3 at bit 17, M >> 4 at bit 24
     const uint32_t ab = fp16 ? 0u : 1u;
@@ -346,11 +442,14 @@ int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, i
     if (pairs.n != (terms == 1 ? 1 : (terms == 2 ? 3 : 6)) || pairs.pa[pairs.n - 1] != 0 ||
         pairs.pb[pairs.n - 1] != 0)
         return -1;
-    auto kern = kc == 32 ? (terms == 1 ? tc_update_kernel<1, 32>
-                                       : (terms == 2 ? tc_update_kernel<2, 32> : tc_update_kernel<3, 32>))
-                         : (terms == 1 ? tc_update_kernel<1, 64>
-                                       : (terms == 2 ? tc_update_kernel<2, 64> : tc_update_kernel<3, 64>));
-    kern<<<grid, kTcThreads, kTcSmem, st>>>(map, C, ld, q, n, kext / kc, idesc, tiles, narrow ? 1 : 0, info,
+    auto kern = epi_tma ? (terms == 1 ? tc_update_kernel<1, 32, true>
+                                      : (terms == 2 ? tc_update_kernel<2, 32, true> : tc_update_kernel<3, 32, true>))
+                : kc == 32 ? (terms == 1 ? tc_update_kernel<1, 32, false>
+                                         : (terms == 2 ? tc_update_kernel<2, 32, false> : tc_update_kernel<3, 32, false>))
+                           : (terms == 1 ? tc_update_kernel<1, 64, false>
+                                         : (terms == 2 ? tc_update_kernel<2, 64, false> : tc_update_kernel<3, 64, false>));
+    kern<<<grid, kTcThreads, tc_smem_bytes(epi_tma), st>>>(map, cmap, C, ld, q, n, kext / kc, idesc, tiles,
+                                                            narrow ? 1 : 0, info,
                                             err_word);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

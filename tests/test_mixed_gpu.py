@@ -277,17 +277,41 @@ def test_headline_size_n16384_kappa_1e6(gpu_lla):
 
 
 @pytest.mark.parametrize("update", ["bf16x6", "bf16x3", "fp16x3"])
-@pytest.mark.parametrize("kchunk", [32, 64])
-def test_update_kchunk_forms(gpu_lla, update, kchunk):
+@pytest.mark.parametrize("kchunk,epilogue", [(64, 1), (32, 1), (32, 0)])
+def test_update_kchunk_forms(gpu_lla, update, kchunk, epilogue):
     """The tensor-core update with 64-wide K-chunks (128-byte swizzle) and with
-    32-wide K-chunks (64-byte swizzle, twice the stages): both converge to the
-    FP64 target, and their factors agree to FP32 accuracy."""
+    32-wide K-chunks (64-byte swizzle, twice the stages), with the register
+    epilogue (1) and the TMA-staged one (0): all converge to the FP64 target."""
     lla = gpu_lla
-    rng = np.random.default_rng(3 + kchunk)
+    rng = np.random.default_rng(3 + kchunk + epilogue)
     n = 1537
     a = qdq(rng, n, 1e6)
     b = rng.standard_normal((n, 9))
     x = b.copy()
-    rep = lla.posv_refined(a, x, update=update, update_kchunk=kchunk)
+    rep = lla.posv_refined(a, x, update=update, update_kchunk=kchunk, update_epilogue=epilogue)
     assert rep["converged"] == 1 and rep["fell_back"] == 0, rep
     assert backward_error(a, x, b) <= 2e-13
+
+
+@pytest.mark.parametrize("n", [300, 1030])
+def test_lowp_factor_leaves_upper_triangle(gpu_lla, n):
+    """The in-place low-precision factorisation writes the lower triangle only:
+    the TMA-staged epilogue (leading dimension a multiple of 4: n = 300) stores
+    whole tiles and must write the upper part of diagonal tiles back unchanged;
+    the register epilogue (n = 1030) never touches it."""
+    torch = pytest.importorskip("torch")
+    lla = gpu_lla
+    rng = np.random.default_rng(n)
+    a = cases.spd_gram(rng, n)
+    d = 1.0 / np.sqrt(np.diag(a))
+    a = (a * d[:, None] * d[None, :]).astype(np.float32)
+    junk = rng.standard_normal((n, n)).astype(np.float32)
+    a_in = np.tril(a) + np.triu(junk, 1)
+    A = torch.tensor(a_in, device="cuda").T.contiguous().T
+    info = lla.spotrf_mixed_device(A, update="bf16x6")
+    torch.cuda.synchronize()
+    assert int(info.item()) == -1
+    out = A.cpu().numpy()
+    assert np.array_equal(np.triu(out, 1), np.triu(junk, 1))
+    L = np.tril(out.astype(np.float64))
+    assert np.linalg.norm(L @ L.T - a) / np.linalg.norm(a) <= 4e-6
