@@ -291,6 +291,14 @@ enum lla_update {
  *                             FP64 -- an error bound like an FP64 product's. */
 enum lla_residual { LLA_RESIDUAL_FP64 = 0, LLA_RESIDUAL_EXACT_SLICES = 1 };
 
+/* The refinement's FP32 triangular solves (with inverted 64 x 64 diagonal blocks):
+ *  LLA_SUB_LOOKBACK  one CTA per (block, column chunk), blocks handed from CTA
+ *                    to CTA through epoch-tagged words (default);
+ *  LLA_SUB_CHAIN     one CTA per column chunk walks every block and keeps the
+ *                    two previous blocks on chip; helper CTAs form the coupling
+ *                    sums with earlier blocks in groups. */
+enum lla_substitution { LLA_SUB_AUTO = 0, LLA_SUB_CHAIN = 1, LLA_SUB_LOOKBACK = 2 };
+
 typedef struct lla_refine_opts {
     int32_t update;      /* lla_update (default LLA_UPDATE_BF16X6) */
     int32_t max_iters;   /* refinement iterations before giving up (default 30) */
@@ -300,7 +308,7 @@ typedef struct lla_refine_opts {
     int32_t update_epilogue; /* tensor-core update epilogue: 0 FP32 tile staged by TMA (default, when
                                 the leading dimension allows), 1 register loads and stores */
     int32_t residual;    /* lla_residual (default LLA_RESIDUAL_FP64) */
-    int32_t sub_ctas_per_sm; /* CTAs per SM of the FP32 substitutions: 1 or 2 (0: default) */
+    int32_t substitution;    /* lla_substitution: form of the FP32 substitutions (0: default) */
     int32_t update_kchunk;   /* K-chunk of the tensor-core update's operand stages: 64 or 32 (0: default) */
 } lla_refine_opts;
 

@@ -66,7 +66,7 @@ class Error(ctypes.Structure):
 class RefineOpts(ctypes.Structure):
     _fields_ = [("update", ctypes.c_int32), ("max_iters", ctypes.c_int32), ("tol", ctypes.c_double),
                 ("equilibrate", ctypes.c_int32), ("fallback", ctypes.c_int32), ("update_epilogue", ctypes.c_int32),
-                ("residual", ctypes.c_int32), ("sub_ctas_per_sm", ctypes.c_int32),
+                ("residual", ctypes.c_int32), ("substitution", ctypes.c_int32),
                 ("update_kchunk", ctypes.c_int32)]
 
 
@@ -544,10 +544,12 @@ def debug_inject_lost_handoff(spin_limit=1000):
 # ---- mixed-precision refined solve (no counterpart in the reference) --------
 
 def refine_opts(update="bf16x6", max_iters=30, tol=1e-13, equilibrate=True, fallback=True, update_epilogue=0,
-                residual="fp64", sub_ctas_per_sm=0, update_kchunk=0):
+                residual="fp64", substitution="auto", update_kchunk=0):
     o = RefineOpts()
     lib.lla_refine_opts_default(ctypes.byref(o))
-    o.sub_ctas_per_sm, o.update_kchunk = sub_ctas_per_sm, update_kchunk
+    o.substitution = {"auto": 0, "chain": 1, "lookback": 2}[substitution] if isinstance(substitution, str) \
+        else int(substitution)
+    o.update_kchunk = update_kchunk
     o.update = UPDATE_NAMES[update] if isinstance(update, str) else int(update)
     o.residual = RESIDUAL_NAMES[residual] if isinstance(residual, str) else int(residual)
     o.max_iters, o.tol = max_iters, tol

@@ -602,7 +602,8 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
     MX_TRY(w.words.ensure(sizeof(double) * (8 + 3 * m)));
     MX_TRY(c->ws.ensure(sizeof(int) * (std::max(trsm_ws_ints(n, m), trsm_inv_ws_ints(n, m)) + 1)));
     MX_TRY(w.winv.ensure(sizeof(float) * diag_inverse_floats(n)));
-    MX_TRY(w.stage.ensure(sizeof(unsigned long long) * trsm_inv_stage_words(n, m)));
+    MX_TRY(w.stage.ensure(sizeof(unsigned long long) *
+                          std::max(trsm_inv_stage_words(n, m), trsm_chain_stage_words(n, m))));
     if (w.stage.p != w.stage_seen || w.stage.cap != w.stage_seen_cap) {
         MX_TRY(cudaMemsetAsync(w.stage.p, 0, w.stage.cap, st));
         w.stage_seen = w.stage.p;
@@ -681,7 +682,8 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
         MX_TRY(cudaMemsetAsync(dX + j * ldx, 0, sizeof(double) * n, st));
     MX_TRY(cudaMemsetAsync(err_word, 0, sizeof(int), st));
     const float *Wi = (const float *)w.winv.p;
-    const int sub_cps = opts.sub_ctas_per_sm == 1 ? 1 : 2;
+    const bool chain = opts.substitution == LLA_SUB_CHAIN;
+    auto subst = chain ? trsm_chain_launch : trsm_inv_launch;
     double eta = INFINITY;
     bool converged = false, lowp_ok = true;
     int enqueued = 0, group = kRefineGroup;
@@ -692,11 +694,9 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
             const int64_t ldrhs = enqueued == 0 ? ldb : n;
             MX_TRY(last_err(scale_to_f32_launch(rhs, ldrhs, s, n, m, Y, st, state)));
             MX_TRY(next_epoch());
-            MX_TRY(last_err(trsm_inv_launch(L, ldl, Wi, n, Y, n, m, 0, stage, w.stage_epoch, tws, err_word, st, state,
-                                            sub_cps)));
+            MX_TRY(last_err(subst(L, ldl, Wi, n, Y, n, m, 0, stage, w.stage_epoch, tws, err_word, st, state)));
             MX_TRY(next_epoch());
-            MX_TRY(last_err(trsm_inv_launch(L, ldl, Wi, n, Y, n, m, 1, stage, w.stage_epoch, tws, err_word, st, state,
-                                            sub_cps)));
+            MX_TRY(last_err(subst(L, ldl, Wi, n, Y, n, m, 1, stage, w.stage_epoch, tws, err_word, st, state)));
             MX_TRY(last_err(update_x_launch(dX, ldx, s, Y, n, m, colmax_x, st, state)));
             // r = b - A x  (FP64 accuracy)
             if (slices)

@@ -47,7 +47,14 @@ size_t trsm_inv_stage_words(int64_t n, int64_t m);
 int diag_inverse_launch(const float *L, int64_t ld, int64_t n, float *W, cudaStream_t st);
 int trsm_inv_launch(const float *L, int64_t ld, const float *W, int64_t n, float *B, int64_t ldb,
                     int64_t m, int trans, unsigned long long *stage, unsigned epoch, int *ws, int *err_word,
-                    cudaStream_t st, const int *state = nullptr, int ctas_per_sm = 2);
+                    cudaStream_t st, const int *state = nullptr);
+// The chain form of the same substitutions (one CTA per column chunk walks the
+// blocks; helper CTAs form the coupling sums): stage holds
+// trsm_chain_stage_words(n, m) 64-bit words, zeroed when allocated.
+size_t trsm_chain_stage_words(int64_t n, int64_t m);
+int trsm_chain_launch(const float *L, int64_t ld, const float *W, int64_t n, float *B, int64_t ldb,
+                      int64_t m, int trans, unsigned long long *stage, unsigned epoch, int *ws, int *err_word,
+                      cudaStream_t st, const int *state = nullptr);
 
 // Exact-slice (tensor-core) residual: workspace size, once-per-solve slicing
 // of A, and the per-iteration residual (colmax_x: column maxima of |X|).

@@ -178,7 +178,6 @@ constexpr int64_t kIvHelperMin = 16;  // first position whose coupling terms are
 constexpr int kIvYd = kIvNb + 2;  // words per staged column (padded: 528-byte columns)
 constexpr size_t kIvSmem = sizeof(float) * ((size_t)kIvStages * kIvNb * kIvLd + 2ull * kIvStages * kIvCols * kIvYd +
                                             2ull * kIvNb * kIvCols + 2ull * kIvCols * kIvLd);
-constexpr size_t kIvSmemSolo = 120 * 1024;  // more than half of an SM's shared memory: one CTA per SM
 
 // TRANS = false: L Y = B (blocks ascending); TRANS = true: L^T X = B (descending).
 // 256 threads.  The coupling tiles and the solved words of earlier blocks
@@ -521,11 +520,384 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
     }
 }
 
+// ---------------------------------------------------------------------------
+// Chain form.  One CTA per column chunk (the chain) walks every block of its
+// chunk in processing order and keeps the two previously solved blocks in
+// shared memory, so the block-to-block critical path has no inter-CTA
+// hand-off:
+//     y_r = sum_g P_{r,g} - F_r^2 y_{r-2} - F_r^1 y_{r-1}
+//     (TRANS: x_r = sum_g P_{r,g} - G_r^2 x_{r+2} - G_r^1 x_{r+1}).
+// Helper CTAs form the partial sums P_{r,g} = W_r (b_r [g = 0] - sum_{q in g}
+// L_rq y_q) over groups g of S earlier positions (all but the two
+// neighbours) with the bulk products above, and publish them as epoch-tagged
+// words; the chain reads the next block's words one step ahead.  Ticket
+// order (ch_decode): the chains first, then the helpers by position, so every
+// wait ends.
+template <bool TRANS>
+__global__ void __launch_bounds__(256, 2) trsm_chain_kernel(const float *__restrict__ L, int64_t ld,
+                                                            const float *__restrict__ Wall, int64_t n,
+                                                            float *B, int64_t ldb, int64_t m, int nchunks,
+                                                            unsigned long long *yw, int64_t ldy,
+                                                            unsigned long long *pw, int64_t S, int64_t Gmax,
+                                                            unsigned epoch, int *counter, int *err_word,
+                                                            const int *state) {
+    if (refine_done(state)) return;  // the refinement has finished: nothing to solve
+    constexpr int C = kIvCols, LPT = kIvTile / 256, NS = kIvStages;
+    constexpr int YCH = kIvNb * C / 2 / 256;  // 16-byte (two-word) copies per thread per stage
+    extern __shared__ __align__(16) float iv_smem[];
+    float(*sT)[kIvNb][kIvLd] = reinterpret_cast<float(*)[kIvNb][kIvLd]>(iv_smem);
+    unsigned long long(*sY)[C][kIvYd] =
+        reinterpret_cast<unsigned long long(*)[C][kIvYd]>(iv_smem + NS * kIvNb * kIvLd);
+    float(*sV)[kIvNb][C] = reinterpret_cast<float(*)[kIvNb][C]>(iv_smem + NS * kIvNb * kIvLd + 2 * NS * C * kIvYd);
+    float(*sYf)[C][kIvLd] =
+        reinterpret_cast<float(*)[C][kIvLd]>(iv_smem + NS * kIvNb * kIvLd + 2 * NS * C * kIvYd + 2 * kIvNb * C);
+    __shared__ int s_ticket, s_abort;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        s_ticket = atomicAdd(counter, 1);
+        s_abort = 0;
+    }
+    __syncthreads();
+    const int64_t R = (n + kIvNb - 1) / kIvNb;
+    bool chain;
+    int64_t pb;  // position in processing order (helpers)
+    int grp, cc;
+    ch_decode(s_ticket, R, S, nchunks, chain, pb, grp, cc);
+    const int ta = tid % kIvNb, tb = tid / kIvNb;
+    const int64_t col0 = (int64_t)cc * C;
+    const unsigned long long tag = (unsigned long long)epoch << 32;
+    const int64_t ldpw = R * Gmax * kIvNb;  // partial-sum words: (position, group, row) then column
+
+    if (chain) {
+        // shared memory of the chain: coupling tiles sM[buf][d - 1][k][i] (element
+        // (i, k) of M^d), double-buffered by position; the two previous blocks
+        // syv[p & 1][k][c]
+        float(*sM)[2][kIvNb][kIvLd] = reinterpret_cast<float(*)[2][kIvNb][kIvLd]>(iv_smem);
+        float(*syv)[kIvNb][C] = reinterpret_cast<float(*)[kIvNb][C]>(iv_smem + 4 * kIvNb * kIvLd);
+        // coupling tiles of position p into buffer b (column-major 64 x 64: 64 floats a column)
+        auto fetch = [&](int64_t p, int b) {
+            const int64_t r = TRANS ? R - 1 - p : p;
+#pragma unroll
+            for (int d = 1; d <= 2; ++d) {
+                if (p < d) continue;
+                const float *Mr = Wall + ((TRANS ? 2 * d : 2 * d - 1) * R + r) * kIvTile;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int e = tid + 256 * j, k = e >> 4, i4 = (e & 15) * 4;
+                    iv_cp16(&sM[b][d - 1][k][i4], Mr + k * kIvNb + i4, 16);
+                }
+            }
+            iv_commit();
+        };
+        // the partial-sum words of position p, row ta, columns col0 + 4 tb + u
+        unsigned long long wn[8][4];
+        auto load_words = [&](int64_t p) {
+            const int64_t r = TRANS ? R - 1 - p : p;
+            const int64_t grow = r * kIvNb + ta;
+            const int64_t G = ch_groups(p, S);
+#pragma unroll
+            for (int g = 0; g < 8; ++g)
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int64_t col = col0 + 4 * tb + u;
+                    wn[g][u] = (g < G && grow < n && col < m)
+                                   ? iv_ld_word(pw + ((p * Gmax + g) * kIvNb + ta) + col * ldpw)
+                                   : tag;
+                }
+        };
+        fetch(0, 0);
+        load_words(0);
+        for (int64_t p = 0; p < R; ++p) {
+            const int64_t r = TRANS ? R - 1 - p : p;
+            const int64_t grow = r * kIvNb + ta;
+            const int buf = (int)(p & 1);
+            const int64_t G = ch_groups(p, S);
+            unsigned long long(&w)[8][4] = wn;  // this position's words (loaded one step ahead)
+            if (p + 1 < R)  // the next position's coupling tiles, one step ahead
+                fetch(p + 1, buf ^ 1);
+            else
+                iv_commit();
+            // 1. the helpers' partial sums of this block (bounded wait for late ones)
+            {
+                long long spins = 0;
+                for (;;) {
+                    bool done = true;
+#pragma unroll
+                    for (int g = 0; g < 8; ++g)
+#pragma unroll
+                        for (int u = 0; u < 4; ++u)
+                            done &= (w[g][u] & 0xffffffff00000000ull) == tag;
+                    if (done) break;
+                    if (((++spins) & 63) == 0) {
+                        if (*(volatile int *)err_word != 0 || spins > kSpinLimit) {
+                            atomicCAS(err_word, 0, (int)LLA_ERR_TIMEOUT);
+                            s_abort = 1;
+                            break;
+                        }
+                        __nanosleep(32);
+                    }
+#pragma unroll
+                    for (int g = 0; g < 8; ++g)
+#pragma unroll
+                        for (int u = 0; u < 4; ++u)
+                            if ((w[g][u] & 0xffffffff00000000ull) != tag) {
+                                const int64_t col = col0 + 4 * tb + u;
+                                w[g][u] = iv_ld_word(pw + ((p * Gmax + g) * kIvNb + ta) + col * ldpw);
+                            }
+                }
+            }
+            float t[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int64_t col = col0 + 4 * tb + u;
+                float v = 0.f;
+                if (grow < n && col < m)
+#pragma unroll
+                    for (int g = 0; g < 8; ++g)
+                        if (g < G) v += __uint_as_float((unsigned)(w[g][u] & 0xffffffffull));
+                t[u] = v;
+            }
+            if (p + 1 < R) load_words(p + 1);  // in flight while the products below run
+            iv_wait<1>();  // this position's tiles (fetched one step earlier) have landed
+            __syncthreads();
+            if (s_abort) return;
+            // 2. t -= M^2 y_{p-2}, then t -= M^1 y_{p-1}
+#pragma unroll
+            for (int d = 2; d >= 1; --d) {
+                if (p < d) continue;
+                const float(*M)[kIvLd] = sM[buf][d - 1];
+                const float(*Y)[C] = syv[(p - d) & 1];
+#pragma unroll 8
+                for (int k = 0; k < kIvNb; ++k) {
+                    const float l = M[k][ta];
+                    const float4 x = *reinterpret_cast<const float4 *>(&Y[k][tb * 4]);
+                    t[0] = fmaf(-l, x.x, t[0]);
+                    t[1] = fmaf(-l, x.y, t[1]);
+                    t[2] = fmaf(-l, x.z, t[2]);
+                    t[3] = fmaf(-l, x.w, t[3]);
+                }
+            }
+            __syncthreads();  // every read of y_{p-2} is done: its buffer takes y_p
+            // 3. publish y_p
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int64_t col = col0 + 4 * tb + u;
+                const bool in = grow < n && col < m;
+                syv[buf][ta][4 * tb + u] = in ? t[u] : 0.f;
+                if (in) {
+                    B[grow + col * ldb] = t[u];
+                    iv_st_word(yw + grow + col * ldy, tag | (unsigned long long)__float_as_uint(t[u]));
+                }
+            }
+        }
+        iv_wait<0>();
+        return;
+    }
+
+    // helper: P_{r,g} for position pb, group grp
+    const int64_t rb = TRANS ? R - 1 - pb : pb;
+    const bool al16 = (ld % 4 == 0) && ((reinterpret_cast<uintptr_t>(L) & 15) == 0);
+    const int bc = tid % C, rg = tid / C;  // bulk mapping: column bc, rows 4 rg .. 4 rg + 3
+    float acc[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int64_t row = rb * kIvNb + 4 * rg + i, col = col0 + bc;
+        acc[i] = (grp == 0 && row < n && col < m) ? B[row + col * ldb] : 0.f;
+    }
+    float preW[LPT];
+    {
+        const float *Wr = Wall + rb * kIvTile + ta + tb * kIvNb;
+#pragma unroll
+        for (int u = 0; u < LPT; ++u) preW[u] = Wr[u * 4 * kIvNb];
+    }
+    // coupling terms of this group: positions q_lo .. q_lo + nbulk - 1 (never the two neighbours)
+    const int64_t q_lo = (int64_t)grp * S;
+    const int64_t q_hi = (q_lo + S < pb - 2) ? q_lo + S : pb - 2;
+    const int64_t nbulk = q_hi > q_lo ? q_hi - q_lo : 0;
+
+    // Stage s <- coupling tile and solved words of processing position pq.
+    // Tile: 64 columns a of 64 contiguous rows b (non-trans: a = k, b = i;
+    // trans: a = i, b = k), zero-filled past n.
+    auto issue = [&](int64_t pi, int s) {
+        if (pi < nbulk) {
+            const int64_t pq = q_lo + pi;
+            const int64_t qb = TRANS ? R - 1 - pq : pq;
+            const int64_t rowbase = (TRANS ? qb : rb) * kIvNb, colbase = (TRANS ? rb : qb) * kIvNb;
+            if (al16) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int e = tid + 256 * j, a = e >> 4, c4 = e & 15;
+                    const int64_t row = rowbase + 4 * c4, col = colbase + a;
+                    const bool ok = row < n && col < n;
+                    const int bytes = ok ? 4 * (int)(n - row < 4 ? n - row : 4) : 0;
+                    iv_cp16(&sT[s][a][4 * c4], ok ? L + row + col * ld : L, bytes);
+                }
+            } else {
+#pragma unroll 4
+                for (int j = 0; j < 16; ++j) {
+                    const int e = tid + 256 * j, a = e >> 6, b = e & 63;
+                    const int64_t row = rowbase + b, col = colbase + a;
+                    const bool ok = row < n && col < n;
+                    iv_cp4(&sT[s][a][b], ok ? L + row + col * ld : L, ok ? 4 : 0);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < YCH; ++j) {
+                const int e = tid + 256 * j, c = e >> 5, kp = e & 31;
+                const int64_t gk = qb * kIvNb + 2 * kp, col = col0 + c;
+                const bool ok = col < m;
+                iv_cp16(&sY[s][c][2 * kp], ok ? yw + gk + col * ldy : yw, ok ? 16 : 0);
+            }
+        }
+        iv_commit();
+    };
+    // The words this thread copied into stage s that are not yet published
+    // are re-read from global memory until they carry this launch's tag; their
+    // values go to sYf[buf] (words past n or m are zero: never written, or
+    // zero-filled by the copy).
+    static_assert(YCH == 2, "a thread settles the four words of its two copies together");
+    auto settle_stage = [&](int64_t pi, int s, int buf) {
+        const int64_t pq = q_lo + pi;
+        const int64_t qb = TRANS ? R - 1 - pq : pq;
+        unsigned long long w[4];
+        const unsigned long long *p[4];
+#pragma unroll
+        for (int j = 0; j < YCH; ++j) {
+            const int e = tid + 256 * j, c = e >> 5, kp = e & 31;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int k = 2 * kp + h;
+                const int64_t gk = qb * kIvNb + k, col = col0 + c;
+                w[2 * j + h] = sY[s][c][k];
+                p[2 * j + h] = (gk < n && col < m) ? yw + gk + col * ldy : nullptr;
+            }
+        }
+        iv_settle4(w, p, tag, err_word, &s_abort);
+#pragma unroll
+        for (int j = 0; j < YCH; ++j) {
+            const int e = tid + 256 * j, c = e >> 5, kp = e & 31;
+            *reinterpret_cast<float2 *>(&sYf[buf][c][2 * kp]) =
+                make_float2(__uint_as_float((unsigned)w[2 * j]), __uint_as_float((unsigned)w[2 * j + 1]));
+        }
+    };
+
+    // 1. every coupling term but the neighbour's (blocks solved well before this one)
+    const int kg = tid >> 6, cg = tid & 3, rq = (tid & 63) >> 2;
+    float part[4][4];  // part[j][jj]: row (trans ? rq + 16 j : 4 rq + j), column cg + 4 jj
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) part[j][jj] = 0.f;
+#pragma unroll
+    for (int s = 0; s < NS - 1; ++s) issue(s, s);
+    for (int64_t pq = 0; pq < nbulk; ++pq) {
+        const int s = (int)(pq % NS), buf = (int)(pq & 1);
+        iv_wait<NS - 2>();
+        settle_stage(pq, s, buf);
+        __syncthreads();
+        if (s_abort) break;
+        issue(pq + NS - 1, (int)((pq + NS - 1) % NS));
+#pragma unroll
+        for (int k4 = 0; k4 < 4; ++k4) {
+            const int k0 = 16 * kg + 4 * k4;
+            float4 x[4];
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) x[jj] = *reinterpret_cast<const float4 *>(&sYf[buf][cg + 4 * jj][k0]);
+            if (!TRANS) {  // coefficient of x_k in row i: sT[s][k][i]
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) {
+                    const float4 l4 = *reinterpret_cast<const float4 *>(&sT[s][k0 + kk][4 * rq]);
+#pragma unroll
+                    for (int jj = 0; jj < 4; ++jj) {
+                        const float xv = kk == 0 ? x[jj].x : kk == 1 ? x[jj].y : kk == 2 ? x[jj].z : x[jj].w;
+                        part[0][jj] = fmaf(-l4.x, xv, part[0][jj]);
+                        part[1][jj] = fmaf(-l4.y, xv, part[1][jj]);
+                        part[2][jj] = fmaf(-l4.z, xv, part[2][jj]);
+                        part[3][jj] = fmaf(-l4.w, xv, part[3][jj]);
+                    }
+                }
+            } else {  // coefficient of x_k in row i: sT[s][i][k]
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const float4 l4 = *reinterpret_cast<const float4 *>(&sT[s][rq + 16 * j][k0]);
+#pragma unroll
+                    for (int jj = 0; jj < 4; ++jj) {
+                        float a = part[j][jj];
+                        a = fmaf(-l4.x, x[jj].x, a);
+                        a = fmaf(-l4.y, x[jj].y, a);
+                        a = fmaf(-l4.z, x[jj].z, a);
+                        a = fmaf(-l4.w, x[jj].w, a);
+                        part[j][jj] = a;
+                    }
+                }
+            }
+        }
+    }
+    iv_wait<0>();
+    __syncthreads();
+    {  // add the four K-quarters' partial sums in order (stage 2 is free now)
+        float *red = &sT[2][0][0];  // red[kg][row][col], row stride 17
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj)
+                red[kg * kIvNb * 17 + (TRANS ? rq + 16 * j : 4 * rq + j) * 17 + cg + 4 * jj] = part[j][jj];
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float *r = red + (4 * rg + i) * 17 + bc;
+            acc[i] = (((acc[i] + r[0]) + r[kIvNb * 17]) + r[2 * kIvNb * 17]) + r[3 * kIvNb * 17];
+        }
+    }
+    if (s_abort) return;
+    // 2. t = W_r acc (W_r^T acc when trans)
+    float(*sK)[kIvLd] = sT[0];  // coefficient tile: sK[k][i]
+    float(*sX)[C] = sV[0];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) sX[4 * rg + i][bc] = acc[i];
+#pragma unroll
+    for (int u = 0; u < LPT; ++u) {  // preW[u] = W[ta][tb + 4u]
+        if (!TRANS)
+            sK[tb + 4 * u][ta] = preW[u];  // W[i][k]
+        else
+            sK[ta][tb + 4 * u] = preW[u];  // W[k][i]
+    }
+    __syncthreads();
+    float t[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 8
+    for (int k = 0; k < kIvNb; ++k) {
+        const float l = sK[k][ta];
+        const float4 x = *reinterpret_cast<const float4 *>(&sX[k][tb * 4]);
+        t[0] = fmaf(l, x.x, t[0]);
+        t[1] = fmaf(l, x.y, t[1]);
+        t[2] = fmaf(l, x.z, t[2]);
+        t[3] = fmaf(l, x.w, t[3]);
+    }
+    // 3. publish the partial sum for the chain
+    {
+        const int64_t grow = rb * kIvNb + ta;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t col = col0 + tb * 4 + u;
+            if (grow < n && col < m)
+                iv_st_word(pw + ((pb * Gmax + grp) * kIvNb + ta) + col * ldpw,
+                           tag | (unsigned long long)__float_as_uint(t[u]));
+        }
+    }
+}
+
 size_t trsm_inv_ws_ints(int64_t, int64_t) { return 1; }
 
 // solved values, then the helpers' partial sums
 size_t trsm_inv_stage_words(int64_t n, int64_t m) {
     return 2 * (size_t)((n + kIvNb - 1) / kIvNb) * kIvNb * (size_t)m;
+}
+
+// chain form: the solved words, then the helpers' partial sums (Gmax groups a position)
+size_t trsm_chain_stage_words(int64_t n, int64_t m) {
+    const int64_t R = (n + kIvNb - 1) / kIvNb;
+    const int64_t S = ch_group_size(R), Gmax = ch_groups(R - 1 > 0 ? R - 1 : 0, S);
+    return (size_t)(1 + Gmax) * R * kIvNb * (size_t)m;
 }
 
 size_t diag_inverse_floats(int64_t n) { return 5 * (size_t)((n + kIvNb - 1) / kIvNb) * kIvTile; }
@@ -545,15 +917,13 @@ int diag_inverse_launch(const float *L, int64_t ld, int64_t n, float *W, cudaStr
 
 int trsm_inv_launch(const float *L, int64_t ld, const float *W, int64_t n, float *B, int64_t ldb,
                     int64_t m, int trans, unsigned long long *stage, unsigned epoch, int *ws, int *err_word,
-                    cudaStream_t st, const int *state, int ctas_per_sm) {
+                    cudaStream_t st, const int *state) {
     if (n == 0 || m == 0) return 0;
     if (epoch == 0) return -1;
     const int nchunks = (int)((m + kIvCols - 1) / kIvCols);
     const int64_t R = (n + kIvNb - 1) / kIvNb;
     auto kern = trans ? trsm_inv_kernel<true> : trsm_inv_kernel<false>;
-    // two CTAs share an SM by default; one CTA per SM (shared memory reserved
-    // beyond half an SM) gives each block's critical product the whole SM
-    const size_t smem = ctas_per_sm == 1 ? std::max<size_t>(kIvSmem, kIvSmemSolo) : kIvSmem;
+    const size_t smem = kIvSmem;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return -1;
     if (cudaMemsetAsync(ws, 0, sizeof(int), st) != cudaSuccess) return -1;
@@ -564,6 +934,27 @@ int trsm_inv_launch(const float *L, int64_t ld, const float *W, int64_t n, float
     const int64_t items = iv_items_before(R, R, hmin, nchunks);  // every group
     kern<<<(unsigned)items, 256, smem, st>>>(L, ld, W, n, B, ldb, m, nchunks, stage, R * kIvNb, epoch, ws,
                                             err_word, hmin, state);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int trsm_chain_launch(const float *L, int64_t ld, const float *W, int64_t n, float *B, int64_t ldb,
+                      int64_t m, int trans, unsigned long long *stage, unsigned epoch, int *ws, int *err_word,
+                      cudaStream_t st, const int *state) {
+    if (n == 0 || m == 0) return 0;
+    if (epoch == 0) return -1;
+    const int nchunks = (int)((m + kIvCols - 1) / kIvCols);
+    const int64_t R = (n + kIvNb - 1) / kIvNb;
+    const int64_t S = ch_group_size(R), Gmax = ch_groups(R - 1, S);
+    auto kern = trans ? trsm_chain_kernel<true> : trsm_chain_kernel<false>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kIvSmem) != cudaSuccess)
+        return -1;
+    if (cudaMemsetAsync(ws, 0, sizeof(int), st) != cudaSuccess) return -1;
+    // algorithmic work: n^2 m flops
+    LaunchScope ls(K_MIXED_TRSM, st, (double)n * n * m);
+    const int64_t items = ch_items(R, S, nchunks);
+    unsigned long long *yw = stage, *pw = stage + R * kIvNb * m;
+    kern<<<(unsigned)items, 256, kIvSmem, st>>>(L, ld, W, n, B, ldb, m, nchunks, yw, R * kIvNb, pw, S, Gmax, epoch,
+                                               ws, err_word, state);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

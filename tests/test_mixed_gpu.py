@@ -315,3 +315,26 @@ def test_lowp_factor_leaves_upper_triangle(gpu_lla, n):
     assert np.array_equal(np.triu(out, 1), np.triu(junk, 1))
     L = np.tril(out.astype(np.float64))
     assert np.linalg.norm(L @ L.T - a) / np.linalg.norm(a) <= 4e-6
+
+
+@pytest.mark.parametrize("n,m", [(100, 3), (191, 5), (777, 20), (2111, 37), (4160, 64), (8193, 17)])
+def test_chain_substitution_matches_lookback(gpu_lla, n, m):
+    """The chain form of the FP32 substitutions against the look-back form on
+    the same factor: the first solve's backward error (set by the
+    substitutions' accuracy) agrees within a factor of two, both converge to
+    the FP64 target without fallback, with the same iteration count +-1.
+    Sizes cover one to three block rows (no helper work), ragged last blocks,
+    several column chunks and positions with several helper groups."""
+    lla = gpu_lla
+    rng = np.random.default_rng(n + m)
+    a = qdq(rng, n, 1e5)
+    b = rng.standard_normal((n, m))
+    reps = {}
+    for form in ("lookback", "chain"):
+        x = b.copy()
+        reps[form] = lla.posv_refined(a, x, residual="slices", substitution=form)
+        assert reps[form]["converged"] == 1 and reps[form]["fell_back"] == 0, (form, reps[form])
+        assert backward_error(a, x, b) <= 2e-13, form
+    e0c, e0l = reps["chain"]["backward_error0"], reps["lookback"]["backward_error0"]
+    assert 0.5 * e0l <= e0c <= 2.0 * e0l, (e0c, e0l)
+    assert abs(reps["chain"]["iterations"] - reps["lookback"]["iterations"]) <= 1

@@ -78,3 +78,66 @@ def test_ticket_order_has_no_forward_waits():
     subprocess.run(["g++", "-std=c++17", "-O2", "-I", CSRC, src, "-o", exe], check=True, timeout=120)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.startswith("ok"), r.stdout + r.stderr
+
+
+CHAIN_HARNESS = r"""
+#include <cstdio>
+#include <set>
+#include <tuple>
+#include "lla_trsm_sched.h"
+using namespace lla;
+int main() {
+    const int64_t Rs[] = {1, 2, 3, 4, 5, 34, 35, 36, 67, 100, 256, 257, 1024, 4096};
+    const int nchs[] = {1, 2, 4, 7};
+    long long checked = 0;
+    for (int64_t R : Rs)
+        for (int nch : nchs) {
+            const int64_t S = ch_group_size(R), total = ch_items(R, S, nch);
+            if (R > 1 && ch_groups(R - 1, S) > 8) { std::printf("too many groups R=%lld\n", (long long)R); return 1; }
+            std::set<std::tuple<int64_t, int, int>> seen;
+            int64_t last_pos = -1;
+            for (int64_t t = 0; t < total; ++t) {
+                bool chain; int64_t pos; int g, c;
+                ch_decode(t, R, S, nch, chain, pos, g, c);
+                if (chain != (t < nch)) { std::printf("chain tickets R=%lld t=%lld\n", (long long)R, (long long)t); return 1; }
+                if (chain) { if (c != t) return 1; continue; }
+                if (pos < 0 || pos >= R || c < 0 || c >= nch || g < 0 || g >= ch_groups(pos, S)) {
+                    std::printf("bad helper R=%lld t=%lld\n", (long long)R, (long long)t); return 1;
+                }
+                // helpers by position: a helper's ticket precedes every helper of a later position
+                if (pos < last_pos) { std::printf("order R=%lld\n", (long long)R); return 1; }
+                last_pos = pos;
+                if (!seen.insert(std::make_tuple(pos, g, c)).second) { std::printf("duplicate\n"); return 1; }
+                ++checked;
+            }
+            // every position has its groups, and the groups cover positions 0 .. p-3 once
+            for (int64_t p = 0; p < R; ++p) {
+                int64_t covered = 0;
+                for (int64_t g = 0; g < ch_groups(p, S); ++g) {
+                    for (int c = 0; c < nch; ++c)
+                        if (!seen.count(std::make_tuple(p, (int)g, c))) { std::printf("missing\n"); return 1; }
+                    const int64_t lo = g * S, hi = (lo + S < p - 2) ? lo + S : p - 2;
+                    covered += hi > lo ? hi - lo : 0;
+                }
+                if (covered != (p > 2 ? p - 2 : 0)) { std::printf("cover R=%lld p=%lld\n", (long long)R, (long long)p); return 1; }
+            }
+        }
+    std::printf("ok %lld\n", checked);
+    return 0;
+}
+"""
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_chain_schedule_covers_every_term_once():
+    """Chain form: the chains take the first tickets, helpers follow by position
+    (so the chain at position p waits only on helpers scheduled before any
+    helper of a later position), and the groups of a position cover its
+    coupling terms 0 .. p-3 exactly once, in at most eight groups."""
+    d = tempfile.mkdtemp(prefix="lla_chain_")
+    src, exe = os.path.join(d, "chain.cpp"), os.path.join(d, "chain")
+    with open(src, "w") as f:
+        f.write(CHAIN_HARNESS)
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", CSRC, src, "-o", exe], check=True, timeout=120)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.startswith("ok"), r.stdout + r.stderr
