@@ -368,6 +368,8 @@ def main():
     ap.add_argument("--update", default="bf16x6",
                     help="trailing-update form of the mixed path: fp32|bf16|bf16x3|bf16x6|fp16|fp16x3")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed steps of the plain FP64 leg")
+    ap.add_argument("--substitution", default="auto", choices=["auto", "chain", "lookback"],
+                    help="form of the refinement's FP32 substitutions")
     ap.add_argument("--residual", default="slices", choices=["fp64", "slices"],
                     help="refinement residual of the headline: FP64 MMA pipe, or exact BF16 slices")
     ap.add_argument("--no-alt", action="store_true", help="skip timing the other residual method")
@@ -445,7 +447,7 @@ def main():
 
     def mixed_step(residual=args.residual):
         reports.append(lla.posv_refined_device(A0c, B0c, Xm, stream=stream, update=args.update,
-                                               residual=residual))
+                                               residual=residual, substitution=args.substitution))
 
     # correctness gates (outside the timed regions)
     plain_step()
@@ -537,7 +539,8 @@ def main():
         for it in range(k_e2e + 1):
             Bh.copy_(B0_cpu)
             t0 = time.perf_counter()
-            lla.posv_refined(Ah.numpy(), Bh.numpy(), update=args.update, residual=args.residual)
+            lla.posv_refined(Ah.numpy(), Bh.numpy(), update=args.update, residual=args.residual,
+                             substitution=args.substitution)
             dt = time.perf_counter() - t0
             if it > 0:
                 tot += dt

@@ -305,8 +305,9 @@ typedef struct lla_refine_opts {
     double tol;          /* target normwise backward error (default 1e-13) */
     int32_t equilibrate; /* 1: symmetric power-of-two scaling (default) */
     int32_t fallback;    /* 1: plain FP64 on breakdown or stall (default); 0: LLA_ERR_NOT_CONVERGED */
-    int32_t update_epilogue; /* tensor-core update epilogue: 0 FP32 tile staged by TMA (default, when
-                                the leading dimension allows), 1 register loads and stores */
+    int32_t update_epilogue; /* tensor-core update epilogue: 1 register loads and stores, 2 FP32 tile
+                                staged through shared memory by TMA (16-byte rows of the matrix
+                                needed); 0 default: TMA for the one- and two-term forms */
     int32_t residual;    /* lla_residual (default LLA_RESIDUAL_FP64) */
     int32_t substitution;    /* lla_substitution: form of the FP32 substitutions (0: default) */
     int32_t update_kchunk;   /* K-chunk of the tensor-core update's operand stages: 64 or 32 (0: default) */

@@ -393,8 +393,12 @@ int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, i
                      int64_t ldp, int64_t rows, int kext, int terms, bool fp16, const TcPairs &pairs,
                      const int64_t *info, int *err_word, bool narrow, cudaStream_t st, int kchunk,
                      int epilogue) {
-    // the TMA-staged epilogue (default) needs 16-byte rows of C and 32-wide K-chunks
-    const bool epi_tma = epilogue != 1 && ld % 4 == 0 && (reinterpret_cast<uintptr_t>(C) & 15) == 0 &&
+    // The TMA-staged epilogue needs 16-byte rows of C (and 32-wide K-chunks).  By
+    // default it serves the one- and two-term forms (fp16x3 at n = 16384: 7.8 vs
+    // 8.8 ms a solve); the six-product form keeps the register epilogue, which
+    // measured slightly faster with its 64-wide K-chunks (8.9 vs 9.1 ms).
+    const bool want_tma = epilogue == 2 || (epilogue == 0 && terms <= 2);
+    const bool epi_tma = want_tma && ld % 4 == 0 && (reinterpret_cast<uintptr_t>(C) & 15) == 0 &&
                          ld * 4 < (1ll << 40) && n < (1ll << 31);
     const int kc = (epi_tma || kchunk == 32) ? 32 : 64;
     if (!g_encode || rows <= 0 || kext % kc != 0 || kext > ldp || (ldp * 2) % 16 != 0 || terms < 1 ||

@@ -277,11 +277,11 @@ def test_headline_size_n16384_kappa_1e6(gpu_lla):
 
 
 @pytest.mark.parametrize("update", ["bf16x6", "bf16x3", "fp16x3"])
-@pytest.mark.parametrize("kchunk,epilogue", [(64, 1), (32, 1), (32, 0)])
+@pytest.mark.parametrize("kchunk,epilogue", [(64, 1), (32, 1), (32, 2)])
 def test_update_kchunk_forms(gpu_lla, update, kchunk, epilogue):
     """The tensor-core update with 64-wide K-chunks (128-byte swizzle) and with
     32-wide K-chunks (64-byte swizzle, twice the stages), with the register
-    epilogue (1) and the TMA-staged one (0): all converge to the FP64 target."""
+    epilogue (1) and the TMA-staged one (2): all converge to the FP64 target."""
     lla = gpu_lla
     rng = np.random.default_rng(3 + kchunk + epilogue)
     n = 1537
@@ -308,7 +308,7 @@ def test_lowp_factor_leaves_upper_triangle(gpu_lla, n):
     junk = rng.standard_normal((n, n)).astype(np.float32)
     a_in = np.tril(a) + np.triu(junk, 1)
     A = torch.tensor(a_in, device="cuda").T.contiguous().T
-    info = lla.spotrf_mixed_device(A, update="bf16x6")
+    info = lla.spotrf_mixed_device(A, update="fp16x3")  # a two-term form: TMA-staged when n % 4 == 0
     torch.cuda.synchronize()
     assert int(info.item()) == -1
     out = A.cpu().numpy()
