@@ -252,16 +252,15 @@ __global__ void __launch_bounds__(256, 2) batch_posv_kernel(const BatchItem *__r
 // One CTA per system, as above: the lower triangle of A (FP64, read only) is
 // copied to FP32 scratch and factored there; x = 0, r = b; each iteration
 // solves L L^T d = fp32(r) in FP32, adds d to x in FP64 and forms
-// r = b - A x in FP64 from the lower triangle of A (row sums for k <= i by
-// one thread per row, the mirrored part k > i by one warp per column, both
-// coalesced).  It stops when the normwise backward error
-// max_j ||r_j|| / (||A|| ||x_j|| + ||b_j||) reaches kBRefTol, or stops
-// improving.  A system whose FP32 factorisation breaks down, or that ends
+// r = b - A x in FP64 from the lower triangle of A (one thread per row,
+// sym_residual).  It stops when the normwise backward error
+// max_j ||r_j|| / (||A|| ||x_j|| + ||b_j||) reaches n eps / 16, or once a
+// correction no longer halves it.  A system whose FP32 factorisation breaks down, or that ends
 // above 10 n eps, is solved again by the plain FP64 routine (whose verdict
 // stands) from a working copy of A.  FP64 arithmetic is the scarce resource
 // on this GPU: the factorisation (n^3/3) moves to the FP32 pipe and only
 // 2 n^2 m per iteration stays in FP64.
-constexpr int kBRefIters = 6;
+constexpr int kBRefIters = 5;
 // Stop at n eps / 16 (about what the plain FP64 batched solve reaches); a
 // system left above 10 n eps is re-solved in plain FP64.
 constexpr double kBRefTolPerN = 2.220446049250313e-16 / 16.0;
@@ -298,64 +297,56 @@ __device__ __forceinline__ void block_max_cols(double (&vx)[kBMaxRhs], double (&
     }
 }
 
-// out[i + j n] (+)= sign * sum_k A_sym(i, k) X[k][j] for the lower triangle of A
-// (ld n); X in shared memory, sX[k * kBMaxRhs + j].  mode 0: out = B - A X;
-// mode 1: out = sum_k |A_sym(i, k)| (row sums, m = 1, X unused).
-__device__ void sym_rows(const double *A, int n, const double *sX, int m, const double *B, double *out,
-                         bool rowsum) {
-    const int tid = threadIdx.x, nthr = blockDim.x, warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
-    // k <= i: one thread per row, consecutive rows read consecutive addresses
-    for (int i = tid; i < n; i += nthr) {
-        double acc[kBMaxRhs];
+// r = B - A_sym X for the lower triangle of A (ld n), X in shared memory
+// (sX[k * kBMaxRhs + j]), one thread per row: the part k <= i along row i
+// (consecutive rows read consecutive addresses), the part k > i down column
+// i (each thread streams its own column through L1).  M right-hand sides at
+// compile time, so the scarce FP64 pipe spends no issue slot on absent
+// columns and no lane waits on a shuffle reduction.
+template <int M>
+__device__ void sym_residual_m(const double *A, int n, const double *sX, const double *B, double *out) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double acc[M];
 #pragma unroll
-        for (int j = 0; j < kBMaxRhs; ++j) acc[j] = 0.0;
+        for (int j = 0; j < M; ++j) acc[j] = 0.0;
         for (int k = 0; k <= i; ++k) {
             const double a = A[i + (int64_t)k * n];
-            if (rowsum) {
-                acc[0] += fabs(a);
-            } else {
 #pragma unroll
-                for (int j = 0; j < kBMaxRhs; ++j)
-                    if (j < m) acc[j] = fma(a, sX[k * kBMaxRhs + j], acc[j]);
-            }
+            for (int j = 0; j < M; ++j) acc[j] = fma(a, sX[k * kBMaxRhs + j], acc[j]);
         }
-        if (rowsum) {
-            out[i] = acc[0];
-        } else {
+        const double *col = A + (int64_t)i * n;
+        for (int k = i + 1; k < n; ++k) {
+            const double a = col[k];
 #pragma unroll
-            for (int j = 0; j < kBMaxRhs; ++j)
-                if (j < m) out[i + (int64_t)j * n] = B[i + (int64_t)j * n] - acc[j];
+            for (int j = 0; j < M; ++j) acc[j] = fma(a, sX[k * kBMaxRhs + j], acc[j]);
         }
+#pragma unroll
+        for (int j = 0; j < M; ++j) out[i + (int64_t)j * n] = B[i + (int64_t)j * n] - acc[j];
     }
     __syncthreads();
-    // k > i: A(k, i) is column i of the lower triangle; one warp per column
-    for (int i = warp; i < n; i += nwarps) {
-        double acc[kBMaxRhs];
-#pragma unroll
-        for (int j = 0; j < kBMaxRhs; ++j) acc[j] = 0.0;
-        for (int k = i + 1 + lane; k < n; k += 32) {
-            const double a = A[k + (int64_t)i * n];
-            if (rowsum) {
-                acc[0] += fabs(a);
-            } else {
-#pragma unroll
-                for (int j = 0; j < kBMaxRhs; ++j)
-                    if (j < m) acc[j] = fma(a, sX[k * kBMaxRhs + j], acc[j]);
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < kBMaxRhs; ++j)
-#pragma unroll
-            for (int o = 16; o; o >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
-        if (lane == 0) {
-            if (rowsum) {
-                out[i] += acc[0];
-            } else {
-#pragma unroll
-                for (int j = 0; j < kBMaxRhs; ++j)
-                    if (j < m) out[i + (int64_t)j * n] -= acc[j];
-            }
-        }
+}
+
+__device__ void sym_residual(const double *A, int n, const double *sX, int m, const double *B, double *out) {
+    switch (m) {
+        case 1: sym_residual_m<1>(A, n, sX, B, out); break;
+        case 2: sym_residual_m<2>(A, n, sX, B, out); break;
+        case 3: sym_residual_m<3>(A, n, sX, B, out); break;
+        case 4: sym_residual_m<4>(A, n, sX, B, out); break;
+        case 5: sym_residual_m<5>(A, n, sX, B, out); break;
+        case 6: sym_residual_m<6>(A, n, sX, B, out); break;
+        case 7: sym_residual_m<7>(A, n, sX, B, out); break;
+        default: sym_residual_m<8>(A, n, sX, B, out); break;
+    }
+}
+
+// out[i] = sum_k |A_sym(i, k)| (the same traversal).
+__device__ void sym_rowsum(const double *A, int n, double *out) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double s = 0.0;
+        for (int k = 0; k <= i; ++k) s += fabs(A[i + (int64_t)k * n]);
+        const double *col = A + (int64_t)i * n;
+        for (int k = i + 1; k < n; ++k) s += fabs(col[k]);
+        out[i] = s;
     }
     __syncthreads();
 }
@@ -390,7 +381,7 @@ __global__ void __launch_bounds__(256, 2) batch_posv_refined_kernel(const BatchI
             if (i >= k) W[e] = (float)A[e];
         }
         // ||A||_inf and ||b_j||_inf
-        sym_rows(A, n, nullptr, 1, nullptr, R, true);
+        sym_rowsum(A, n, R);
         double an = 0.0;
         {
             double vb[kBMaxRhs], va[kBMaxRhs];
@@ -426,7 +417,7 @@ __global__ void __launch_bounds__(256, 2) batch_posv_refined_kernel(const BatchI
                     sX[i * kBMaxRhs + j] += (double)R32[e];
                 }
                 __syncthreads();
-                sym_rows(A, n, sX, m, B, R, false);
+                sym_residual(A, n, sX, m, B, R);
                 double vx[kBMaxRhs], vr[kBMaxRhs];
 #pragma unroll
                 for (int j = 0; j < kBMaxRhs; ++j) vx[j] = vr[j] = 0.0;
@@ -449,7 +440,8 @@ __global__ void __launch_bounds__(256, 2) batch_posv_refined_kernel(const BatchI
                     e_max = fmax(e_max, ej);
                 }
                 eta = e_max;  // uniform across the CTA
-                if (eta <= tol || !(eta < INFINITY) || (itr >= 2 && eta > 0.5 * eta_prev)) break;
+                // done at the target, or once a correction no longer halves the error
+                if (eta <= tol || !(eta < INFINITY) || (itr >= 1 && eta > 0.5 * eta_prev)) break;
                 eta_prev = eta;
             }
             ok = eta <= 10.0 * n * 2.220446049250313e-16;
