@@ -449,6 +449,13 @@ def main():
         reports.append(lla.posv_refined_device(A0c, B0c, Xm, stream=stream, update=args.update,
                                                residual=residual, substitution=args.substitution))
 
+    # the refined solve's schedule for this shape, from the per-shape autotuner (recorded in the
+    # autotune cache; the timed solves below take it up with their default options)
+    schedule = None
+    if args.substitution == "auto":
+        chosen, tune_ms = lla.refine_autotune(A0c, B0c, Xm, stream=stream, update=args.update,
+                                              residual=args.residual)
+        schedule = dict(chosen, autotune_best_ms=tune_ms)
     # correctness gates (outside the timed regions)
     plain_step()
     torch.cuda.synchronize()
@@ -575,6 +582,7 @@ def main():
                        "path": f"mixed: equilibrated low-precision Cholesky ({args.update} trailing "
                                f"updates) + FP64 refinement ({args.residual} residual), FP64 fallback",
                        "l2": "inputs larger than L2 (A = %.2f GB)" % (n * n * 8 / 1e9),
+                       "refine_schedule": schedule,
                        "parallelism": "replicas" if world > 1 else "single"},
             "backward_error": max(r["backward_error"] for r in timed_reports),
             "latency": latency,

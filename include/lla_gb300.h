@@ -320,7 +320,7 @@ typedef struct lla_refine_report {
     int32_t converged;       /* 1 when the refinement reached tol */
     int32_t fell_back;       /* 1 when the plain FP64 path produced X */
     int32_t factor_failed;   /* 1 when the low-precision factorisation broke down */
-    int32_t reserved;
+    int32_t schedule;        /* schedule used: update K-chunk << 8 | update epilogue << 4 | substitution */
     double backward_error;   /* final normwise backward error (max over columns) */
     double backward_error0;  /* after the first low-precision solve */
     double ms_factor, ms_refine, ms_fallback, ms_total;
@@ -334,6 +334,21 @@ void lla_refine_opts_default(lla_refine_opts *opts);
 int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda, const double *dB, int64_t m,
                              int64_t ldb, double *dX, int64_t ldx, const lla_refine_opts *opts,
                              lla_refine_report *report, void *stream, lla_error *err);
+
+/* Per-shape autotuner of the refined solve's schedule (no counterpart in the
+ * reference): times lla_dposv_refined_device on this system for each candidate
+ * of the tensor-core update's epilogue and K-chunk (registers / 64, registers /
+ * 32, TMA-staged / 32) and of the substitution form (look-back, chain), keeps
+ * the fastest that converges without fallback, records it in the autotune
+ * cache (LLA_AUTOTUNE_CACHE, default ~/.cache/lla_gb300_autotune.txt) under the
+ * shape key (n and m rounded up to powers of two, update form, residual) and
+ * writes it into *opts.  Later solves whose opts leave update_kchunk,
+ * update_epilogue and substitution at 0 take the cached schedule for their
+ * shape (lla_refine_report.schedule says which ran).  dX receives X; errors as
+ * lla_dposv_refined_device. */
+int lla_refine_autotune(const double *dA, int64_t n, int64_t lda, const double *dB, int64_t m, int64_t ldb,
+                        double *dX, int64_t ldx, lla_refine_opts *opts, double *best_ms, void *stream,
+                        lla_error *err);
 
 /* R = B - A_sym X (A_sym: the symmetric matrix defined by the lower triangle
  * of dA), column-major device arrays, by the given lla_residual method;
@@ -434,7 +449,7 @@ typedef struct lla_serve_opts {
     int32_t slots;           /* concurrent large-request streams (default 6) */
     int32_t small_n;         /* largest order sent to the device-resident loop (default 256) */
     int32_t batch_max;       /* most small requests in flight in the loop's ring (default and limit 1024) */
-    int32_t device_ctas;     /* persistent CTAs of the device loop (0: half the SMs) */
+    int32_t device_ctas;     /* persistent CTAs of the device loop (0: an eighth of the SMs, at least 8) */
     double batch_window_us;  /* idle time after which the loop's CTAs return (default 2000) */
 } lla_serve_opts;
 

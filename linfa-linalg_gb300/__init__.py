@@ -73,7 +73,7 @@ class RefineOpts(ctypes.Structure):
 class RefineReport(ctypes.Structure):
     _fields_ = [("update", ctypes.c_int32), ("iterations", ctypes.c_int32),
                 ("converged", ctypes.c_int32), ("fell_back", ctypes.c_int32),
-                ("factor_failed", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("factor_failed", ctypes.c_int32), ("schedule", ctypes.c_int32),
                 ("backward_error", ctypes.c_double), ("backward_error0", ctypes.c_double),
                 ("ms_factor", ctypes.c_double), ("ms_refine", ctypes.c_double),
                 ("ms_fallback", ctypes.c_double), ("ms_total", ctypes.c_double)]
@@ -112,6 +112,9 @@ EXPORTS = {
                           ctypes.c_int),
     "lla_spotrf_mixed_device": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
                                  ctypes.c_void_p, ctypes.c_void_p, _E], ctypes.c_int),
+    "lla_refine_autotune": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                             ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(RefineOpts),
+                             ctypes.POINTER(ctypes.c_double), ctypes.c_void_p, _E], ctypes.c_int),
     "lla_dresidual_device": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
                               ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                               ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, _E],
@@ -583,6 +586,22 @@ def posv_refined_device(A, B, X, stream=None, **kw):
                                  ctypes.byref(e))
     _raise(e)
     return r.as_dict()
+
+
+def refine_autotune(A, B, X, stream=None, **kw):
+    """Per-shape autotuner of the refined solve's schedule (lla_refine_autotune):
+    times the candidates on this system (column-major CUDA tensors as in
+    posv_refined_device), records the winner in the autotune cache and returns
+    ({"update_kchunk", "update_epilogue", "substitution"}, best_ms)."""
+    n, m = A.shape[0], B.shape[1]
+    assert A.stride(0) == 1 and B.stride(0) == 1 and X.stride(0) == 1
+    o, e, ms = refine_opts(**kw), Error(), ctypes.c_double(0.0)
+    lib.lla_refine_autotune(ctypes.c_void_p(A.data_ptr()), n, _ld(A), ctypes.c_void_p(B.data_ptr()), m, _ld(B),
+                            ctypes.c_void_p(X.data_ptr()), _ld(X), ctypes.byref(o), ctypes.byref(ms),
+                            _stream_ptr(stream), ctypes.byref(e))
+    _raise(e)
+    return ({"update_kchunk": o.update_kchunk, "update_epilogue": o.update_epilogue,
+             "substitution": o.substitution}, ms.value)
 
 
 def spotrf_mixed_device(A, update="bf16x6", info=None, stream=None):

@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "../../include/lla_gb300.h"
+#include "lla_autotune.h"
 #include "lla_common.cuh"
 #include "lla_kernels.h"
 #include "lla_prof.h"
@@ -621,46 +622,8 @@ struct lla_batch_plan {
 
 static size_t batch_smem(int dtype) { return (size_t)dtype * (32 * 33 + (size_t)kBMaxN * 33); }
 
-static std::string cache_path() {
-    const char *p = std::getenv("LLA_AUTOTUNE_CACHE");
-    if (p && *p) return p;
-    const char *h = std::getenv("HOME");
-    return std::string(h ? h : "/tmp") + "/.cache/lla_gb300_autotune.txt";
-}
-
-static std::mutex g_cache_mu;
-
-static bool cache_lookup(const std::string &key, int &cps, int &thr) {
-    std::lock_guard<std::mutex> lk(g_cache_mu);
-    FILE *f = std::fopen(cache_path().c_str(), "r");
-    if (!f) return false;
-    char k[512];
-    int a, b;
-    bool found = false;
-    while (std::fscanf(f, "%511s %d %d", k, &a, &b) == 3)
-        if (key == k) {
-            cps = a;
-            thr = b;
-            found = true;
-        }
-    std::fclose(f);
-    return found;
-}
-
-static void cache_store(const std::string &key, int cps, int thr) {
-    std::lock_guard<std::mutex> lk(g_cache_mu);
-    const std::string path = cache_path();
-    const size_t slash = path.rfind('/');
-    if (slash != std::string::npos) {
-        const std::string dir = path.substr(0, slash);
-        for (size_t i = 1; i <= dir.size(); ++i)
-            if (i == dir.size() || dir[i] == '/') (void)mkdir(dir.substr(0, i).c_str(), 0755);
-    }
-    FILE *f = std::fopen(path.c_str(), "a");
-    if (!f) return;
-    std::fprintf(f, "%s %d %d\n", key.c_str(), cps, thr);
-    std::fclose(f);
-}
+static bool cache_lookup(const std::string &key, int &cps, int &thr) { return lla::autotune_lookup(key, cps, thr); }
+static void cache_store(const std::string &key, int cps, int thr) { lla::autotune_store(key, cps, thr); }
 
 static int sm_count() {
     static int sms = 0;

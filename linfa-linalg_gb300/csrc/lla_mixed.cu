@@ -20,9 +20,11 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "lla_api_internal.h"
+#include "lla_autotune.h"
 #include "lla_common.cuh"
 #include "lla_kernels.h"
 #include "lla_mixed.h"
@@ -535,6 +537,18 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 
 }  // namespace
 
+// Autotune-cache key of the refined solve's schedule for a shape.
+static std::string refine_key(int64_t n, int64_t m, const lla_refine_opts &o) {
+    auto lg = [](int64_t v) {
+        int e = 0;
+        while ((int64_t(1) << e) < v) ++e;
+        return e;
+    };
+    char k[96];
+    std::snprintf(k, sizeof(k), "r:n%d:m%d:u%d:s%d", lg(n), lg(m), (int)o.update, (int)o.residual);
+    return k;
+}
+
 // Smallest pivot_k / a_kk that the FMA-order fallback factorisation accepts
 // without the exact-order re-run (the host-view entry points use the same guard).
 constexpr double kFallbackPivotGuard = 1e-10;
@@ -575,9 +589,18 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
         lla_refine_opts_default(&opts);
     if (opts.max_iters <= 0) opts.max_iters = 30;
     if (!(opts.tol > 0)) opts.tol = 1e-13;
+    if (opts.update_kchunk == 0 && opts.update_epilogue == 0 && opts.substitution == 0) {
+        int a, b;  // the schedule the autotuner recorded for this shape, if any
+        if (autotune_lookup(refine_key(n, m, opts), a, b)) {
+            opts.update_kchunk = a >> 4;
+            opts.update_epilogue = a & 15;
+            opts.substitution = b;
+        }
+    }
     lla_refine_report r;
     std::memset(&r, 0, sizeof(r));
     r.update = opts.update;
+    r.schedule = (opts.update_kchunk << 8) | (opts.update_epilogue << 4) | opts.substitution;
     lla__set_status(err, LLA_OK);
     if (n == 0 || m == 0) {
         r.converged = 1;
@@ -797,6 +820,67 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
     }
     r.ms_total = ms_since(t_start);
     if (rep) *rep = r;
+    return LLA_OK;
+}
+
+extern "C" int lla_refine_autotune(const double *dA, int64_t n, int64_t lda, const double *dB, int64_t m,
+                                   int64_t ldb, double *dX, int64_t ldx, lla_refine_opts *opts, double *best_ms,
+                                   void *stream, lla_error *err) {
+    if (!opts) return lla__set_status(err, LLA_ERR_INVALID_ARG);
+    lla__set_status(err, LLA_OK);
+    const lla_refine_opts base = *opts;
+    struct Cand {
+        int kc, epi, sub;
+    };
+    const Cand cands[] = {{64, 1, LLA_SUB_LOOKBACK}, {32, 1, LLA_SUB_LOOKBACK}, {32, 2, LLA_SUB_LOOKBACK},
+                          {64, 1, LLA_SUB_CHAIN},    {32, 2, LLA_SUB_CHAIN}};
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t ce = cudaEventCreate(&e0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        return lla__set_cuda_error(err, ce);
+    }
+    float best = 1e30f;
+    Cand win = cands[0];
+    int rc = LLA_OK;
+    for (const Cand &c : cands) {
+        lla_refine_opts o = base;
+        o.update_kchunk = c.kc;
+        o.update_epilogue = c.epi;
+        o.substitution = c.sub;
+        float tmin = 1e30f;
+        bool ok = true;
+        for (int rep = 0; rep < 2 && rc == LLA_OK; ++rep) {
+            lla_refine_report r;
+            if ((ce = cudaEventRecord(e0, st)) != cudaSuccess) break;
+            rc = lla_dposv_refined_device(dA, n, lda, dB, m, ldb, dX, ldx, &o, &r, stream, err);
+            if (rc != LLA_OK) break;
+            float ms = 0.f;
+            if ((ce = cudaEventRecord(e1, st)) != cudaSuccess || (ce = cudaEventSynchronize(e1)) != cudaSuccess ||
+                (ce = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess)
+                break;
+            ok = ok && r.converged && !r.fell_back;
+            tmin = ms < tmin ? ms : tmin;
+        }
+        if (rc != LLA_OK || ce != cudaSuccess) break;
+        if (ok && tmin < best) {
+            best = tmin;
+            win = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != LLA_OK) return rc;
+    if (ce != cudaSuccess) return lla__set_cuda_error(err, ce);
+    if (best < 1e30f) {
+        autotune_store(refine_key(n, m, base), (win.kc << 4) | win.epi, win.sub);
+        opts->update_kchunk = win.kc;
+        opts->update_epilogue = win.epi;
+        opts->substitution = win.sub;
+        if (best_ms) *best_ms = best;
+    }
     return LLA_OK;
 }
 

@@ -412,10 +412,12 @@ int lla_server_create(const lla_serve_opts *opts, lla_server **out, lla_error *e
     s->t0 = Clock::now();
     int dev = 0;
     cudaGetDevice(&dev);
-    if (s->opts.device_ctas <= 0) {  // default: one CTA on every other SM
+    if (s->opts.device_ctas <= 0) {  // default: one CTA on every eighth SM (19 on 152 SMs)
+        // Small requests take 50-300 us each on one CTA, so 19 CTAs serve tens of
+        // thousands a second; a larger loop holds SMs the large requests need.
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        s->opts.device_ctas = std::max(1, sms / 2);
+        s->opts.device_ctas = std::max(8, sms / 8);
     }
     auto bind = [dev](void (*fn)(lla_server *), lla_server *srv) {
         return std::thread([dev, fn, srv] {

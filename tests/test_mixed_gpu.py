@@ -338,3 +338,27 @@ def test_chain_substitution_matches_lookback(gpu_lla, n, m):
     e0c, e0l = reps["chain"]["backward_error0"], reps["lookback"]["backward_error0"]
     assert 0.5 * e0l <= e0c <= 2.0 * e0l, (e0c, e0l)
     assert abs(reps["chain"]["iterations"] - reps["lookback"]["iterations"]) <= 1
+
+
+def test_refine_autotune_records_and_reuses(gpu_lla, tmp_path, monkeypatch):
+    """The per-shape autotuner times the refined solve's schedule candidates on
+    the caller's system, records the winner under the shape key, and a later
+    solve with default options runs that schedule (the report says which)."""
+    torch = pytest.importorskip("torch")
+    lla = gpu_lla
+    monkeypatch.setenv("LLA_AUTOTUNE_CACHE", str(tmp_path / "tune.txt"))
+    rng = np.random.default_rng(77)
+    n, m = 1537, 9
+    a = qdq(rng, n, 1e5)
+    b = rng.standard_normal((n, m))
+    A = torch.tensor(a, device="cuda").T.contiguous().T
+    B = torch.tensor(b, device="cuda").T.contiguous().T
+    X = torch.empty_like(B.T.contiguous()).T
+    chosen, ms = lla.refine_autotune(A, B, X, residual="slices")
+    assert ms > 0 and chosen["update_kchunk"] in (32, 64) and chosen["update_epilogue"] in (1, 2)
+    assert chosen["substitution"] in (1, 2)
+    assert "r:n11:m4:u6:s1" in (tmp_path / "tune.txt").read_text()
+    rep = lla.posv_refined_device(A, B, X, residual="slices")
+    want = (chosen["update_kchunk"] << 8) | (chosen["update_epilogue"] << 4) | chosen["substitution"]
+    assert rep["schedule"] == want and rep["converged"] == 1
+    assert backward_error(a, X.cpu().numpy(), b) <= 2e-13
