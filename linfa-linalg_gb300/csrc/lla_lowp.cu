@@ -386,10 +386,11 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
     const int64_t plane_stride = n * ldp;  // elements per plane
     if (c->mixed.opA.ensure(sizeof(uint16_t) * plane_stride * terms) != cudaSuccess) return -1;
     void *planes = c->mixed.opA.p;
-    int *err_word = nullptr;
-    if (c->mixed.tcerr.ensure(sizeof(int)) != cudaSuccess) return -1;
-    err_word = (int *)c->mixed.tcerr.p;
-    if (cudaMemsetAsync(err_word, 0, sizeof(int), st) != cudaSuccess) return -1;
+    // status word, then the update's two tile-scheduling words (zero between launches)
+    if (c->mixed.tcerr.ensure(4 * sizeof(int)) != cudaSuccess) return -1;
+    int *err_word = (int *)c->mixed.tcerr.p;
+    unsigned *sched = (unsigned *)c->mixed.tcerr.p + 1;
+    if (cudaMemsetAsync(err_word, 0, 4 * sizeof(int), st) != cudaSuccess) return -1;
     const size_t smem_l11 = sizeof(float) * (kLpNb * kLpLd + 32 * kLpPd);
     const size_t smem_panel = kPnSmem;
     if (c->mixed.pinv.ensure(sizeof(float) * 4 * 32 * 32) != cudaSuccess) return -1;
@@ -428,7 +429,7 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
                        narrow ? (double)rows * cols * kext * 2.0 - (double)cols * (cols - 1) * kext
                               : (double)rows * (rows + 1) * kext);
         return tc_update_launch(L, ld, q, n, (char *)planes + (size_t)q * ldp * esz, plane_stride, ldp, rows,
-                                kext, terms, fp16, pairs, info, err_word, narrow, st, opts.update_kchunk,
+                                kext, terms, fp16, pairs, info, err_word, sched, narrow, st, opts.update_kchunk,
                                 opts.update_epilogue);
     };
     // Panels in pairs: after panel p only the next panel's 128 columns are

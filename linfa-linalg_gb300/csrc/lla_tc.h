@@ -25,10 +25,12 @@ int tc_update_prepare();
 // planes: `terms` planes of rows x ldp BF16 (or FP16) values, plane_stride
 // elements apart, row-major, 16-byte aligned; kext (a multiple of 64, <= ldp)
 // columns of each row are the K extent.  Skips all work when *info >= 0;
-// bounded waits record LLA_ERR_TIMEOUT in *err_word.
+// bounded waits record LLA_ERR_TIMEOUT in *err_word.  sched: two zeroed words
+// (the next unclaimed tile, the CTAs finished) that CTAs claim tiles from;
+// the last CTA to finish zeroes them again for the next launch on the stream.
 int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, int64_t plane_stride,
                      int64_t ldp, int64_t rows, int kext, int terms, bool fp16, const TcPairs &pairs,
-                     const int64_t *info, int *err_word, bool narrow, cudaStream_t st, int kchunk = 64,
-                     int epilogue = 0);
+                     const int64_t *info, int *err_word, unsigned *sched, bool narrow, cudaStream_t st,
+                     int kchunk = 64, int epilogue = 0);
 
 }  // namespace lla

@@ -1,8 +1,10 @@
 // lla_tc_update.cu -- trailing update A22 -= L21 L21^T of the mixed-precision
 // Cholesky on the 5th-generation tensor cores (tcgen05, sm_103a).
 //
-// Persistent CTAs (one per SM) walk the 128 x 128 lower tiles (I >= J) of the
-// trailing matrix:
+// Persistent CTAs (at most one per SM) claim the 128 x 128 lower tiles
+// (I >= J) of the trailing matrix one at a time from a global counter, so a
+// CTA that starts late -- its SM still busy with another stream's work --
+// takes fewer tiles instead of delaying the launch:
 //   * one thread streams 64-wide K chunks of the two operand row blocks, every
 //     term plane of a chunk in one TMA box (cp.async.bulk.tensor, 128-byte
 //     swizzle), into a shared-memory ring of 2-6 stages, completion tracked by
@@ -88,12 +90,28 @@ __device__ __forceinline__ void tc_tri_tile(int64_t t, int64_t &I, int64_t &J) {
 
 // Persistent, warp-specialised: warps 0-7 drain accumulators (epilogue, two
 // warps per 32-lane quarter of tensor memory, 64 columns each), warp 8 lane 0
-// feeds the shared-memory ring with TMA, warp 9 lane 0 issues the MMAs.  Two
-// tensor-memory accumulators let the epilogue of one tile overlap the MMAs of
-// the next, and the epilogue fetches its FP32 tile before the accumulator is
-// ready.
+// claims tiles and feeds the shared-memory ring with TMA, warp 9 lane 0
+// issues the MMAs.  Two tensor-memory accumulators let the epilogue of one
+// tile overlap the MMAs of the next, and the epilogue fetches its FP32 tile
+// before the accumulator is ready.  The claimed tile indices reach the MMA and
+// epilogue warps through a small shared-memory ring (-1: no tiles left).
 constexpr int kTcThreads = 320;  // 8 epilogue warps, 1 producer warp, 1 MMA warp
 constexpr int kTcEpiThreads = 256;
+constexpr int kTcTileRing = 8;  // claimed tile indices in flight inside a CTA
+
+// The CTA claims no more tiles: the last CTA of the launch to get here zeroes
+// the scheduling words (next tile, CTAs finished) for the next launch.
+__device__ __forceinline__ void tc_sched_done(unsigned *sched) {
+    __threadfence();
+    if (atomicAdd(&sched[1], 1u) == gridDim.x - 1) {
+        atomicExch(&sched[0], 0u);
+        atomicExch(&sched[1], 0u);
+    }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
 
 // Term pairs (a, b) per number of terms, small products first; the last one,
 // (0, 0), is the leading product.
@@ -118,15 +136,20 @@ template <int TERMS, int KC, bool EPI_TMA>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap cmap, float *C, int64_t ld,
     int64_t q, int64_t n, int kchunks, uint32_t idesc, int64_t ntiles, int narrow, const int64_t *info,
-    int *err_word) {
+    int *err_word, unsigned *sched) {
     constexpr int terms = TERMS, NP = tc_npairs(TERMS);
     extern __shared__ uint8_t smem_raw[];
-    __shared__ int s_abort, s_skip, s_epi_abort;
+    __shared__ int s_abort, s_skip, s_epi_abort, s_epi_tile;
+    __shared__ int s_tile[kTcTileRing];
+    __shared__ __align__(8) uint64_t s_tbar[2 * kTcTileRing];  // tile ring: full[R], empty[R]
     // one reader decides for the whole CTA (another CTA may set err_word meanwhile)
     if (threadIdx.x == 0)
         s_skip = (*(volatile const int64_t *)info >= 0 || *(volatile const int *)err_word != 0);
     __syncthreads();
-    if (s_skip) return;
+    if (s_skip) {
+        if (threadIdx.x == 0) tc_sched_done(sched);
+        return;
+    }
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     constexpr int kTile = tc_tile_bytes<KC>();
     const int S = tc_stages<KC>(terms, EPI_TMA);
@@ -140,6 +163,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kTcMaxStages);
     const uint32_t tfull0 = smem_u32(bars + 2 * kTcMaxStages), tempty0 = tfull0 + 16;
     const uint32_t cfull = tfull0 + 32;
+    const uint32_t rfull0 = smem_u32(s_tbar), rempty0 = rfull0 + 8 * kTcTileRing;  // tile ring
     if (tid == 0) {
         for (int s = 0; s < S; ++s) {
             mbar_init(full0 + 8 * s, 1);
@@ -148,6 +172,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
         for (int a = 0; a < 2; ++a) {
             mbar_init(tfull0 + 8 * a, 1);
             mbar_init(tempty0 + 8 * a, kTcEpiThreads);  // every epilogue thread releases
+        }
+        for (int r = 0; r < kTcTileRing; ++r) {
+            mbar_init(rfull0 + 8 * r, 1);
+            // readers of a claimed index: the MMA thread and the epilogue (one
+            // thread for the staged epilogue, each warp's lane 0 otherwise)
+            mbar_init(rempty0 + 8 * r, EPI_TMA ? 2 : 9);
         }
         mbar_init(cfull, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -167,9 +197,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     const uint32_t tmem = *tslot;
 
     if (warp == 8) {
-        if (lane == 0) {  // TMA producer
+        if (lane == 0) {  // tile claims and TMA producer
             int64_t g = 0;
-            for (int64_t t = blockIdx.x; t < ntiles && !*(volatile int *)&s_abort; t += gridDim.x) {
+            for (int64_t lt = 0; !*(volatile int *)&s_abort; ++lt) {
+                const int slot = (int)(lt % kTcTileRing);
+                const int64_t ruse = lt / kTcTileRing;
+                if (ruse > 0 && !mbar_wait(rempty0 + 8 * slot, (uint32_t)((ruse - 1) & 1), err_word)) {
+                    s_abort = 1;
+                    break;
+                }
+                const int64_t t = (int64_t)atomicAdd(&sched[0], 1u);
+                s_tile[slot] = t < ntiles ? (int)t : -1;
+                mbar_arrive(rfull0 + 8 * slot);  // release: the index is visible to the waiters
+                if (t >= ntiles) break;
                 int64_t I, J;
                 tc_tile(t, narrow, I, J);
                 for (int kc = 0; kc < kchunks; ++kc, ++g) {
@@ -188,8 +228,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
         }
     } else if (warp == 9) {
         if (lane == 0) {  // MMA issuer
-            int64_t g = 0, lt = 0;
-            for (int64_t t = blockIdx.x; t < ntiles && !*(volatile int *)&s_abort; t += gridDim.x, ++lt) {
+            int64_t g = 0;
+            for (int64_t lt = 0; !*(volatile int *)&s_abort; ++lt) {
+                const int slot = (int)(lt % kTcTileRing);
+                if (!mbar_wait(rfull0 + 8 * slot, (uint32_t)((lt / kTcTileRing) & 1), err_word)) {
+                    s_abort = 1;
+                    break;
+                }
+                const int t = s_tile[slot];
+                mbar_arrive(rempty0 + 8 * slot);
+                if (t < 0) break;
                 int64_t I, J;
                 tc_tile(t, narrow, I, J);
                 const int a = (int)(lt & 1);
@@ -229,21 +277,39 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
             }
         }
     } else if (EPI_TMA) {  // warps 0-7: epilogue through the shared-memory tile
-        int64_t lt = 0;
         const int qw = warp & 3, half = warp >> 2;
         constexpr bool cross = NP > 1;
         const int r = qw * 32 + lane;
-        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
+        for (int64_t lt = 0;; ++lt) {
             const int a = (int)(lt & 1);
             const int64_t use = lt >> 1;
+            if (tid == 0) {
+                // thread 0 reads the claimed index for the eight warps (-2: gave up waiting)
+                const int slot = (int)(lt % kTcTileRing);
+                int t = -2;
+                if (mbar_wait(rfull0 + 8 * slot, (uint32_t)((lt / kTcTileRing) & 1), err_word)) {
+                    t = s_tile[slot];
+                    mbar_arrive(rempty0 + 8 * slot);
+                }
+                s_epi_tile = t;
+                if (t >= 0) {
+                    int64_t I, J;
+                    tc_tile(t, narrow, I, J);
+                    // the previous tile's store has read the buffer: load this tile into it
+                    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                    mbar_expect_tx(cfull, (uint32_t)kTcTileC);
+                    tma_load_2d(smem_u32(sC), &cmap, (int)(q + I * kTcM), (int)(q + J * kTcN), cfull);
+                }
+            }
+            asm volatile("bar.sync 1, %0;" ::"n"(kTcEpiThreads) : "memory");
+            const int t = *(volatile int *)&s_epi_tile;  // the same for all eight warps
+            if (t == -1) break;
+            if (t < 0) {
+                if (tid == 0) s_abort = 1;
+                break;
+            }
             int64_t I, J;
             tc_tile(t, narrow, I, J);
-            if (tid == 0) {
-                // the previous tile's store has read the buffer: load this tile into it
-                asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-                mbar_expect_tx(cfull, (uint32_t)kTcTileC);
-                tma_load_2d(smem_u32(sC), &cmap, (int)(q + I * kTcM), (int)(q + J * kTcN), cfull);
-            }
             bool okc = mbar_wait(cfull, (uint32_t)(lt & 1), err_word);
             bool ok = mbar_wait(tfull0 + 8 * a, (uint32_t)(use & 1), err_word) && okc;
             ok = __all_sync(0xffffffffu, ok) && !*(volatile int *)&s_abort;
@@ -289,13 +355,26 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
         }
         if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");  // stores complete
     } else {  // warps 0-7: epilogue; warp w drains lane quarter w % 4, columns 64 (w / 4) ..
-        int64_t lt = 0;
         const int qw = warp & 3, half = warp >> 2;
         constexpr bool cross = NP > 1;  // the cross-term accumulator is in use
         const int r = qw * 32 + lane;
-        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
+        for (int64_t lt = 0;; ++lt) {
             const int a = (int)(lt & 1);
             const int64_t use = lt >> 1;
+            int t = -2;  // the claimed index, read by lane 0 (-2: gave up waiting)
+            if (lane == 0) {
+                const int slot = (int)(lt % kTcTileRing);
+                if (mbar_wait(rfull0 + 8 * slot, (uint32_t)((lt / kTcTileRing) & 1), err_word)) {
+                    t = s_tile[slot];
+                    mbar_arrive(rempty0 + 8 * slot);
+                }
+            }
+            t = __shfl_sync(0xffffffffu, t, 0);
+            if (t == -1) break;
+            if (t < 0) {
+                if (lane == 0) s_abort = 1;
+                break;
+            }
             int64_t I, J;
             tc_tile(t, narrow, I, J);
             const int64_t grow = q + I * kTcM + r;
@@ -355,6 +434,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcAlloc)
                      : "memory");
+    if (tid == 0) tc_sched_done(sched);  // this CTA's producer claims no more tiles
 }
 
 // ---------------------------------------------------------------------------
@@ -391,8 +471,8 @@ int tc_update_prepare() {
 
 int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, int64_t plane_stride,
                      int64_t ldp, int64_t rows, int kext, int terms, bool fp16, const TcPairs &pairs,
-                     const int64_t *info, int *err_word, bool narrow, cudaStream_t st, int kchunk,
-                     int epilogue) {
+                     const int64_t *info, int *err_word, unsigned *sched, bool narrow, cudaStream_t st,
+                     int kchunk, int epilogue) {
     // The TMA-staged epilogue needs 16-byte rows of C (and 32-wide K-chunks).  By
     // default it serves the one- and two-term forms (fp16x3 at n = 16384: 7.8 vs
     // 8.8 ms a solve); the six-product form keeps the register epilogue, which
@@ -401,7 +481,7 @@ int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, i
     const bool epi_tma = want_tma && ld % 4 == 0 && (reinterpret_cast<uintptr_t>(C) & 15) == 0 &&
                          ld * 4 < (1ll << 40) && n < (1ll << 31);
     const int kc = (epi_tma || kchunk == 32) ? 32 : 64;
-    if (!g_encode || rows <= 0 || kext % kc != 0 || kext > ldp || (ldp * 2) % 16 != 0 || terms < 1 ||
+    if (!g_encode || !sched || rows <= 0 || kext % kc != 0 || kext > ldp || (ldp * 2) % 16 != 0 || terms < 1 ||
         terms > 3 || (reinterpret_cast<uintptr_t>(planes) & 15) != 0)
         return -1;
     const int64_t tr = (rows + kTcM - 1) / kTcM;
@@ -453,8 +533,7 @@ int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, i
                            : (terms == 1 ? tc_update_kernel<1, 64, false>
                                          : (terms == 2 ? tc_update_kernel<2, 64, false> : tc_update_kernel<3, 64, false>));
     kern<<<grid, kTcThreads, tc_smem_bytes(epi_tma), st>>>(map, cmap, C, ld, q, n, kext / kc, idesc, tiles,
-                                                            narrow ? 1 : 0, info,
-                                            err_word);
+                                                            narrow ? 1 : 0, info, err_word, sched);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
