@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 #include "../../include/lla_gb300.h"
 
 namespace lla {
@@ -45,6 +47,35 @@ __device__ __forceinline__ const T &cm(const T *p, int64_t ld, int64_t i, int64_
 constexpr long long kSpinLimit = 1ll << 24;
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialization may start while its predecessor in the stream still runs;
+// pdl_wait() returns once the predecessor has completed and its writes are
+// visible (at once for a kernel launched without the attribute).  Every
+// kernel of such a chain calls pdl_wait() before its first read of the
+// predecessor's output and before any exit, then pdl_trigger() to let its
+// own successor start: so a kernel may read, before its wait, anything
+// written two or more launches earlier.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Launches `kern` on `st`, allowed to overlap the tail of the stream's
+// previous kernel when `pdl` (the kernel must follow the pdl_wait rules).
+template <typename... Exp, typename... Act>
+inline cudaError_t launch_maybe_pdl(bool pdl, void (*kern)(Exp...), dim3 grid, dim3 block, size_t smem,
+                                    cudaStream_t st, Act &&...args) {
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = pdl ? attr : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Act>(args)...);
+}
 
 }  // namespace lla
 

@@ -3,9 +3,11 @@
 //
 // Right-looking with panels of nb = 128 columns:
 //   diag   : one CTA factors the 128 x 128 diagonal block in FP32 (32-column
-//            sub-blocks: an unpredicated one-warp shuffle Cholesky, a
-//            row-parallel solve of the rows below it, a shared-memory update
-//            of the rest; a short last block is padded with the identity);
+//            sub-blocks: an unpredicated one-warp shuffle Cholesky without
+//            square roots on its pivot chain, a row-parallel solve of the
+//            rows below it, a shared-memory update of the next sub-block's
+//            columns first and of the rest while the next pivots run; a
+//            short last block is padded with the identity);
 //   panel  : L21 = A21 L11^-T in FP32 by 32-column blocks (products with the
 //            inverted 32 x 32 diagonal blocks of L11), and the operand
 //            planes of L21 for the tensor cores: a one-, two- or three-term
@@ -51,74 +53,151 @@ __device__ __forceinline__ void lp_cp16(float *dst, const float *src, int bytes)
 __device__ __forceinline__ void lp_cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // ---------------------------------------------------------------------------
-// diagonal block: b <= 128, one CTA of 1024 threads, block in shared memory
+// diagonal block: b <= 128, one CTA of 512 threads, block in shared memory
 
-__global__ void __launch_bounds__(1024) lowp_diag_kernel(float *L, int64_t ld, int64_t p, int b,
-                                                         int64_t *info, double *min_ratio, float *Wd) {
-    extern __shared__ float sa[];  // [128][129]: sa[r * kLpLd + c] = L11[r][c]; then sp, sw
-    float *sp = sa + kLpNb * kLpLd;  // sp[t * kLpPd + r] = L11[r][kb + t] for the rows below
-    __shared__ float rdiag[32];      // reciprocals of the current 32 x 32 factor's diagonal
-    __shared__ int failed;
-    if (*(volatile int64_t *)info >= 0) return;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    // A short last block is padded with the identity (blockdiag(A11, I) factors
-    // as blockdiag(L11, I)), so every step below runs unpredicated on 128 rows.
-    for (int e = tid; e < kLpNb * kLpNb; e += 1024) {
-        const int r = e % kLpNb, c = e / kLpNb;
-        if (c <= r) {
-            if (r < b)
-                lp_cp4(&sa[r * kLpLd + c], &L[(p + r) + (p + c) * ld]);
-            else
-                sa[r * kLpLd + c] = (r == c) ? 1.f : 0.f;
+constexpr int kDgThreads = 512;
+constexpr int kDgLt = 36;  // row stride of a transposed 32 x 32 factor (16-byte rows)
+constexpr size_t kDgSmem = sizeof(float) * (kLpNb * kLpLd + 2 * 32 * kLpPd + 32 * kDgLt);
+
+__device__ __forceinline__ float dg_rcp(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// a[r][c] -= sum_t P[t][r] P[t][c] over the 32 columns t of a solved panel
+// (P[t * kLpPd + r]), for rows r >= r0 and columns c0 <= c < c1, c <= r, in
+// 4 x 4 register tiles; thread `thr` of `nthr`.
+__device__ __forceinline__ void dg_syrk(float *sa, const float *P, int r0, int c0, int c1, int thr, int nthr) {
+    const int wr = (kLpNb - r0) / 4, wc = (c1 - c0) / 4;
+    for (int e = thr; e < wr * wc; e += nthr) {
+        const int rr = r0 + 4 * (e % wr), cc = c0 + 4 * (e / wr);
+        if (cc > rr + 3) continue;  // above the diagonal
+        float acc[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = sa[(rr + i) * kLpLd + cc + j];
+#pragma unroll 8
+        for (int t = 0; t < 32; ++t) {
+            const float4 a4 = *reinterpret_cast<const float4 *>(&P[t * kLpPd + rr]);
+            const float4 b4 = *reinterpret_cast<const float4 *>(&P[t * kLpPd + cc]);
+            const float av[4] = {a4.x, a4.y, a4.z, a4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(-av[i], bv[j], acc[i][j]);
         }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (cc + j <= rr + i) sa[(rr + i) * kLpLd + cc + j] = acc[i][j];
     }
-    if (tid == 0) failed = 0;
-    lp_cp_wait_all();
+}
+
+// Right-looking by 32-column blocks J with a look-ahead inside the block:
+//   (1) warp 0 factors the 32 x 32 diagonal block in registers (lane i holds
+//       row i) without square roots on the pivot chain: with d_c the pivot,
+//       a_ij -= (a_ic / d_c) a_jc, so one shuffle, one reciprocal, one
+//       multiply and one FMA separate successive pivots; the columns are
+//       scaled by 1/sqrt(d_c) afterwards.  Meanwhile warps 1-15 subtract the
+//       previous block's panel from the columns right of the next block;
+//   (2) the rows below solve x L_JJ^T = a, and 32 more threads solve the rows
+//       of the identity, giving W_JJ = L_JJ^-1 for the panel kernel (products
+//       with a transposed copy of L_JJ, read four entries at a time);
+//   (3) the panel is subtracted from the next block's 32 columns only, and
+//       the finished column block goes back to HBM.
+// A short last block is padded with the identity (blockdiag(A11, I) factors
+// as blockdiag(L11, I)), so every step runs unpredicated on 128 rows.
+__global__ void __launch_bounds__(kDgThreads) lowp_diag_kernel(float *L, int64_t ld, int64_t p, int b,
+                                                               int64_t *info, double *min_ratio, float *Wd) {
+    extern __shared__ __align__(16) float sa[];  // sa[r * kLpLd + c] = A11[r][c]
+    float *sp = sa + kLpNb * kLpLd;               // sp[(J & 1) * 32 * kLpPd + t * kLpPd + r] = L11[r][32 J + t]
+    float *slt = sp + 2 * 32 * kLpPd;             // slt[c * kDgLt + c2] = L_JJ[c2][c] for c2 > c, else 0
+    __shared__ float rdiag[32];                   // 1 / L_JJ[c][c]
+    __shared__ int failed, skip;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    pdl_wait();  // the block comes from the update just before
+    pdl_trigger();
+    // the block in two copy groups: columns 0-31 (the first factor step), then the rest
+#pragma unroll
+    for (int grp = 0; grp < 2; ++grp) {
+        const int ncol = grp == 0 ? 32 : kLpNb - 32, cbase = grp == 0 ? 0 : 32;
+        for (int e = tid; e < kLpNb * ncol; e += kDgThreads) {
+            const int r = e % kLpNb, c = cbase + e / kLpNb;
+            if (c <= r) {
+                if (r < b)
+                    lp_cp4(&sa[r * kLpLd + c], &L[(p + r) + (p + c) * ld]);
+                else
+                    sa[r * kLpLd + c] = (r == c) ? 1.f : 0.f;
+            }
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    if (tid == 0) {
+        failed = 0;
+        skip = *(volatile int64_t *)info >= 0;
+    }
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
     __syncthreads();
+    if (skip) {
+        lp_cp_wait_all();
+        return;
+    }
     float ratio = 1e30f;
 #pragma unroll 1
-    for (int kb = 0; kb < kLpNb; kb += 32) {
-        // (1) one warp: Cholesky of the 32 x 32 block; lane i holds row kb+i.
-        // The column loop is branch-free (selects only) so that its shuffles
-        // overlap; entries above the diagonal pick up values never read.
+    for (int J = 0; J < 4; ++J) {
+        const int kb = 32 * J;
+        const float *Pprev = sp + ((J + 1) & 1) * 32 * kLpPd;
+        float *Pcur = sp + (J & 1) * 32 * kLpPd;
         if (warp == 0) {
+            // (1) sqrt-free Cholesky of the 32 x 32 block; the column loop is
+            // branch-free (selects only) so that its shuffles overlap
             float v[32];
 #pragma unroll
             for (int c = 0; c < 32; ++c) v[c] = (c <= lane) ? sa[(kb + lane) * kLpLd + kb + c] : 0.f;
             bool bad = false;
-            float mypiv = 1.f, myd = 1.f;  // this lane's pivot and L[lane][lane]
+            float myd = 1.f;  // this lane's pivot d_lane
 #pragma unroll
             for (int c = 0; c < 32; ++c) {
-                const float piv = __shfl_sync(0xffffffffu, v[c], c);
-                bad |= !(piv > 0.f);  // non-positive (or NaN) pivot: breakdown
-                const float rl = rsqrtf(fmaxf(piv, 1e-30f));  // 1 / L[c][c]
-                const float d = piv * rl;
-                mypiv = (lane == c) ? piv : mypiv;
+                const float d = __shfl_sync(0xffffffffu, v[c], c);
+                bad |= !(d > 0.f);  // non-positive (or NaN) pivot: breakdown
                 myd = (lane == c) ? d : myd;
-                v[c] = (lane == c) ? d : v[c] * rl;
+                const float s = v[c] * dg_rcp(d);  // a_{lane,c} / d_c
 #pragma unroll
                 for (int c2 = c + 1; c2 < 32; ++c2) {
                     const float t = __shfl_sync(0xffffffffu, v[c], c2);
-                    v[c2] = fmaf(-v[c], t, v[c2]);
+                    v[c2] = fmaf(-s, t, v[c2]);
                 }
             }
-            if (kb + lane < b) ratio = fminf(ratio, mypiv);
+            // L[lane][c] = a_{lane,c} / sqrt(d_c) (c < lane), L[lane][lane] = sqrt(d_lane)
+            const float rs_me = rsqrtf(myd);
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+                const float rs = __shfl_sync(0xffffffffu, rs_me, c);
+                v[c] = (c < lane) ? v[c] * rs : (c == lane ? myd * rs_me : 0.f);
+            }
+            if (kb + lane < b) ratio = fminf(ratio, myd);
             if (lane == 0 && bad) failed = 1;
 #pragma unroll
-            for (int c = 0; c < 32; ++c)
+            for (int c = 0; c < 32; ++c) {
                 if (c <= lane) sa[(kb + lane) * kLpLd + kb + c] = v[c];
-            rdiag[lane] = 1.f / myd;
+                slt[c * kDgLt + lane] = (lane > c) ? v[c] : 0.f;
+            }
+            rdiag[lane] = rs_me;
+        } else if (J > 0) {
+            // the previous panel's product for the columns right of this block
+            dg_syrk(sa, Pprev, kb + 32, kb + 32, kLpNb, tid - 32, kDgThreads - 32);
         }
+        if (J == 0) asm volatile("cp.async.wait_group 0;" ::: "memory");  // this thread's copies, columns 32-127
         __syncthreads();
         if (failed) break;
-        const int rest0 = kb + 32;
-        const int w = kLpNb - rest0;
-        // (2) rows below inside the block: row r solves against the 32 x 32
-        // factor, x L_JJ^T = a.  32 more threads solve the rows of the identity,
-        // which gives the columns of W_JJ = L_JJ^-1 for the panel kernel.
+        const int w = kLpNb - kb - 32;  // rows below the diagonal block
+        // (2) rows below: x L_JJ^T = a; rows of the identity: W_JJ
         if (tid < w + 32) {
-            const int ie = tid - w;               // identity row, when >= 0
-            const int r = ie < 0 ? rest0 + tid : 0;  // (row 0: any in-bounds address)
+            const int ie = tid - w;                  // identity row, when >= 0
+            const int r = ie < 0 ? kb + 32 + tid : 0;  // (row 0: any in-bounds address)
             float v[32];
 #pragma unroll
             for (int c = 0; c < 32; ++c) v[c] = (ie < 0) ? sa[r * kLpLd + kb + c] : (c == ie ? 1.f : 0.f);
@@ -126,13 +205,19 @@ __global__ void __launch_bounds__(1024) lowp_diag_kernel(float *L, int64_t ld, i
             for (int c = 0; c < 32; ++c) {
                 v[c] *= rdiag[c];
 #pragma unroll
-                for (int c2 = c + 1; c2 < 32; ++c2) v[c2] = fmaf(-v[c], sa[(kb + c2) * kLpLd + kb + c], v[c2]);
+                for (int g = (c + 1) / 4; g < 8; ++g) {
+                    const float4 l4 = *reinterpret_cast<const float4 *>(&slt[c * kDgLt + 4 * g]);
+                    const float lv[4] = {l4.x, l4.y, l4.z, l4.w};
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        if (4 * g + i > c) v[4 * g + i] = fmaf(-v[c], lv[i], v[4 * g + i]);
+                }
             }
             if (ie < 0) {
 #pragma unroll
                 for (int c = 0; c < 32; ++c) {
                     sa[r * kLpLd + kb + c] = v[c];
-                    sp[c * kLpPd + r] = v[c];
+                    Pcur[c * kLpPd + r] = v[c];
                 }
             } else {
 #pragma unroll
@@ -140,33 +225,13 @@ __global__ void __launch_bounds__(1024) lowp_diag_kernel(float *L, int64_t ld, i
             }
         }
         __syncthreads();
-        // (3) trailing part of the block, a[r][c] -= sum_t a[r][kb+t] a[c][kb+t],
-        // in 4 x 4 register tiles on or below the diagonal
-        const int wt = w / 4;
-        for (int e = tid; e < wt * wt; e += 1024) {
-            const int ti = e % wt, tj = e / wt;
-            if (tj <= ti) {
-                const int r0 = rest0 + 4 * ti, c0 = rest0 + 4 * tj;
-                float acc[4][4];
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) acc[i][j] = sa[(r0 + i) * kLpLd + c0 + j];
-#pragma unroll 8
-                for (int t = 0; t < 32; ++t) {
-                    const float4 a4 = *reinterpret_cast<const float4 *>(&sp[t * kLpPd + r0]);
-                    const float4 b4 = *reinterpret_cast<const float4 *>(&sp[t * kLpPd + c0]);
-                    const float av[4] = {a4.x, a4.y, a4.z, a4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
-#pragma unroll
-                    for (int i = 0; i < 4; ++i)
-#pragma unroll
-                        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(-av[i], bv[j], acc[i][j]);
-                }
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int j = 0; j < 4; ++j)
-                        if (c0 + j <= r0 + i) sa[(r0 + i) * kLpLd + c0 + j] = acc[i][j];
+        // (3) the next block's columns; the finished column block to HBM
+        if (tid < 256) {
+            if (w > 0) dg_syrk(sa, Pcur, kb + 32, kb + 32, kb + 64, tid, 256);
+        } else {
+            for (int e = tid - 256; e < (kLpNb - kb) * 32; e += kDgThreads - 256) {
+                const int r = kb + e % (kLpNb - kb), c = kb + e / (kLpNb - kb);
+                if (r < b && c <= r) L[(p + r) + (p + c) * ld] = sa[r * kLpLd + c];
             }
         }
         __syncthreads();
@@ -186,10 +251,6 @@ __global__ void __launch_bounds__(1024) lowp_diag_kernel(float *L, int64_t ld, i
                 atomicMin((unsigned long long *)min_ratio,
                           (unsigned long long)__double_as_longlong(d));
         }
-    }
-    for (int e = tid; e < kLpNb * kLpNb; e += 1024) {
-        const int r = e % kLpNb, c = e / kLpNb;
-        if (r < b && c <= r) L[(p + r) + (p + c) * ld] = sa[r * kLpLd + c];
     }
 }
 
@@ -222,7 +283,7 @@ constexpr int kPnWd = 32 + 4;       // row stride of sWT (k-major W_JJ)
 constexpr size_t kPnSmem = sizeof(float) * (kLpNb * kPnXd + (kLpNb - 32) * kPnLd + 4 * 32 * kPnWd);
 
 template <typename H>
-__global__ void __launch_bounds__(256) lowp_panel_kernel(float *L, int64_t ld, int64_t n, int64_t p,
+__global__ void __launch_bounds__(256, 2) lowp_panel_kernel(float *L, int64_t ld, int64_t n, int64_t p,
                                                          const float *__restrict__ Wd, H *planes,
                                                          int64_t plane_stride, int64_t ldp, int koff, int terms,
                                                          const int64_t *info) {
@@ -230,21 +291,31 @@ __global__ void __launch_bounds__(256) lowp_panel_kernel(float *L, int64_t ld, i
     float *sXT = sm;                         // sXT[k * kPnXd + r] = row r, column k of the tile
     float *sLT = sXT + kLpNb * kPnXd;        // sLT[k * kPnLd + c] = L11[c][k]
     float *sWT = sLT + (kLpNb - 32) * kPnLd;  // sWT[(J * 32 + k) * kPnWd + c] = W_JJ[c][k]
-    if (*(volatile const int64_t *)info >= 0) return;
     const int tid = threadIdx.x;
     const int64_t q = p + kLpNb;
     const int64_t row0 = q + (int64_t)blockIdx.x * kPnRows;
     // Columns of the row tile and of L11 are contiguous in memory.  With
     // 16-byte aligned columns every input is copied by cp.async, all of a
     // thread's copies in flight at once; otherwise by plain loads.
-    if (ld % 4 == 0 && (reinterpret_cast<uintptr_t>(L) & 15) == 0) {
-        // row tile: sXT[k][r] = L[row0 + r][p + k], 16 four-row chunks per column
+    const bool al16 = ld % 4 == 0 && (reinterpret_cast<uintptr_t>(L) & 15) == 0;
+    if (al16) {
+        // row tile: sXT[k][r] = L[row0 + r][p + k], 16 four-row chunks per column.
+        // It was written by the update before the diagonal block's kernel, so
+        // it is copied before the wait on that kernel.
         for (int e = tid; e < kLpNb * (kPnRows / 4); e += 256) {
             const int k = e / (kPnRows / 4), c4 = e % (kPnRows / 4);
             const int64_t r = row0 + 4 * c4;
             const int valid = n - r >= 4 ? 4 : (n - r > 0 ? (int)(n - r) : 0);
             lp_cp16(&sXT[k * kPnXd + 4 * c4], valid ? L + r + (p + k) * ld : L, 4 * valid);
         }
+    }
+    pdl_wait();  // L11, W_JJ and the status from the diagonal block's kernel
+    pdl_trigger();
+    if (*(volatile const int64_t *)info >= 0) {
+        lp_cp_wait_all();
+        return;
+    }
+    if (al16) {
         // L11 below its diagonal blocks: column k < 96, rows c in [32 (k/32 + 1), 128)
         for (int e = tid; e < 32 * (24 + 16 + 8); e += 256) {
             const int kb = e < 32 * 24 ? 0 : (e < 32 * 40 ? 1 : 2);
@@ -287,15 +358,25 @@ __global__ void __launch_bounds__(256) lowp_panel_kernel(float *L, int64_t ld, i
             acc[0][u] = sXT[(cj + u) * kPnXd + rt];
             acc[1][u] = sXT[(cj + u) * kPnXd + rt + 32];
         }
-        // Y_J = A_J - X_{<J} L_J,<J^T
-        for (int k = 0; k < J * 32; ++k) {
-            const float x0 = sXT[k * kPnXd + rt], x1 = sXT[k * kPnXd + rt + 32];
-            const float4 l4 = *reinterpret_cast<const float4 *>(&sLT[k * kPnLd + cj]);
-            const float lv[4] = {l4.x, l4.y, l4.z, l4.w};
+        // Y_J = A_J - X_{<J} L_J,<J^T, eight k at a time: all their shared loads
+        // issue before the products, so the loop is not a chain of load latencies
+        for (int k0 = 0; k0 < J * 32; k0 += 8) {
+            float x0[8], x1[8];
+            float4 l4[8];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                acc[0][u] = fmaf(-x0, lv[u], acc[0][u]);
-                acc[1][u] = fmaf(-x1, lv[u], acc[1][u]);
+            for (int kk = 0; kk < 8; ++kk) {
+                x0[kk] = sXT[(k0 + kk) * kPnXd + rt];
+                x1[kk] = sXT[(k0 + kk) * kPnXd + rt + 32];
+                l4[kk] = *reinterpret_cast<const float4 *>(&sLT[(k0 + kk) * kPnLd + cj]);
+            }
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+                const float lv[4] = {l4[kk].x, l4[kk].y, l4[kk].z, l4[kk].w};
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    acc[0][u] = fmaf(-x0[kk], lv[u], acc[0][u]);
+                    acc[1][u] = fmaf(-x1[kk], lv[u], acc[1][u]);
+                }
             }
         }
         __syncthreads();  // every thread has read A_J
@@ -307,15 +388,25 @@ __global__ void __launch_bounds__(256) lowp_panel_kernel(float *L, int64_t ld, i
         __syncthreads();
         // X_J = Y_J W_JJ^T
         float x[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-#pragma unroll 8
-        for (int k = 0; k < 32; ++k) {
-            const float y0 = sXT[(J * 32 + k) * kPnXd + rt], y1 = sXT[(J * 32 + k) * kPnXd + rt + 32];
-            const float4 w4 = *reinterpret_cast<const float4 *>(&sWT[(J * 32 + k) * kPnWd + 4 * ct]);
-            const float wv[4] = {w4.x, w4.y, w4.z, w4.w};
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                x[0][u] = fmaf(y0, wv[u], x[0][u]);
-                x[1][u] = fmaf(y1, wv[u], x[1][u]);
+        for (int k0 = 0; k0 < 32; k0 += 8) {
+            float y0[8], y1[8];
+            float4 w4[8];
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+                const int k = J * 32 + k0 + kk;
+                y0[kk] = sXT[k * kPnXd + rt];
+                y1[kk] = sXT[k * kPnXd + rt + 32];
+                w4[kk] = *reinterpret_cast<const float4 *>(&sWT[k * kPnWd + 4 * ct]);
+            }
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+                const float wv[4] = {w4[kk].x, w4[kk].y, w4[kk].z, w4[kk].w};
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    x[0][u] = fmaf(y0[kk], wv[u], x[0][u]);
+                    x[1][u] = fmaf(y1[kk], wv[u], x[1][u]);
+                }
             }
         }
         __syncthreads();  // every thread has read Y_J
@@ -391,7 +482,7 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
     int *err_word = (int *)c->mixed.tcerr.p;
     unsigned *sched = (unsigned *)c->mixed.tcerr.p + 1;
     if (cudaMemsetAsync(err_word, 0, 4 * sizeof(int), st) != cudaSuccess) return -1;
-    const size_t smem_l11 = sizeof(float) * (kLpNb * kLpLd + 32 * kLpPd);
+    const size_t smem_l11 = kDgSmem;
     const size_t smem_panel = kPnSmem;
     if (c->mixed.pinv.ensure(sizeof(float) * 4 * 32 * 32) != cudaSuccess) return -1;
     float *Wd = (float *)c->mixed.pinv.p;
@@ -405,20 +496,27 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
         tc_update_prepare() != 0)
         return -1;
     const size_t esz = sizeof(uint16_t);
+    // Every launch of the loop below is a programmatic dependent of the one
+    // before it (each kernel waits for its predecessor's output after its
+    // set-up), so a kernel's launch and prologue overlap the previous tail.
     auto diag = [&](int64_t p, int b) {
         LaunchScope ls(K_MIXED_DIAG, st, (double)b * b * b / 3.0);
-        lowp_diag_kernel<<<1, 1024, smem_l11, st>>>(L, ld, p, b, info, min_ratio, Wd);
+        launch_maybe_pdl(true, lowp_diag_kernel, dim3(1), dim3(kDgThreads), smem_l11, st, L, ld, p, b, info,
+                         min_ratio, Wd);
     };
     // L21 and its planes for rows [p + 128, n), written to plane half `half`
     auto panel = [&](int64_t p, int half) {
         const int64_t rest = n - p - kLpNb;
         LaunchScope ls(K_MIXED_PANEL, st, (double)rest * kLpNb * kLpNb);
+        const dim3 grid((unsigned)ceil_div(rest, kPnRows));
         if (fp16)
-            lowp_panel_kernel<__half><<<(unsigned)ceil_div(rest, kPnRows), 256, smem_panel, st>>>(
-                L, ld, n, p, Wd, (__half *)planes, plane_stride, ldp, half * kLpNb, terms, info);
+            launch_maybe_pdl(true, lowp_panel_kernel<__half>, grid, dim3(256), smem_panel, st, L, ld, n, p,
+                             (const float *)Wd, (__half *)planes, plane_stride, ldp, half * kLpNb, terms,
+                             (const int64_t *)info);
         else
-            lowp_panel_kernel<__nv_bfloat16><<<(unsigned)ceil_div(rest, kPnRows), 256, smem_panel, st>>>(
-                L, ld, n, p, Wd, (__nv_bfloat16 *)planes, plane_stride, ldp, half * kLpNb, terms, info);
+            launch_maybe_pdl(true, lowp_panel_kernel<__nv_bfloat16>, grid, dim3(256), smem_panel, st, L, ld, n,
+                             p, (const float *)Wd, (__nv_bfloat16 *)planes, plane_stride, ldp, half * kLpNb,
+                             terms, (const int64_t *)info);
     };
     // A22 -= sum of the products of K columns of the planes, rows [q, n)
     auto update = [&](int64_t q, int kext, bool narrow) -> int {
@@ -430,7 +528,7 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
                               : (double)rows * (rows + 1) * kext);
         return tc_update_launch(L, ld, q, n, (char *)planes + (size_t)q * ldp * esz, plane_stride, ldp, rows,
                                 kext, terms, fp16, pairs, info, err_word, sched, narrow, st, opts.update_kchunk,
-                                opts.update_epilogue);
+                                opts.update_epilogue, true);
     };
     // Panels in pairs: after panel p only the next panel's 128 columns are
     // updated (narrow); panel p + 128 is factored, and then both panels'

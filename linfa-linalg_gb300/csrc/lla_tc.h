@@ -28,9 +28,11 @@ int tc_update_prepare();
 // bounded waits record LLA_ERR_TIMEOUT in *err_word.  sched: two zeroed words
 // (the next unclaimed tile, the CTAs finished) that CTAs claim tiles from;
 // the last CTA to finish zeroes them again for the next launch on the stream.
+// pdl: launched as a programmatic dependent of the stream's previous kernel,
+// whose output it waits for after its set-up.
 int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, int64_t plane_stride,
                      int64_t ldp, int64_t rows, int kext, int terms, bool fp16, const TcPairs &pairs,
                      const int64_t *info, int *err_word, unsigned *sched, bool narrow, cudaStream_t st,
-                     int kchunk = 64, int epilogue = 0);
+                     int kchunk = 64, int epilogue = 0, bool pdl = false);
 
 }  // namespace lla

@@ -142,14 +142,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     __shared__ int s_abort, s_skip, s_epi_abort, s_epi_tile;
     __shared__ int s_tile[kTcTileRing];
     __shared__ __align__(8) uint64_t s_tbar[2 * kTcTileRing];  // tile ring: full[R], empty[R]
-    // one reader decides for the whole CTA (another CTA may set err_word meanwhile)
-    if (threadIdx.x == 0)
-        s_skip = (*(volatile const int64_t *)info >= 0 || *(volatile const int *)err_word != 0);
-    __syncthreads();
-    if (s_skip) {
-        if (threadIdx.x == 0) tc_sched_done(sched);
-        return;
-    }
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     constexpr int kTile = tc_tile_bytes<KC>();
     const int S = tc_stages<KC>(terms, EPI_TMA);
@@ -195,10 +187,26 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
+    // The set-up above may overlap the previous kernel's tail (programmatic
+    // launch); the operand planes and the status words come from it.
+    pdl_wait();
+    pdl_trigger();
+    // one reader decides for the whole CTA (another CTA may set err_word meanwhile)
+    if (tid == 0) s_skip = (*(volatile const int64_t *)info >= 0 || *(volatile const int *)err_word != 0);
+    __syncthreads();
+    if (s_skip) {
+        if (warp == 0)
+            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcAlloc)
+                         : "memory");
+        if (tid == 0) tc_sched_done(sched);
+        return;
+    }
 
     if (warp == 8) {
         if (lane == 0) {  // tile claims and TMA producer
             int64_t g = 0;
+            // one claim ahead: the next tile is claimed while this one's chunks load
+            int64_t t_next = (int64_t)atomicAdd(&sched[0], 1u);
             for (int64_t lt = 0; !*(volatile int *)&s_abort; ++lt) {
                 const int slot = (int)(lt % kTcTileRing);
                 const int64_t ruse = lt / kTcTileRing;
@@ -206,10 +214,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
                     s_abort = 1;
                     break;
                 }
-                const int64_t t = (int64_t)atomicAdd(&sched[0], 1u);
+                const int64_t t = t_next;
                 s_tile[slot] = t < ntiles ? (int)t : -1;
                 mbar_arrive(rfull0 + 8 * slot);  // release: the index is visible to the waiters
                 if (t >= ntiles) break;
+                t_next = (int64_t)atomicAdd(&sched[0], 1u);
                 int64_t I, J;
                 tc_tile(t, narrow, I, J);
                 for (int kc = 0; kc < kchunks; ++kc, ++g) {
@@ -472,7 +481,7 @@ int tc_update_prepare() {
 int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, int64_t plane_stride,
                      int64_t ldp, int64_t rows, int kext, int terms, bool fp16, const TcPairs &pairs,
                      const int64_t *info, int *err_word, unsigned *sched, bool narrow, cudaStream_t st,
-                     int kchunk, int epilogue) {
+                     int kchunk, int epilogue, bool pdl) {
     // The TMA-staged epilogue needs 16-byte rows of C (and 32-wide K-chunks).  By
     // default it serves the one- and two-term forms (fp16x3 at n = 16384: 7.8 vs
     // 8.8 ms a solve); the six-product form keeps the register epilogue, which
@@ -532,9 +541,10 @@ int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, i
                                          : (terms == 2 ? tc_update_kernel<2, 32, false> : tc_update_kernel<3, 32, false>))
                            : (terms == 1 ? tc_update_kernel<1, 64, false>
                                          : (terms == 2 ? tc_update_kernel<2, 64, false> : tc_update_kernel<3, 64, false>));
-    kern<<<grid, kTcThreads, tc_smem_bytes(epi_tma), st>>>(map, cmap, C, ld, q, n, kext / kc, idesc, tiles,
-                                                            narrow ? 1 : 0, info, err_word, sched);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    const cudaError_t e = launch_maybe_pdl(pdl, kern, dim3(grid), dim3(kTcThreads), (size_t)tc_smem_bytes(epi_tma),
+                                           st, map, cmap, C, ld, q, n, kext / kc, idesc, tiles, narrow ? 1 : 0,
+                                           info, err_word, sched);
+    return e == cudaSuccess ? 0 : -1;
 }
 
 }  // namespace lla
