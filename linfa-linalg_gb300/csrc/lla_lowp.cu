@@ -477,10 +477,12 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
     const int64_t plane_stride = n * ldp;  // elements per plane
     if (c->mixed.opA.ensure(sizeof(uint16_t) * plane_stride * terms) != cudaSuccess) return -1;
     void *planes = c->mixed.opA.p;
-    // status word, then the update's two tile-scheduling words (zero between launches)
+    // status word, then the update's tile-claim counter (zeroed here; the
+    // launches below advance sched_base in step with it)
     if (c->mixed.tcerr.ensure(4 * sizeof(int)) != cudaSuccess) return -1;
     int *err_word = (int *)c->mixed.tcerr.p;
     unsigned *sched = (unsigned *)c->mixed.tcerr.p + 1;
+    unsigned sched_base = 0;
     if (cudaMemsetAsync(err_word, 0, 4 * sizeof(int), st) != cudaSuccess) return -1;
     const size_t smem_l11 = kDgSmem;
     const size_t smem_panel = kPnSmem;
@@ -527,8 +529,8 @@ int lowp_factor_launch(float *L, int64_t n, int64_t ld, const lla_refine_opts &o
                        narrow ? (double)rows * cols * kext * 2.0 - (double)cols * (cols - 1) * kext
                               : (double)rows * (rows + 1) * kext);
         return tc_update_launch(L, ld, q, n, (char *)planes + (size_t)q * ldp * esz, plane_stride, ldp, rows,
-                                kext, terms, fp16, pairs, info, err_word, sched, narrow, st, opts.update_kchunk,
-                                opts.update_epilogue, true);
+                                kext, terms, fp16, pairs, info, err_word, sched, &sched_base, narrow, st,
+                                opts.update_kchunk, opts.update_epilogue, true);
     };
     // Panels in pairs: after panel p only the next panel's 128 columns are
     // updated (narrow); panel p + 128 is factored, and then both panels'

@@ -4,7 +4,10 @@
 // Persistent CTAs (at most one per SM) claim the 128 x 128 lower tiles
 // (I >= J) of the trailing matrix one at a time from a global counter, so a
 // CTA that starts late -- its SM still busy with another stream's work --
-// takes fewer tiles instead of delaying the launch:
+// takes fewer tiles instead of delaying the launch.  The counter is never
+// reset between launches: every CTA makes exactly one claim more than the
+// tiles it processes, so a launch advances it by tiles + CTAs and the host
+// passes each launch the value it starts from:
 //   * one thread streams 64-wide K chunks of the two operand row blocks, every
 //     term plane of a chunk in one TMA box (cp.async.bulk.tensor, 128-byte
 //     swizzle), into a shared-memory ring of 2-6 stages, completion tracked by
@@ -99,16 +102,6 @@ constexpr int kTcThreads = 320;  // 8 epilogue warps, 1 producer warp, 1 MMA war
 constexpr int kTcEpiThreads = 256;
 constexpr int kTcTileRing = 8;  // claimed tile indices in flight inside a CTA
 
-// The CTA claims no more tiles: the last CTA of the launch to get here zeroes
-// the scheduling words (next tile, CTAs finished) for the next launch.
-__device__ __forceinline__ void tc_sched_done(unsigned *sched) {
-    __threadfence();
-    if (atomicAdd(&sched[1], 1u) == gridDim.x - 1) {
-        atomicExch(&sched[0], 0u);
-        atomicExch(&sched[1], 0u);
-    }
-}
-
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
@@ -136,7 +129,7 @@ template <int TERMS, int KC, bool EPI_TMA>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap cmap, float *C, int64_t ld,
     int64_t q, int64_t n, int kchunks, uint32_t idesc, int64_t ntiles, int narrow, const int64_t *info,
-    int *err_word, unsigned *sched) {
+    int *err_word, unsigned *sched, unsigned sched_base) {
     constexpr int terms = TERMS, NP = tc_npairs(TERMS);
     extern __shared__ uint8_t smem_raw[];
     __shared__ int s_abort, s_skip, s_epi_abort, s_epi_tile;
@@ -198,15 +191,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
         if (warp == 0)
             asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcAlloc)
                          : "memory");
-        if (tid == 0) tc_sched_done(sched);
-        return;
+        return;  // the launch is void (a failed or timed-out factorisation): its claims do not matter
     }
 
     if (warp == 8) {
         if (lane == 0) {  // tile claims and TMA producer
             int64_t g = 0;
             // one claim ahead: the next tile is claimed while this one's chunks load
-            int64_t t_next = (int64_t)atomicAdd(&sched[0], 1u);
+            int64_t t_next = (int64_t)(atomicAdd(sched, 1u) - sched_base);
             for (int64_t lt = 0; !*(volatile int *)&s_abort; ++lt) {
                 const int slot = (int)(lt % kTcTileRing);
                 const int64_t ruse = lt / kTcTileRing;
@@ -218,7 +210,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
                 s_tile[slot] = t < ntiles ? (int)t : -1;
                 mbar_arrive(rfull0 + 8 * slot);  // release: the index is visible to the waiters
                 if (t >= ntiles) break;
-                t_next = (int64_t)atomicAdd(&sched[0], 1u);
+                t_next = (int64_t)(atomicAdd(sched, 1u) - sched_base);
                 int64_t I, J;
                 tc_tile(t, narrow, I, J);
                 for (int kc = 0; kc < kchunks; ++kc, ++g) {
@@ -443,7 +435,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_update_kernel(
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcAlloc)
                      : "memory");
-    if (tid == 0) tc_sched_done(sched);  // this CTA's producer claims no more tiles
 }
 
 // ---------------------------------------------------------------------------
@@ -480,8 +471,8 @@ int tc_update_prepare() {
 
 int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, int64_t plane_stride,
                      int64_t ldp, int64_t rows, int kext, int terms, bool fp16, const TcPairs &pairs,
-                     const int64_t *info, int *err_word, unsigned *sched, bool narrow, cudaStream_t st,
-                     int kchunk, int epilogue, bool pdl) {
+                     const int64_t *info, int *err_word, unsigned *sched, unsigned *sched_base, bool narrow,
+                     cudaStream_t st, int kchunk, int epilogue, bool pdl) {
     // The TMA-staged epilogue needs 16-byte rows of C (and 32-wide K-chunks).  By
     // default it serves the one- and two-term forms (fp16x3 at n = 16384: 7.8 vs
     // 8.8 ms a solve); the six-product form keeps the register epilogue, which
@@ -490,7 +481,7 @@ int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, i
     const bool epi_tma = want_tma && ld % 4 == 0 && (reinterpret_cast<uintptr_t>(C) & 15) == 0 &&
                          ld * 4 < (1ll << 40) && n < (1ll << 31);
     const int kc = (epi_tma || kchunk == 32) ? 32 : 64;
-    if (!g_encode || !sched || rows <= 0 || kext % kc != 0 || kext > ldp || (ldp * 2) % 16 != 0 || terms < 1 ||
+    if (!g_encode || !sched || !sched_base || rows <= 0 || kext % kc != 0 || kext > ldp || (ldp * 2) % 16 != 0 || terms < 1 ||
         terms > 3 || (reinterpret_cast<uintptr_t>(planes) & 15) != 0)
         return -1;
     const int64_t tr = (rows + kTcM - 1) / kTcM;
@@ -543,7 +534,8 @@ int tc_update_launch(float *C, int64_t ld, int64_t q, int64_t n, void *planes, i
                                          : (terms == 2 ? tc_update_kernel<2, 64, false> : tc_update_kernel<3, 64, false>));
     const cudaError_t e = launch_maybe_pdl(pdl, kern, dim3(grid), dim3(kTcThreads), (size_t)tc_smem_bytes(epi_tma),
                                            st, map, cmap, C, ld, q, n, kext / kc, idesc, tiles, narrow ? 1 : 0,
-                                           info, err_word, sched);
+                                           info, err_word, sched, *sched_base);
+    *sched_base += (unsigned)(tiles + grid);  // every CTA claims once more than it processes
     return e == cudaSuccess ? 0 : -1;
 }
 
