@@ -56,8 +56,9 @@ __device__ __forceinline__ void lp_cp_wait_all() { asm volatile("cp.async.wait_a
 // diagonal block: b <= 128, one CTA of 512 threads, block in shared memory
 
 constexpr int kDgThreads = 512;
-constexpr int kDgLt = 36;  // row stride of a transposed 32 x 32 factor (16-byte rows)
-constexpr size_t kDgSmem = sizeof(float) * (kLpNb * kLpLd + 2 * 32 * kLpPd + 32 * kDgLt);
+constexpr int kDgLd = kLpNb + 4;  // column stride of the block in shared memory (16-byte columns)
+constexpr int kDgLt = 36;         // row stride of a transposed 32 x 32 factor (16-byte rows)
+constexpr size_t kDgSmem = sizeof(float) * (kLpNb * kDgLd + 32 * kDgLt + 3 * 32);
 
 __device__ __forceinline__ float dg_rcp(float x) {
     float r;
@@ -65,134 +66,173 @@ __device__ __forceinline__ float dg_rcp(float x) {
     return r;
 }
 
-// a[r][c] -= sum_t P[t][r] P[t][c] over the 32 columns t of a solved panel
-// (P[t * kLpPd + r]), for rows r >= r0 and columns c0 <= c < c1, c <= r, in
-// 4 x 4 register tiles; thread `thr` of `nthr`.
-__device__ __forceinline__ void dg_syrk(float *sa, const float *P, int r0, int c0, int c1, int thr, int nthr) {
+// a(r, c) -= sum_t a(r, k0 + t) a(c, k0 + t) over the 32 solved columns
+// k0 .. k0 + 31, for rows r >= r0 and columns c0 <= c < c1, c <= r, in 4 x 4
+// register tiles (column-major block, sa[c * kDgLd + r]); thread `thr` of `nthr`.
+__device__ __forceinline__ void dg_syrk(float *sa, int k0, int r0, int c0, int c1, int thr, int nthr) {
     const int wr = (kLpNb - r0) / 4, wc = (c1 - c0) / 4;
     for (int e = thr; e < wr * wc; e += nthr) {
         const int rr = r0 + 4 * (e % wr), cc = c0 + 4 * (e / wr);
         if (cc > rr + 3) continue;  // above the diagonal
-        float acc[4][4];
+        float4 acc[4];              // acc[j]: column cc + j, rows rr .. rr + 3
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) acc[i][j] = sa[(rr + i) * kLpLd + cc + j];
+        for (int j = 0; j < 4; ++j) acc[j] = *reinterpret_cast<const float4 *>(&sa[(cc + j) * kDgLd + rr]);
 #pragma unroll 8
         for (int t = 0; t < 32; ++t) {
-            const float4 a4 = *reinterpret_cast<const float4 *>(&P[t * kLpPd + rr]);
-            const float4 b4 = *reinterpret_cast<const float4 *>(&P[t * kLpPd + cc]);
-            const float av[4] = {a4.x, a4.y, a4.z, a4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
+            const float4 a4 = *reinterpret_cast<const float4 *>(&sa[(k0 + t) * kDgLd + rr]);
+            const float4 b4 = *reinterpret_cast<const float4 *>(&sa[(k0 + t) * kDgLd + cc]);
+            const float bv[4] = {b4.x, b4.y, b4.z, b4.w};
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(-av[i], bv[j], acc[i][j]);
+            for (int j = 0; j < 4; ++j) {
+                acc[j].x = fmaf(-a4.x, bv[j], acc[j].x);
+                acc[j].y = fmaf(-a4.y, bv[j], acc[j].y);
+                acc[j].z = fmaf(-a4.z, bv[j], acc[j].z);
+                acc[j].w = fmaf(-a4.w, bv[j], acc[j].w);
+            }
         }
+        if (cc + 3 <= rr) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) *reinterpret_cast<float4 *>(&sa[(cc + j) * kDgLd + rr]) = acc[j];
+        } else {
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
-                if (cc + j <= rr + i) sa[(rr + i) * kLpLd + cc + j] = acc[i][j];
+            for (int j = 0; j < 4; ++j) {
+                const float av[4] = {acc[j].x, acc[j].y, acc[j].z, acc[j].w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    if (cc + j <= rr + i) sa[(cc + j) * kDgLd + rr + i] = av[i];
+            }
+        }
     }
 }
 
 // Right-looking by 32-column blocks J with a look-ahead inside the block:
-//   (1) warp 0 factors the 32 x 32 diagonal block in registers (lane i holds
-//       row i) without square roots on the pivot chain: with d_c the pivot,
-//       a_ij -= (a_ic / d_c) a_jc, so one shuffle, one reciprocal, one
-//       multiply and one FMA separate successive pivots; the columns are
-//       scaled by 1/sqrt(d_c) afterwards.  Meanwhile warps 1-15 subtract the
-//       previous block's panel from the columns right of the next block;
+//   (1) warp 0 factors the 32 x 32 diagonal block (lane i holds row i in
+//       registers) without square roots on the pivot chain: with d_c the
+//       pivot, a_ij -= (a_ic / d_c) a_jc; column c reaches every lane through
+//       shared memory (one store, four-wide broadcast loads), so the chain
+//       between pivots is a store, a load, a reciprocal, a multiply and an
+//       FMA; the columns are scaled by 1/sqrt(d_c) afterwards.  Meanwhile
+//       warps 1-15 subtract the previous block's panel from the columns right
+//       of the next block;
 //   (2) the rows below solve x L_JJ^T = a, and 32 more threads solve the rows
 //       of the identity, giving W_JJ = L_JJ^-1 for the panel kernel (products
 //       with a transposed copy of L_JJ, read four entries at a time);
 //   (3) the panel is subtracted from the next block's 32 columns only, and
 //       the finished column block goes back to HBM.
-// A short last block is padded with the identity (blockdiag(A11, I) factors
-// as blockdiag(L11, I)), so every step runs unpredicated on 128 rows.
+// The block is column-major in shared memory, copied in 16-byte pieces
+// (4-byte pieces for an unaligned matrix or a short last block, which is
+// padded with the identity: blockdiag(A11, I) factors as blockdiag(L11, I),
+// so every step runs unpredicated on 128 rows).
+// The kernel starts on whichever SM frees first, with a cold instruction
+// cache, and its unrolled steps are tens of KB of code: a first pass of the
+// step loop (J = -1) runs on the uninitialised shared memory, with every
+// global store off, while the previous kernel still finishes (before
+// pdl_wait), so the real passes run from a warm cache.
 __global__ void __launch_bounds__(kDgThreads) lowp_diag_kernel(float *L, int64_t ld, int64_t p, int b,
                                                                int64_t *info, double *min_ratio, float *Wd) {
-    extern __shared__ __align__(16) float sa[];  // sa[r * kLpLd + c] = A11[r][c]
-    float *sp = sa + kLpNb * kLpLd;               // sp[(J & 1) * 32 * kLpPd + t * kLpPd + r] = L11[r][32 J + t]
-    float *slt = sp + 2 * 32 * kLpPd;             // slt[c * kDgLt + c2] = L_JJ[c2][c] for c2 > c, else 0
+    extern __shared__ __align__(16) float sa[];  // sa[c * kDgLd + r] = A11[r][c]
+    float *slt = sa + kLpNb * kDgLd;              // slt[c * kDgLt + c2] = L_JJ[c2][c] for c2 > c, else 0
+    float *colb = slt + 32 * kDgLt;               // two column buffers of the factor, then 1/sqrt(d)
     __shared__ float rdiag[32];                   // 1 / L_JJ[c][c]
     __shared__ int failed, skip;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    pdl_wait();  // the block comes from the update just before
-    pdl_trigger();
-    // the block in two copy groups: columns 0-31 (the first factor step), then the rest
-#pragma unroll
-    for (int grp = 0; grp < 2; ++grp) {
-        const int ncol = grp == 0 ? 32 : kLpNb - 32, cbase = grp == 0 ? 0 : 32;
-        for (int e = tid; e < kLpNb * ncol; e += kDgThreads) {
-            const int r = e % kLpNb, c = cbase + e / kLpNb;
-            if (c <= r) {
-                if (r < b)
-                    lp_cp4(&sa[r * kLpLd + c], &L[(p + r) + (p + c) * ld]);
-                else
-                    sa[r * kLpLd + c] = (r == c) ? 1.f : 0.f;
-            }
-        }
-        asm volatile("cp.async.commit_group;" ::: "memory");
-    }
-    if (tid == 0) {
-        failed = 0;
-        skip = *(volatile int64_t *)info >= 0;
-    }
-    asm volatile("cp.async.wait_group 1;" ::: "memory");
-    __syncthreads();
-    if (skip) {
-        lp_cp_wait_all();
-        return;
-    }
+    const bool v16 = b == kLpNb && ld % 4 == 0 && (reinterpret_cast<uintptr_t>(L) & 15) == 0;
     float ratio = 1e30f;
 #pragma unroll 1
-    for (int J = 0; J < 4; ++J) {
-        const int kb = 32 * J;
-        const float *Pprev = sp + ((J + 1) & 1) * 32 * kLpPd;
-        float *Pcur = sp + (J & 1) * 32 * kLpPd;
+    for (int J = -1; J < 4; ++J) {
+        const bool dry = J < 0;  // the warm-up pass: step 1's code, nothing stored globally
+        if (J == 0) {
+            pdl_wait();  // the block comes from the update just before
+            pdl_trigger();
+            // the lower triangle in two copy groups: columns 0-31 (the first step), then the rest
+#pragma unroll
+            for (int grp = 0; grp < 2; ++grp) {
+                const int ncol = grp == 0 ? 32 : kLpNb - 32, cbase = grp == 0 ? 0 : 32;
+                if (v16) {
+                    for (int e = tid; e < ncol * (kLpNb / 4); e += kDgThreads) {
+                        const int r4 = 4 * (e % (kLpNb / 4)), c = cbase + e / (kLpNb / 4);
+                        if (r4 + 3 >= c) lp_cp16(&sa[c * kDgLd + r4], &L[(p + r4) + (p + c) * ld], 16);
+                    }
+                } else {
+                    for (int e = tid; e < ncol * kLpNb; e += kDgThreads) {
+                        const int r = e % kLpNb, c = cbase + e / kLpNb;
+                        if (c <= r) {
+                            if (r < b)
+                                lp_cp4(&sa[c * kDgLd + r], &L[(p + r) + (p + c) * ld]);
+                            else
+                                sa[c * kDgLd + r] = (r == c) ? 1.f : 0.f;
+                        }
+                    }
+                }
+                asm volatile("cp.async.commit_group;" ::: "memory");
+            }
+            if (tid == 0) {
+                failed = 0;
+                skip = *(volatile int64_t *)info >= 0;
+            }
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+            __syncthreads();
+            if (skip) {
+                lp_cp_wait_all();
+                return;
+            }
+            ratio = 1e30f;  // forget the warm-up pass's pivots
+        }
+        const int kb = dry ? 32 : 32 * J;
         if (warp == 0) {
-            // (1) sqrt-free Cholesky of the 32 x 32 block; the column loop is
-            // branch-free (selects only) so that its shuffles overlap
+            // (1) sqrt-free Cholesky of the 32 x 32 block
             float v[32];
 #pragma unroll
-            for (int c = 0; c < 32; ++c) v[c] = (c <= lane) ? sa[(kb + lane) * kLpLd + kb + c] : 0.f;
+            for (int c = 0; c < 32; ++c) v[c] = (c <= lane) ? sa[(kb + c) * kDgLd + kb + lane] : 0.f;
             bool bad = false;
             float myd = 1.f;  // this lane's pivot d_lane
 #pragma unroll
             for (int c = 0; c < 32; ++c) {
-                const float d = __shfl_sync(0xffffffffu, v[c], c);
+                float *cb = colb + (c & 1) * 32;  // column c of every lane (two buffers: no reuse hazard)
+                cb[lane] = v[c];
+                __syncwarp();
+                const float d = cb[c];
                 bad |= !(d > 0.f);  // non-positive (or NaN) pivot: breakdown
                 myd = (lane == c) ? d : myd;
                 const float s = v[c] * dg_rcp(d);  // a_{lane,c} / d_c
 #pragma unroll
-                for (int c2 = c + 1; c2 < 32; ++c2) {
-                    const float t = __shfl_sync(0xffffffffu, v[c], c2);
-                    v[c2] = fmaf(-s, t, v[c2]);
+                for (int g = (c + 1) / 4; g < 8; ++g) {
+                    const float4 t4 = *reinterpret_cast<const float4 *>(&cb[4 * g]);
+                    const float tv[4] = {t4.x, t4.y, t4.z, t4.w};
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        if (4 * g + i > c) v[4 * g + i] = fmaf(-s, tv[i], v[4 * g + i]);
                 }
             }
             // L[lane][c] = a_{lane,c} / sqrt(d_c) (c < lane), L[lane][lane] = sqrt(d_lane)
             const float rs_me = rsqrtf(myd);
+            colb[64 + lane] = rs_me;
+            __syncwarp();
 #pragma unroll
-            for (int c = 0; c < 32; ++c) {
-                const float rs = __shfl_sync(0xffffffffu, rs_me, c);
-                v[c] = (c < lane) ? v[c] * rs : (c == lane ? myd * rs_me : 0.f);
+            for (int g = 0; g < 8; ++g) {
+                const float4 r4 = *reinterpret_cast<const float4 *>(&colb[64 + 4 * g]);
+                const float rv[4] = {r4.x, r4.y, r4.z, r4.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int c = 4 * g + i;
+                    v[c] = (c < lane) ? v[c] * rv[i] : (c == lane ? myd * rs_me : 0.f);
+                }
             }
             if (kb + lane < b) ratio = fminf(ratio, myd);
-            if (lane == 0 && bad) failed = 1;
+            if (lane == 0 && bad && !dry) failed = 1;
 #pragma unroll
             for (int c = 0; c < 32; ++c) {
-                if (c <= lane) sa[(kb + lane) * kLpLd + kb + c] = v[c];
+                if (c <= lane) sa[(kb + c) * kDgLd + kb + lane] = v[c];
                 slt[c * kDgLt + lane] = (lane > c) ? v[c] : 0.f;
             }
             rdiag[lane] = rs_me;
-        } else if (J > 0) {
+        } else if (J != 0) {
             // the previous panel's product for the columns right of this block
-            dg_syrk(sa, Pprev, kb + 32, kb + 32, kLpNb, tid - 32, kDgThreads - 32);
+            dg_syrk(sa, kb - 32, kb + 32, kb + 32, kLpNb, tid - 32, kDgThreads - 32);
         }
         if (J == 0) asm volatile("cp.async.wait_group 0;" ::: "memory");  // this thread's copies, columns 32-127
         __syncthreads();
-        if (failed) break;
+        if (failed && !dry) break;  // (`failed` is set at the first real step)
         const int w = kLpNb - kb - 32;  // rows below the diagonal block
         // (2) rows below: x L_JJ^T = a; rows of the identity: W_JJ
         if (tid < w + 32) {
@@ -200,7 +240,7 @@ __global__ void __launch_bounds__(kDgThreads) lowp_diag_kernel(float *L, int64_t
             const int r = ie < 0 ? kb + 32 + tid : 0;  // (row 0: any in-bounds address)
             float v[32];
 #pragma unroll
-            for (int c = 0; c < 32; ++c) v[c] = (ie < 0) ? sa[r * kLpLd + kb + c] : (c == ie ? 1.f : 0.f);
+            for (int c = 0; c < 32; ++c) v[c] = (ie < 0) ? sa[(kb + c) * kDgLd + r] : (c == ie ? 1.f : 0.f);
 #pragma unroll
             for (int c = 0; c < 32; ++c) {
                 v[c] *= rdiag[c];
@@ -215,23 +255,21 @@ __global__ void __launch_bounds__(kDgThreads) lowp_diag_kernel(float *L, int64_t
             }
             if (ie < 0) {
 #pragma unroll
-                for (int c = 0; c < 32; ++c) {
-                    sa[r * kLpLd + kb + c] = v[c];
-                    Pcur[c * kLpPd + r] = v[c];
-                }
+                for (int c = 0; c < 32; ++c) sa[(kb + c) * kDgLd + r] = v[c];
             } else {
 #pragma unroll
-                for (int c = 0; c < 32; ++c) Wd[kb * 32 + ie * 32 + c] = v[c];  // W[c][ie] at [J][ie][c]
+                for (int c = 0; c < 32; ++c)
+                    if (!dry) Wd[kb * 32 + ie * 32 + c] = v[c];  // W[c][ie] at [J][ie][c]
             }
         }
         __syncthreads();
         // (3) the next block's columns; the finished column block to HBM
         if (tid < 256) {
-            if (w > 0) dg_syrk(sa, Pcur, kb + 32, kb + 32, kb + 64, tid, 256);
+            if (w > 0) dg_syrk(sa, kb, kb + 32, kb + 32, kb + 64, tid, 256);
         } else {
-            for (int e = tid - 256; e < (kLpNb - kb) * 32; e += kDgThreads - 256) {
+            for (int e = tid - 256; e < (dry ? 0 : (kLpNb - kb) * 32); e += kDgThreads - 256) {
                 const int r = kb + e % (kLpNb - kb), c = kb + e / (kLpNb - kb);
-                if (r < b && c <= r) L[(p + r) + (p + c) * ld] = sa[r * kLpLd + c];
+                if (r < b && c <= r) L[(p + r) + (p + c) * ld] = sa[c * kDgLd + r];
             }
         }
         __syncthreads();
