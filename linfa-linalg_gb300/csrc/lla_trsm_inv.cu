@@ -179,6 +179,39 @@ constexpr int kIvYd = kIvNb + 2;  // words per staged column (padded: 528-byte c
 constexpr size_t kIvSmem = sizeof(float) * ((size_t)kIvStages * kIvNb * kIvLd + 2ull * kIvStages * kIvCols * kIvYd +
                                             2ull * kIvNb * kIvCols + 2ull * kIvCols * kIvLd);
 
+// t[j] += sign * sum_k A[k][ta] X[k][4 tb + j] over the 64 k of a block: four k
+// at a time with all their shared loads issued before the products, and two
+// partial sums per output (even and odd k), so the loop is neither a chain of
+// load latencies nor one long FMA chain.
+template <int SIGN, int XC>
+__device__ __forceinline__ void iv_dot64(float (&t)[4], const float (*A)[kIvLd], const float (*X)[XC], int ta,
+                                         int tb) {
+    float pe[4] = {0.f, 0.f, 0.f, 0.f}, po[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k0 = 0; k0 < kIvNb; k0 += 4) {
+        float l[4];
+        float4 x[4];
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+            l[kk] = A[k0 + kk][ta];
+            x[kk] = *reinterpret_cast<const float4 *>(&X[k0 + kk][tb * 4]);
+        }
+#pragma unroll
+        for (int kk = 0; kk < 4; kk += 2) {
+            pe[0] = fmaf(l[kk], x[kk].x, pe[0]);
+            pe[1] = fmaf(l[kk], x[kk].y, pe[1]);
+            pe[2] = fmaf(l[kk], x[kk].z, pe[2]);
+            pe[3] = fmaf(l[kk], x[kk].w, pe[3]);
+            po[0] = fmaf(l[kk + 1], x[kk + 1].x, po[0]);
+            po[1] = fmaf(l[kk + 1], x[kk + 1].y, po[1]);
+            po[2] = fmaf(l[kk + 1], x[kk + 1].z, po[2]);
+            po[3] = fmaf(l[kk + 1], x[kk + 1].w, po[3]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) t[j] = SIGN > 0 ? t[j] + (pe[j] + po[j]) : t[j] - (pe[j] + po[j]);
+}
+
 // TRANS = false: L Y = B (blocks ascending); TRANS = true: L^T X = B (descending).
 // 256 threads.  The coupling tiles and the solved words of earlier blocks
 // stream through a kIvStages-deep cp.async ring.  Each thread validates the
@@ -446,15 +479,7 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
     }
     __syncthreads();
     float t[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 8
-    for (int k = 0; k < kIvNb; ++k) {
-        const float l = sK[k][ta];
-        const float4 x = *reinterpret_cast<const float4 *>(&sX[k][tb * 4]);
-        t[0] = fmaf(l, x.x, t[0]);
-        t[1] = fmaf(l, x.y, t[1]);
-        t[2] = fmaf(l, x.z, t[2]);
-        t[3] = fmaf(l, x.w, t[3]);
-    }
+    iv_dot64<1>(t, sK, sX, ta, tb);
     // 3. t -= M2_r x_second_neighbour, then t -= M_r x_neighbour; M_r, M2_r
     // (F_r^1, F_r^2 or G_r^1, G_r^2) stored as plain coefficient matrices
     if (pb > 1) {
@@ -466,22 +491,14 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
             const int64_t gk = qn2 * kIvNb + ta, col = col0 + tb + 4 * u;
             p[u] = (gk < n && col < m) ? ll + gk + col * ldl : nullptr;
         }
+#pragma unroll
+        for (int u = 0; u < LPT; ++u) sM[tb + 4 * u][ta] = preM2[u];  // before the wait: off the critical path
         iv_settle4(wy2, p, tag, err_word, &s_abort);
 #pragma unroll
         for (int u = 0; u < 4; ++u) sN[ta][tb + 4 * u] = p[u] ? __uint_as_float((unsigned)wy2[u]) : 0.f;
-#pragma unroll
-        for (int u = 0; u < LPT; ++u) sM[tb + 4 * u][ta] = preM2[u];
         __syncthreads();
         if (s_abort) return;
-#pragma unroll 8
-        for (int k = 0; k < kIvNb; ++k) {
-            const float l = sM[k][ta];
-            const float4 x = *reinterpret_cast<const float4 *>(&sN[k][tb * 4]);
-            t[0] = fmaf(-l, x.x, t[0]);
-            t[1] = fmaf(-l, x.y, t[1]);
-            t[2] = fmaf(-l, x.z, t[2]);
-            t[3] = fmaf(-l, x.w, t[3]);
-        }
+        iv_dot64<-1>(t, sM, sN, ta, tb);
     }
     if (pb > 0) {
         float(*sM)[kIvLd] = sT[1];
@@ -492,22 +509,14 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
             const int64_t gk = qn * kIvNb + ta, col = col0 + tb + 4 * u;
             p[u] = (gk < n && col < m) ? ll + gk + col * ldl : nullptr;
         }
+#pragma unroll
+        for (int u = 0; u < LPT; ++u) sM[tb + 4 * u][ta] = preM[u];  // M[i = ta][k = tb + 4u], before the wait
         iv_settle4(wy, p, tag, err_word, &s_abort);
 #pragma unroll
         for (int u = 0; u < 4; ++u) sN[ta][tb + 4 * u] = p[u] ? __uint_as_float((unsigned)wy[u]) : 0.f;
-#pragma unroll
-        for (int u = 0; u < LPT; ++u) sM[tb + 4 * u][ta] = preM[u];  // M[i = ta][k = tb + 4u]
         __syncthreads();
         if (s_abort) return;
-#pragma unroll 8
-        for (int k = 0; k < kIvNb; ++k) {
-            const float l = sM[k][ta];
-            const float4 x = *reinterpret_cast<const float4 *>(&sN[k][tb * 4]);
-            t[0] = fmaf(-l, x.x, t[0]);
-            t[1] = fmaf(-l, x.y, t[1]);
-            t[2] = fmaf(-l, x.z, t[2]);
-            t[3] = fmaf(-l, x.w, t[3]);
-        }
+        iv_dot64<-1>(t, sM, sN, ta, tb);
     }
     // 4. publish
 #pragma unroll
@@ -667,15 +676,7 @@ __global__ void __launch_bounds__(256, 2) trsm_chain_kernel(const float *__restr
                 if (p < d) continue;
                 const float(*M)[kIvLd] = sM[buf][d - 1];
                 const float(*Y)[C] = syv[(p - d) & 1];
-#pragma unroll 8
-                for (int k = 0; k < kIvNb; ++k) {
-                    const float l = M[k][ta];
-                    const float4 x = *reinterpret_cast<const float4 *>(&Y[k][tb * 4]);
-                    t[0] = fmaf(-l, x.x, t[0]);
-                    t[1] = fmaf(-l, x.y, t[1]);
-                    t[2] = fmaf(-l, x.z, t[2]);
-                    t[3] = fmaf(-l, x.w, t[3]);
-                }
+                iv_dot64<-1>(t, M, Y, ta, tb);
             }
             __syncthreads();  // every read of y_{p-2} is done: its buffer takes y_p
             // 3. publish y_p
@@ -864,15 +865,7 @@ __global__ void __launch_bounds__(256, 2) trsm_chain_kernel(const float *__restr
     }
     __syncthreads();
     float t[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 8
-    for (int k = 0; k < kIvNb; ++k) {
-        const float l = sK[k][ta];
-        const float4 x = *reinterpret_cast<const float4 *>(&sX[k][tb * 4]);
-        t[0] = fmaf(l, x.x, t[0]);
-        t[1] = fmaf(l, x.y, t[1]);
-        t[2] = fmaf(l, x.z, t[2]);
-        t[3] = fmaf(l, x.w, t[3]);
-    }
+    iv_dot64<1>(t, sK, sX, ta, tb);
     // 3. publish the partial sum for the chain
     {
         const int64_t grow = rb * kIvNb + ta;
