@@ -58,7 +58,7 @@ __device__ __forceinline__ void lp_cp_wait_all() { asm volatile("cp.async.wait_a
 constexpr int kDgThreads = 512;
 constexpr int kDgLd = kLpNb + 4;  // column stride of the block in shared memory (16-byte columns)
 constexpr int kDgLt = 36;         // row stride of a transposed 32 x 32 factor (16-byte rows)
-constexpr size_t kDgSmem = sizeof(float) * (kLpNb * kDgLd + 32 * kDgLt + 3 * 32);
+constexpr size_t kDgSmem = sizeof(float) * (kLpNb * kDgLd + 32 * kDgLt + 5 * 32);
 
 __device__ __forceinline__ float dg_rcp(float x) {
     float r;
@@ -108,10 +108,11 @@ __device__ __forceinline__ void dg_syrk(float *sa, int k0, int r0, int c0, int c
 // Right-looking by 32-column blocks J with a look-ahead inside the block:
 //   (1) warp 0 factors the 32 x 32 diagonal block (lane i holds row i in
 //       registers) without square roots on the pivot chain: with d_c the
-//       pivot, a_ij -= (a_ic / d_c) a_jc; column c reaches every lane through
-//       shared memory (one store, four-wide broadcast loads), so the chain
-//       between pivots is a store, a load, a reciprocal, a multiply and an
-//       FMA; the columns are scaled by 1/sqrt(d_c) afterwards.  Meanwhile
+//       pivot, a_ij -= (a_ic / d_c) a_jc.  Columns go through shared memory
+//       two at a time (one store, four-wide broadcast loads) and every lane
+//       forms the second pivot of the pair itself, so one store, barrier and
+//       load serve two pivots; the columns are scaled by 1/sqrt(d_c)
+//       afterwards.  Meanwhile
 //       warps 1-15 subtract the previous block's panel from the columns right
 //       of the next block;
 //   (2) the rows below solve x L_JJ^T = a, and 32 more threads solve the rows
@@ -132,8 +133,8 @@ __global__ void __launch_bounds__(kDgThreads) lowp_diag_kernel(float *L, int64_t
                                                                int64_t *info, double *min_ratio, float *Wd) {
     extern __shared__ __align__(16) float sa[];  // sa[c * kDgLd + r] = A11[r][c]
     float *slt = sa + kLpNb * kDgLd;              // slt[c * kDgLt + c2] = L_JJ[c2][c] for c2 > c, else 0
-    float *colb = slt + 32 * kDgLt;               // two column buffers of the factor, then 1/sqrt(d)
-    __shared__ float rdiag[32];                   // 1 / L_JJ[c][c]
+    float *colb = slt + 32 * kDgLt;               // two pairs of column buffers, then 1/sqrt(d)
+    __shared__ __align__(16) float rdiag[32];     // 1 / L_JJ[c][c]
     __shared__ int failed, skip;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const bool v16 = b == kLpNb && ld % 4 == 0 && (reinterpret_cast<uintptr_t>(L) & 15) == 0;
@@ -186,31 +187,48 @@ __global__ void __launch_bounds__(kDgThreads) lowp_diag_kernel(float *L, int64_t
             for (int c = 0; c < 32; ++c) v[c] = (c <= lane) ? sa[(kb + c) * kDgLd + kb + lane] : 0.f;
             bool bad = false;
             float myd = 1.f;  // this lane's pivot d_lane
+            // Two columns per round: both go to shared memory together, every lane
+            // forms the 2 x 2 pivot block's recurrence itself (d_{c+1} after column
+            // c's update) and the column c + 1 entries it needs, so one store,
+            // barrier and load serve two pivots.
 #pragma unroll
-            for (int c = 0; c < 32; ++c) {
-                float *cb = colb + (c & 1) * 32;  // column c of every lane (two buffers: no reuse hazard)
-                cb[lane] = v[c];
+            for (int c = 0; c < 32; c += 2) {
+                float *cb0 = colb + ((c >> 1) & 1) * 64, *cb1 = cb0 + 32;  // two buffer pairs: no reuse hazard
+                cb0[lane] = v[c];
+                cb1[lane] = v[c + 1];
                 __syncwarp();
-                const float d = cb[c];
-                bad |= !(d > 0.f);  // non-positive (or NaN) pivot: breakdown
-                myd = (lane == c) ? d : myd;
-                const float s = v[c] * dg_rcp(d);  // a_{lane,c} / d_c
+                const float a00 = cb0[c], a10 = cb0[c + 1], a11 = cb1[c + 1];
+                const float r0 = dg_rcp(a00);
+                const float d1 = fmaf(-(a10 * r0), a10, a11);  // pivot c + 1 after column c's update
+                const float r1 = dg_rcp(d1);
+                bad |= !(a00 > 0.f) || !(d1 > 0.f);  // non-positive (or NaN) pivot: breakdown
+                myd = (lane == c) ? a00 : ((lane == c + 1) ? d1 : myd);
+                const float s0 = v[c] * r0;                // l_{lane,c}
+                const float u = fmaf(-s0, a10, v[c + 1]);  // a_{lane,c+1} after column c
+                v[c + 1] = u;
+                const float s1 = u * r1;  // l_{lane,c+1}
 #pragma unroll
-                for (int g = (c + 1) / 4; g < 8; ++g) {
-                    const float4 t4 = *reinterpret_cast<const float4 *>(&cb[4 * g]);
-                    const float tv[4] = {t4.x, t4.y, t4.z, t4.w};
+                for (int g = (c + 2) / 4; g < 8; ++g) {
+                    const float4 t0 = *reinterpret_cast<const float4 *>(&cb0[4 * g]);
+                    const float4 t1 = *reinterpret_cast<const float4 *>(&cb1[4 * g]);
+                    const float tv0[4] = {t0.x, t0.y, t0.z, t0.w}, tv1[4] = {t1.x, t1.y, t1.z, t1.w};
 #pragma unroll
-                    for (int i = 0; i < 4; ++i)
-                        if (4 * g + i > c) v[4 * g + i] = fmaf(-s, tv[i], v[4 * g + i]);
+                    for (int i = 0; i < 4; ++i) {
+                        const int c2 = 4 * g + i;
+                        if (c2 > c + 1) {
+                            const float w1 = fmaf(-(tv0[i] * r0), a10, tv1[i]);  // a_{c2,c+1} after column c
+                            v[c2] = fmaf(-s1, w1, fmaf(-s0, tv0[i], v[c2]));
+                        }
+                    }
                 }
             }
             // L[lane][c] = a_{lane,c} / sqrt(d_c) (c < lane), L[lane][lane] = sqrt(d_lane)
             const float rs_me = rsqrtf(myd);
-            colb[64 + lane] = rs_me;
+            colb[128 + lane] = rs_me;
             __syncwarp();
 #pragma unroll
             for (int g = 0; g < 8; ++g) {
-                const float4 r4 = *reinterpret_cast<const float4 *>(&colb[64 + 4 * g]);
+                const float4 r4 = *reinterpret_cast<const float4 *>(&colb[128 + 4 * g]);
                 const float rv[4] = {r4.x, r4.y, r4.z, r4.w};
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
@@ -238,12 +256,17 @@ __global__ void __launch_bounds__(kDgThreads) lowp_diag_kernel(float *L, int64_t
         if (tid < w + 32) {
             const int ie = tid - w;                  // identity row, when >= 0
             const int r = ie < 0 ? kb + 32 + tid : 0;  // (row 0: any in-bounds address)
-            float v[32];
+            float v[32], rd[32];
 #pragma unroll
             for (int c = 0; c < 32; ++c) v[c] = (ie < 0) ? sa[(kb + c) * kDgLd + r] : (c == ie ? 1.f : 0.f);
 #pragma unroll
+            for (int g = 0; g < 8; ++g) {  // the reciprocal diagonal in registers: off the chain
+                const float4 r4 = *reinterpret_cast<const float4 *>(&rdiag[4 * g]);
+                rd[4 * g] = r4.x, rd[4 * g + 1] = r4.y, rd[4 * g + 2] = r4.z, rd[4 * g + 3] = r4.w;
+            }
+#pragma unroll
             for (int c = 0; c < 32; ++c) {
-                v[c] *= rdiag[c];
+                v[c] *= rd[c];
 #pragma unroll
                 for (int g = (c + 1) / 4; g < 8; ++g) {
                     const float4 l4 = *reinterpret_cast<const float4 *>(&slt[c * kDgLt + 4 * g]);
