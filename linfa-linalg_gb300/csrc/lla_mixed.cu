@@ -428,12 +428,16 @@ __global__ void refine_begin_kernel(double *words) {
 }
 
 // eta = max_j ||r_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf); converged when
-// eta <= tol; stalled when eta is not finite, or does not halve over an
-// iteration after the second, or max_iters ran out.  While refining, the
-// column maxima of |r| and |x| are cleared for the next iteration.
-__global__ void __launch_bounds__(256) refine_check_kernel(double *words, int64_t m, double tol, int max_iters) {
+// eta <= tol (from a full-level residual: with the exact-slice residual the
+// levels of this iteration follow refine_levels); stalled when eta is not
+// finite, or does not halve over an iteration after the second, or max_iters
+// ran out.  While refining, the column maxima of |r| and |x| are cleared for
+// the next iteration.
+__global__ void __launch_bounds__(256) refine_check_kernel(double *words, int64_t m, double tol, int max_iters,
+                                                           int slices) {
     int *st = (int *)(words + 4);
     if (*(volatile int *)st != 0) return;
+    const bool coarse = slices && refine_levels(st) < 8;  // before this iteration's updates below
     __shared__ double red[8];
     __shared__ int s_go;
     const int tid = threadIdx.x;
@@ -456,7 +460,7 @@ __global__ void __launch_bounds__(256) refine_check_kernel(double *words, int64_
         words[5] = e;
         if (it == 1) words[7] = e;
         int state = 0;
-        if (e <= tol)
+        if (e <= tol && !coarse)
             state = 1;
         else if (!isfinite(e) || (it >= 3 && e > 0.5 * words[6]) || it >= max_iters)
             state = 2;
@@ -477,9 +481,9 @@ int refine_begin_launch(double *words, cudaStream_t st) {
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int refine_check_launch(double *words, int64_t m, double tol, int max_iters, cudaStream_t st) {
+int refine_check_launch(double *words, int64_t m, double tol, int max_iters, cudaStream_t st, bool slices) {
     LaunchScope ls(K_MISC, st);
-    refine_check_kernel<<<1, 256, 0, st>>>(words, m, tol, max_iters);
+    refine_check_kernel<<<1, 256, 0, st>>>(words, m, tol, max_iters, slices ? 1 : 0);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -728,7 +732,7 @@ extern "C" int lla_dposv_refined_device(const double *dA, int64_t n, int64_t lda
             else
                 MX_TRY(last_err(residual_launch(dA, lda, n, dX, ldx, dB, ldb, R, n, m, colmax_r,
                                                 (double *)w.P.p, st, state)));
-            MX_TRY(last_err(refine_check_launch(words, m, opts.tol, opts.max_iters, st)));
+            MX_TRY(last_err(refine_check_launch(words, m, opts.tol, opts.max_iters, st, slices)));
         }
         MX_TRY(cudaEventRecord(w.ev[2], st));
         MX_TRY(read_words(8));

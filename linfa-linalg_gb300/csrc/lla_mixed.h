@@ -29,6 +29,22 @@ int equilibrate_launch(const double *A, int64_t lda, int64_t n, bool scale, doub
 __device__ __forceinline__ bool refine_done(const int *state) {
     return state != nullptr && *(volatile const int *)state != 0;
 }
+// Levels of the exact-slice residual of the current refinement iteration.
+// The residual only has to resolve the error that is left: while the previous
+// iteration's backward error is above kOzCoarseEta (and for the first
+// residual) six levels (dropped terms below 2^-49 of the row and column
+// scales) suffice, after that all eight.  The convergence test accepts only a
+// residual formed with all eight (refine_check_kernel evaluates the same rule).
+// Outside a refinement (state == nullptr) always eight.  state points at
+// words + 4 of the refinement control block: [0] state, [1] iterations done,
+// and the double after it is the previous iteration's backward error.
+constexpr double kOzCoarseEta = 1e-11;
+__device__ __forceinline__ int refine_levels(const int *state) {
+    if (state == nullptr) return 8;
+    const int done = *(volatile const int *)(state + 1);
+    const double eta_prev = *(volatile const double *)((const double *)state + 1);
+    return (done == 0 || !(eta_prev <= kOzCoarseEta)) ? 6 : 8;
+}
 int colmax_launch(const double *M, int64_t ld, int64_t n, int64_t m, double *colmax, cudaStream_t st);
 // R = B - A_sym X in FP64; P: workspace of residual_splits(n, m) * n * m
 // doubles for the split-K partials (NULL: no split).

@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) oz_residual_kernel(
     // uniform for the CTA: nothing below (barriers, tensor memory) is touched
     if (refine_done(state)) return;
     extern __shared__ uint8_t smem_raw[];
-    __shared__ int s_abort;
+    __shared__ int s_abort, s_levels;
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *sA = smem;                              // kOzAStages x 16 KiB
     uint8_t *sX = smem + kOzAStages * kOzATile;      // 2 x 64 KiB
@@ -235,6 +235,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) oz_residual_kernel(
         for (int h = 0; h < 2; ++h) mbar_init(tempty0 + 8 * h, 256);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
+        s_levels = refine_levels(state);  // levels kept this iteration (6 or 8), the same in every CTA
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -252,6 +253,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) oz_residual_kernel(
 
     if (warp == 8) {
         if (lane == 0) {  // TMA producer
+            const int S = s_levels;
             int64_t ga = 0;
             for (int kc = kc_beg, j = 0; kc < kc_end && !*(volatile int *)&s_abort; ++kc, ++j) {
                 const int xb = j & 1, use = j >> 1;
@@ -261,7 +263,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) oz_residual_kernel(
                 }
                 mbar_expect_tx(fullX0 + 8 * xb, kOzXSet);
                 tma_load_3d(smem_u32(sX + xb * kOzXSet), &tmX, kc * kOzK, 0, 0, fullX0 + 8 * xb);
-                for (int p = 0; p < kOzS; ++p, ++ga) {
+                for (int p = 0; p < S; ++p, ++ga) {
                     const int s = (int)(ga % kOzAStages);
                     const int64_t round = ga / kOzAStages;
                     if (round > 0 && !mbar_wait(emptyA0 + 8 * s, (uint32_t)((round - 1) & 1), err_word)) {
@@ -275,6 +277,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) oz_residual_kernel(
         }
     } else if (warp == 9) {
         if (lane == 0) {  // MMA issuer
+            const int S = s_levels;
             int64_t ga = 0;
             int win = 0;
             for (int kc = kc_beg, j = 0; kc < kc_end && !*(volatile int *)&s_abort; ++kc, ++j) {
@@ -286,7 +289,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) oz_residual_kernel(
                 }
                 tc_fence_after();
                 const uint32_t x0 = smem_u32(sX + xb * kOzXSet);
-                for (int p = 0; p < kOzS; ++p, ++ga) {
+                for (int p = 0; p < S; ++p, ++ga) {
                     const int s = (int)(ga % kOzAStages);
                     if (!mbar_wait(fullA0 + 8 * s, (uint32_t)((ga / kOzAStages) & 1), err_word)) {
                         s_abort = 1;
@@ -298,7 +301,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) oz_residual_kernel(
                     // the levels p+q0 .. p+q1-1 consecutive 64-column accumulators
                     const uint64_t ad = sw128_desc(smem_u32(sA + s * kOzATile));
                     for (int h = 0; h < 2; ++h) {
-                        const int q0 = 4 * h, q1 = min(4 * h + 4, kOzS - p);
+                        const int q0 = 4 * h, q1 = min(4 * h + 4, S - p);
                         if (q0 >= q1) break;
                         // first product of a window into these levels: wait until the
                         // epilogue has read them out of the previous window
@@ -348,7 +351,12 @@ __global__ void __launch_bounds__(kOzThreads, 1) oz_residual_kernel(
 #pragma unroll 1
             for (int d = 0; d < kOzS; ++d) {
                 uint32_t v[32];
-                tc_ld32(tmem + (uint32_t)(d * kOzN) + ((uint32_t)(qw * 32) << 16) + (uint32_t)(half * 32), v);
+                if (d < *(volatile int *)&s_levels) {  // uniform: the levels formed this iteration
+                    tc_ld32(tmem + (uint32_t)(d * kOzN) + ((uint32_t)(qw * 32) << 16) + (uint32_t)(half * 32), v);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) v[c] = 0u;
+                }
                 if ((d & 3) == 3) {  // levels d-3 .. d read out
                     tc_fence_before();
                     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tempty0 + 8 * (d >> 2)) : "memory");
