@@ -30,20 +30,25 @@ __device__ __forceinline__ bool refine_done(const int *state) {
     return state != nullptr && *(volatile const int *)state != 0;
 }
 // Levels of the exact-slice residual of the current refinement iteration.
-// The residual only has to resolve the error that is left: while the previous
-// iteration's backward error is above kOzCoarseEta (and for the first
-// residual) six levels (dropped terms below 2^-49 of the row and column
-// scales) suffice, after that all eight.  The convergence test accepts only a
-// residual formed with all eight (refine_check_kernel evaluates the same rule).
-// Outside a refinement (state == nullptr) always eight.  state points at
-// words + 4 of the refinement control block: [0] state, [1] iterations done,
-// and the double after it is the previous iteration's backward error.
-constexpr double kOzCoarseEta = 1e-11;
+// The residual only has to resolve the error that is left.  Dropping levels
+// d >= S leaves an error of about (S+1) 2^-7S per product relative to the row
+// and column scales, ~2^-7S+4 sqrt(n) summed over a row: for S = 6 about
+// 2e-10 and for S = 7 about 2e-12 of the scales at n = 16384, one to two
+// orders below the backward error they are used at.  So: all eight for the
+// first residual (the first solve may already be accurate), six while the
+// previous backward error is above 1e-9, seven while it is above 1e-11,
+// eight after; the convergence test accepts only a residual formed with all
+// eight (refine_check_kernel evaluates the same rule).  Outside a refinement
+// (state == nullptr) always eight.  state points at words + 4 of the
+// refinement control block: [0] state, [1] iterations done, and the double
+// after it is the previous iteration's backward error.
+constexpr double kOzEta6 = 1e-9, kOzEta7 = 1e-11;
 __device__ __forceinline__ int refine_levels(const int *state) {
     if (state == nullptr) return 8;
     const int done = *(volatile const int *)(state + 1);
     const double eta_prev = *(volatile const double *)((const double *)state + 1);
-    return (done == 0 || !(eta_prev <= kOzCoarseEta)) ? 6 : 8;
+    if (done == 0 || eta_prev <= kOzEta7) return 8;
+    return eta_prev <= kOzEta6 ? 7 : 6;  // (a NaN backward error stops the refinement first)
 }
 int colmax_launch(const double *M, int64_t ld, int64_t n, int64_t m, double *colmax, cudaStream_t st);
 // R = B - A_sym X in FP64; P: workspace of residual_splits(n, m) * n * m

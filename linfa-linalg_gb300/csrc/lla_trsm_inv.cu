@@ -328,22 +328,32 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
     // zero-filled by the copy).
     static_assert(YCH == 2, "a thread settles the four words of its two copies together");
     auto settle_stage = [&](int64_t pi, int s, int buf) {
-        const int64_t pq = q_lo + pi;
-        const int64_t qb = TRANS ? R - 1 - pq : pq;
         unsigned long long w[4];
-        const unsigned long long *p[4];
+        bool tagged = true;  // the usual case: every copied word was already published
 #pragma unroll
         for (int j = 0; j < YCH; ++j) {
             const int e = tid + 256 * j, c = e >> 5, kp = e & 31;
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const int k = 2 * kp + h;
-                const int64_t gk = qb * kIvNb + k, col = col0 + c;
-                w[2 * j + h] = sY[s][c][k];
-                p[2 * j + h] = (gk < n && col < m) ? ll + gk + col * ldl : nullptr;
+                w[2 * j + h] = sY[s][c][2 * kp + h];
+                tagged &= (w[2 * j + h] & 0xffffffff00000000ull) == tag;
             }
         }
-        iv_settle4(w, p, tag, err_word, &s_abort);
+        if (!tagged) {  // late words (or words past n or m, which are never tagged): poll those
+            const int64_t pq = q_lo + pi;
+            const int64_t qb = TRANS ? R - 1 - pq : pq;
+            const unsigned long long *p[4];
+#pragma unroll
+            for (int j = 0; j < YCH; ++j) {
+                const int e = tid + 256 * j, c = e >> 5, kp = e & 31;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int64_t gk = qb * kIvNb + 2 * kp + h, col = col0 + c;
+                    p[2 * j + h] = (gk < n && col < m) ? ll + gk + col * ldl : nullptr;
+                }
+            }
+            iv_settle4(w, p, tag, err_word, &s_abort);
+        }
 #pragma unroll
         for (int j = 0; j < YCH; ++j) {
             const int e = tid + 256 * j, c = e >> 5, kp = e & 31;
