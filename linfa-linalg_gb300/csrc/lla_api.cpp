@@ -243,6 +243,20 @@ void gather_scatter(const View &v, char *stage, bool gather) {
 
 // Copies a host view into `raw` (device).  On return (drs, dcs) describe the
 // raw layout: column-major (1, rows) or row-major (cols, 1).
+// The device address of a contiguous view in page-locked host memory that is
+// mapped into the device's address space (cudaHostAlloc / pinned tensors), or
+// nullptr: kernels can then read the view in place over the host link
+// instead of from a staged device copy.
+const void *mapped_alias(const View &v) {
+    if (!(colmajor_contig(v) || rowmajor_contig(v))) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, v.p) != cudaSuccess) {
+        cudaGetLastError();  // not a pointer the runtime knows: clear the error
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 cudaError_t upload(Ctx &c, const View &v, DevBuf &raw, HostBuf &stage, int64_t &drs, int64_t &dcs) {
     const size_t bytes = (size_t)(v.rows * v.cols) * v.esz;
     cudaError_t e = raw.ensure(bytes);
@@ -770,11 +784,19 @@ int lla_dposv_refined(const double *a, int64_t rows, int64_t cols, int64_t rs, i
     if (!c) return err ? err->code : LLA_ERR_NO_DEVICE;
     View va{(char *)a, rows, cols, rs, cs, sizeof(double)};
     int64_t ars, acs;
-    LLA_TRY_CUDA(upload(*c, va, c->raw_a, c->stage_a, ars, acs));
+    // A in mapped page-locked memory is read in place by the import kernel (one
+    // pass over the host link instead of a staging copy followed by a device pass)
+    const double *src = (const double *)mapped_alias(va);
+    if (src) {
+        ars = colmajor_contig(va) ? 1 : n;
+        acs = colmajor_contig(va) ? n : 1;
+    } else {
+        LLA_TRY_CUDA(upload(*c, va, c->raw_a, c->stage_a, ars, acs));
+        src = (const double *)c->raw_a.p;
+    }
     LLA_TRY_CUDA(c->work_a.ensure(sizeof(double) * n * n));
     double *W = (double *)c->work_a.p;
-    LLA_TRY_CUDA(launch_status(
-        import_launch<double>((const double *)c->raw_a.p, ars, acs, n, n, W, n, c->stream)));
+    LLA_TRY_CUDA(launch_status(import_launch<double>(src, ars, acs, n, n, W, n, c->stream)));
     View vb{(char *)b, brows, bcols, brs, bcs, sizeof(double)};
     int64_t drs, dcs;
     LLA_TRY_CUDA(upload(*c, vb, c->raw_b, c->stage_b, drs, dcs));

@@ -138,6 +138,28 @@ def test_device_form_matches_host_form(gpu_lla):
     assert np.array_equal(X.cpu().numpy(), x)
 
 
+@pytest.mark.parametrize("order", ["C", "F"])
+def test_pinned_host_input_read_in_place(gpu_lla, order):
+    """A in page-locked host memory is read in place by the import kernel (no
+    staging copy); the result is bit-identical to the pageable-memory path."""
+    torch = pytest.importorskip("torch")
+    lla = gpu_lla
+    rng = np.random.default_rng(12)
+    n, m = 700, 3
+    a = qdq(rng, n, 1e4)
+    b = rng.standard_normal((n, m))
+    ap = torch.empty((n, n), dtype=torch.float64, pin_memory=True).numpy()
+    if order == "F":
+        ap = ap.T  # a column-major view of the pinned buffer
+    ap[...] = a
+    x1, x2 = b.copy(), b.copy()
+    r1 = lla.posv_refined(ap, x1)
+    r2 = lla.posv_refined(np.array(a, order=order), x2)
+    assert r1["converged"] == 1 and r1["iterations"] == r2["iterations"]
+    assert np.array_equal(x1, x2)
+    assert np.array_equal(ap, a)  # A is only read
+
+
 # accuracy of the low-precision factorisation alone: ||L L^T - A|| / ||A||
 # bounds per update form (FP32 panels; the split forms are FP32-accurate)
 FACTOR_TOL = {"fp32": 2e-6, "fp16x3": 4e-6, "bf16x6": 4e-6, "bf16x3": 3e-5, "fp16": 3e-3,
