@@ -384,3 +384,46 @@ def test_refine_autotune_records_and_reuses(gpu_lla, tmp_path, monkeypatch):
     want = (chosen["update_kchunk"] << 8) | (chosen["update_epilogue"] << 4) | chosen["substitution"]
     assert rep["schedule"] == want and rep["converged"] == 1
     assert backward_error(a, X.cpu().numpy(), b) <= 2e-13
+
+
+def test_concurrent_solves_on_two_streams_match_alone(gpu_lla):
+    """Two refined solves from two host threads (each its own stream and
+    workspace) overlap on the device: the persistent update kernels then share
+    the SMs and claim their tiles from their own counters.  Each result is
+    bit-identical to the same solve run alone."""
+    import threading
+    torch = pytest.importorskip("torch")
+    lla = gpu_lla
+    rng = np.random.default_rng(31)
+    systems = []
+    for n in (2200, 1700):
+        a = qdq(rng, n, 1e5)
+        b = rng.standard_normal((n, 3))
+        A = torch.tensor(a, device="cuda").T.contiguous().T
+        B = torch.tensor(b, device="cuda").T.contiguous().T
+        systems.append((A, B))
+    alone = []
+    for A, B in systems:
+        X = torch.empty_like(B.T.contiguous()).T
+        lla.posv_refined_device(A, B, X)
+        torch.cuda.synchronize()
+        alone.append(X.cpu().numpy())
+    outs = [None, None]
+
+    def run(i):
+        A, B = systems[i]
+        st = torch.cuda.Stream()
+        X = torch.empty_like(B.T.contiguous()).T
+        for _ in range(3):  # several rounds so that the solves do overlap
+            with torch.cuda.stream(st):
+                lla.posv_refined_device(A, B, X, stream=st)
+        st.synchronize()
+        outs[i] = X.cpu().numpy()
+
+    th = [threading.Thread(target=run, args=(i,)) for i in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for i in range(2):
+        assert np.array_equal(outs[i], alone[i])
