@@ -128,7 +128,9 @@ __device__ __forceinline__ void dg_syrk(float *sa, int k0, int r0, int c0, int c
 // cache, and its unrolled steps are tens of KB of code: a first pass of the
 // step loop (J = -1) runs on the uninitialised shared memory, with every
 // global store off, while the previous kernel still finishes (before
-// pdl_wait), so the real passes run from a warm cache.
+// pdl_wait), so the real passes run from a warm cache; its phases run side
+// by side without barriers (warp 0 the pivots, the others the solves and
+// updates), so it takes about as long as its longest phase.
 __global__ void __launch_bounds__(kDgThreads) lowp_diag_kernel(float *L, int64_t ld, int64_t p, int b,
                                                                int64_t *info, double *min_ratio, float *Wd) {
     extern __shared__ __align__(16) float sa[];  // sa[c * kDgLd + r] = A11[r][c]
@@ -143,6 +145,7 @@ __global__ void __launch_bounds__(kDgThreads) lowp_diag_kernel(float *L, int64_t
     for (int J = -1; J < 4; ++J) {
         const bool dry = J < 0;  // the warm-up pass: step 1's code, nothing stored globally
         if (J == 0) {
+            __syncthreads();  // the warm-up pass has left shared memory
             pdl_wait();  // the block comes from the update just before
             pdl_trigger();
             // the lower triangle in two copy groups: columns 0-31 (the first step), then the rest
@@ -249,7 +252,7 @@ __global__ void __launch_bounds__(kDgThreads) lowp_diag_kernel(float *L, int64_t
             dg_syrk(sa, kb - 32, kb + 32, kb + 32, kLpNb, tid - 32, kDgThreads - 32);
         }
         if (J == 0) asm volatile("cp.async.wait_group 0;" ::: "memory");  // this thread's copies, columns 32-127
-        __syncthreads();
+        if (!dry) __syncthreads();  // (the warm-up pass runs its phases side by side: its data is discarded)
         if (failed && !dry) break;  // (`failed` is set at the first real step)
         const int w = kLpNb - kb - 32;  // rows below the diagonal block
         // (2) rows below: x L_JJ^T = a; rows of the identity: W_JJ
@@ -285,7 +288,7 @@ __global__ void __launch_bounds__(kDgThreads) lowp_diag_kernel(float *L, int64_t
                     if (!dry) Wd[kb * 32 + ie * 32 + c] = v[c];  // W[c][ie] at [J][ie][c]
             }
         }
-        __syncthreads();
+        if (!dry) __syncthreads();
         // (3) the next block's columns; the finished column block to HBM
         if (tid < 256) {
             if (w > 0) dg_syrk(sa, kb, kb + 32, kb + 32, kb + 64, tid, 256);
@@ -295,7 +298,7 @@ __global__ void __launch_bounds__(kDgThreads) lowp_diag_kernel(float *L, int64_t
                 if (r < b && c <= r) L[(p + r) + (p + c) * ld] = sa[c * kDgLd + r];
             }
         }
-        __syncthreads();
+        if (!dry) __syncthreads();
     }
     if (failed) {
         if (tid == 0) *info = p;  // the low-precision factorisation broke down in this panel
