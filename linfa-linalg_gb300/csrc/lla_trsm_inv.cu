@@ -9,11 +9,14 @@
 // and every substitution is a chain of small matrix products:
 //     forward  L Y = B  : Y_r = W_r (B_r - sum_{q<r-2} L_rq Y_q) - F_r^2 Y_{r-2} - F_r^1 Y_{r-1}
 //     backward L^T X = Y: X_r = W_r^T (Y_r - sum_{q>r+2} L_qr^T X_q) - G_r^2 X_{r+2} - G_r^1 X_{r+1}
-// One CTA per (64-row block, 16-column chunk); CTAs take tickets in
+// One owner CTA per (64-row block, 16-column chunk); CTAs take tickets in
 // processing order.  The sum over blocks solved three or more steps earlier
 // and its product with W_r are formed while the two previous blocks are
 // still being solved, the second neighbour's term while the first is, so the
 // only work on the block-to-block critical path is one 64 x 64 x 16 product.
+// An owner sums at most the last kIvOwn of those coupling terms itself; wide
+// helper CTAs sum the earlier ones in groups of kIvGroup positions for 64
+// columns at a time (lla_trsm_sched.h gives the ticket order).
 //
 // Hand-off between CTAs: a solved value is published as one 64-bit word
 // (launch epoch << 32 | float bits) in a staging array, so a consumer polls
@@ -148,7 +151,12 @@ __device__ __forceinline__ void iv_wait() {
 
 // Bounded re-read of up to four hand-off words (p[u] == nullptr: none)
 // until each carries this launch's tag; the words are re-read together, so a
-// hand-off costs one memory round trip however many of them were late.
+// hand-off costs one memory round trip however many of them were late.  NAP:
+// nanoseconds to sleep after every unsuccessful re-read, for waits off the
+// critical path (0: re-read at once, for the block-to-block hand-off), so
+// that CTAs waiting far ahead of the chain leave L2 and the SMs to the CTAs
+// that compute.
+template <int NAP = 0>
 __device__ __forceinline__ void iv_settle4(unsigned long long (&w)[4], const unsigned long long *const (&p)[4],
                                            unsigned long long tag, int *err_word, int *abort_flag) {
     long long spins = 0;
@@ -157,13 +165,14 @@ __device__ __forceinline__ void iv_settle4(unsigned long long (&w)[4], const uns
 #pragma unroll
         for (int u = 0; u < 4; ++u) done &= (p[u] == nullptr) || ((w[u] & 0xffffffff00000000ull) == tag);
         if (done) return;
-        if (((++spins) & 63) == 0) {
+        if (NAP > 0 || ((++spins) & 63) == 0) {
+            if (NAP > 0) ++spins;
             if (*(volatile int *)err_word != 0 || spins > kSpinLimit) {
                 atomicCAS(err_word, 0, (int)LLA_ERR_TIMEOUT);
                 *abort_flag = 1;
                 return;
             }
-            __nanosleep(32);
+            __nanosleep(NAP > 0 ? NAP : 32);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u)
@@ -174,7 +183,6 @@ __device__ __forceinline__ void iv_settle4(unsigned long long (&w)[4], const uns
 constexpr int kIvCols = 16;   // right-hand-side columns per CTA
 constexpr int kIvLd = 68;     // shared row stride of a staged 64 x 64 tile (floats; 16-byte rows)
 constexpr int kIvStages = 3;  // coupling tiles in flight per CTA
-constexpr int64_t kIvHelperMin = 16;  // first position whose coupling terms are split with a helper
 constexpr int kIvYd = kIvNb + 2;  // words per staged column (padded: 528-byte columns)
 constexpr size_t kIvSmem = sizeof(float) * ((size_t)kIvStages * kIvNb * kIvLd + 2ull * kIvStages * kIvCols * kIvYd +
                                             2ull * kIvNb * kIvCols + 2ull * kIvCols * kIvLd);
@@ -212,6 +220,166 @@ __device__ __forceinline__ void iv_dot64(float (&t)[4], const float (*A)[kIvLd],
     for (int j = 0; j < 4; ++j) t[j] = SIGN > 0 ? t[j] + (pe[j] + po[j]) : t[j] - (pe[j] + po[j]);
 }
 
+// Wide helpers: shared memory of a coupling-tile ring and a ring of 64-column
+// tiles of solved values (64 rows each, k contiguous per column).
+constexpr size_t kIvWideSmem = sizeof(float) * 2ull * kIvStages * kIvNb * kIvLd;
+constexpr size_t kIvLaunchSmem = kIvWideSmem > kIvSmem ? kIvWideSmem : kIvSmem;
+
+__device__ __forceinline__ unsigned long long iv_ld_acquire(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void iv_st_release(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.release.gpu.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// One wide helper: the coupling terms of positions [q0, q1) for block rb, all
+// 64 columns of column group cgrp at once (four times the work of a 16-column
+// stage for the same copies and barriers), published negated as epoch-tagged
+// words pw[row + 64 col].  The solved values come as plain floats from B, once
+// the owners of (position, chunk) have raised their flags (release after
+// their stores; acquire here, all of the group's flags polled at once before
+// the first copy: one round trip, not one per position).  Thread (ri = tid % 16,
+// ci = tid / 16) owns columns 4 ci .. 4 ci + 3 and rows 4 ri + j (ri + 16 j
+// when trans).
+template <bool TRANS>
+__device__ __forceinline__ void iv_wide_helper(const float *__restrict__ L, int64_t ld, const float *B, int64_t ldb,
+                                               int64_t n, int64_t m, int64_t R, int64_t rb, int64_t q0, int64_t q1,
+                                               int cgrp, int nch, unsigned long long *pw, unsigned long long *hflag,
+                                               const unsigned long long *flags, unsigned long long tag,
+                                               int *err_word, int *abort_flag, float *smem, bool al16) {
+    constexpr int NS = kIvStages;
+    float(*sT)[kIvNb][kIvLd] = reinterpret_cast<float(*)[kIvNb][kIvLd]>(smem);
+    float(*sY)[kIvNb][kIvLd] = reinterpret_cast<float(*)[kIvNb][kIvLd]>(smem + NS * kIvNb * kIvLd);
+    const int tid = threadIdx.x, ri = tid % 16, ci = tid / 16;
+    const int64_t c0 = (int64_t)cgrp * kIvNb;
+    const int64_t nst = q1 - q0;
+    auto issue = [&](int64_t i, int s) {
+        if (i < nst && !*(volatile int *)abort_flag) {
+            const int64_t pq = q0 + i;
+            const int64_t qb = TRANS ? R - 1 - pq : pq;
+            const int64_t rowbase = (TRANS ? qb : rb) * kIvNb, colbase = (TRANS ? rb : qb) * kIvNb;
+            if (al16) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int e = tid + 256 * j, a = e >> 4, c4 = e & 15;
+                    const int64_t row = rowbase + 4 * c4, col = colbase + a;
+                    const bool ok = row < n && col < n;
+                    const int bytes = ok ? 4 * (int)(n - row < 4 ? n - row : 4) : 0;
+                    iv_cp16(&sT[s][a][4 * c4], ok ? L + row + col * ld : L, bytes);
+                }
+            } else {
+#pragma unroll 4
+                for (int j = 0; j < 16; ++j) {
+                    const int e = tid + 256 * j, a = e >> 6, b = e & 63;
+                    const int64_t row = rowbase + b, col = colbase + a;
+                    const bool ok = row < n && col < n;
+                    iv_cp4(&sT[s][a][b], ok ? L + row + col * ld : L, ok ? 4 : 0);
+                }
+            }
+            // solved values of block qb, columns c0 + cy: chunk (c0 + cy) / 16 = 4 cgrp + j
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int e = tid + 256 * j, cy = e >> 4, r4 = 4 * (e & 15);
+                const int64_t col = c0 + cy, row = qb * kIvNb + r4;
+                const bool ok = col < m && row < n;
+                if (ok && !(al16 && ldb % 4 == 0 && (reinterpret_cast<uintptr_t>(B) & 15) == 0)) {
+#pragma unroll
+                    for (int h = 0; h < 4; ++h)
+                        iv_cp4(&sY[s][cy][r4 + h], row + h < n ? B + row + h + col * ldb : B, row + h < n ? 4 : 0);
+                } else {
+                    const int bytes = ok ? 4 * (int)(n - row < 4 ? n - row : 4) : 0;
+                    iv_cp16(&sY[s][cy][r4], ok ? B + row + col * ldb : B, bytes);
+                }
+            }
+        }
+        iv_commit();
+    };
+    {  // every (position, chunk) flag this helper depends on, polled at once: thread 4 i + j
+       // waits for position q0 + i, chunk 4 cgrp + j (bounded), then the barrier passes
+       // the acquired values on to the whole CTA before the copies
+        const int64_t i = tid >> 2;
+        const int j = tid & 3;
+        if (i < nst && c0 + 16 * j < m) {
+            const unsigned long long *f = flags + (q0 + i) * nch + (4 * cgrp + j);
+            long long spins = 0;
+            while (iv_ld_acquire(f) != (tag | 1ull)) {
+                if (*(volatile int *)err_word != 0 || ++spins > kSpinLimit) {
+                    atomicCAS(err_word, 0, (int)LLA_ERR_TIMEOUT);
+                    *abort_flag = 1;
+                    break;
+                }
+                __nanosleep(256);
+            }
+        }
+        __syncthreads();
+    }
+    float part[4][4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) part[j][jj] = 0.f;
+#pragma unroll
+    for (int s = 0; s < NS - 1; ++s) issue(s, s);
+    for (int64_t pq = 0; pq < nst; ++pq) {
+        const int s = (int)(pq % NS);
+        iv_wait<NS - 2>();
+        __syncthreads();
+        if (*(volatile int *)abort_flag) break;
+        issue(pq + NS - 1, (int)((pq + NS - 1) % NS));
+#pragma unroll 4
+        for (int k0 = 0; k0 < kIvNb; k0 += 4) {
+            float4 y[4];
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) y[jj] = *reinterpret_cast<const float4 *>(&sY[s][4 * ci + jj][k0]);
+            if (!TRANS) {  // coefficient of y_k in row i: sT[s][k][i]
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) {
+                    const float4 l4 = *reinterpret_cast<const float4 *>(&sT[s][k0 + kk][4 * ri]);
+#pragma unroll
+                    for (int jj = 0; jj < 4; ++jj) {
+                        const float yv = kk == 0 ? y[jj].x : kk == 1 ? y[jj].y : kk == 2 ? y[jj].z : y[jj].w;
+                        part[0][jj] = fmaf(-l4.x, yv, part[0][jj]);
+                        part[1][jj] = fmaf(-l4.y, yv, part[1][jj]);
+                        part[2][jj] = fmaf(-l4.z, yv, part[2][jj]);
+                        part[3][jj] = fmaf(-l4.w, yv, part[3][jj]);
+                    }
+                }
+            } else {  // coefficient of y_k in row i: sT[s][i][k]
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const float4 l4 = *reinterpret_cast<const float4 *>(&sT[s][ri + 16 * j][k0]);
+#pragma unroll
+                    for (int jj = 0; jj < 4; ++jj) {
+                        float a = part[j][jj];
+                        a = fmaf(-l4.x, y[jj].x, a);
+                        a = fmaf(-l4.y, y[jj].y, a);
+                        a = fmaf(-l4.z, y[jj].z, a);
+                        a = fmaf(-l4.w, y[jj].w, a);
+                        part[j][jj] = a;
+                    }
+                }
+            }
+        }
+    }
+    iv_wait<0>();
+    if (*(volatile int *)abort_flag) return;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int rl = TRANS ? ri + 16 * j : 4 * ri + j;
+        if (rb * kIvNb + rl >= n) continue;
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+            const int cl = 4 * ci + jj;
+            if (c0 + cl < m) iv_st_word(pw + rl + kIvNb * cl, tag | (unsigned long long)__float_as_uint(part[j][jj]));
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) iv_st_release(hflag, tag | 1ull);  // one flag for the owners to wait on
+}
+
 // TRANS = false: L Y = B (blocks ascending); TRANS = true: L^T X = B (descending).
 // 256 threads.  The coupling tiles and the solved words of earlier blocks
 // stream through a kIvStages-deep cp.async ring.  Each thread validates the
@@ -228,7 +396,8 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
                                                           const float *__restrict__ Wall, int64_t n,
                                                           float *B, int64_t ldb, int64_t m, int nchunks,
                                                           unsigned long long *ll, int64_t ldl, unsigned epoch,
-                                                          int *counter, int *err_word, int64_t hmin,
+                                                          int *counter, int *err_word, int ngrp,
+                                                          unsigned long long *pw, unsigned long long *flags,
                                                           const int *state) {
     if (refine_done(state)) return;  // the refinement has finished: nothing to solve
     constexpr int C = kIvCols, LPT = kIvTile / 256, NS = kIvStages;
@@ -251,23 +420,28 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
     __syncthreads();
     const int64_t R = (n + kIvNb - 1) / kIvNb;
     bool helper;
-    int64_t pb;  // position in processing order
-    int cc;
-    iv_decode(s_ticket, R, hmin, nchunks, helper, pb, cc);
+    int64_t pb, slot;  // position in processing order; a helper's partial-sum slot
+    int grp, cc;
+    iv_decode(s_ticket, R, nchunks, ngrp, helper, pb, grp, cc, slot);
     const int64_t rb = TRANS ? R - 1 - pb : pb;
-    unsigned long long *pl = ll + R * kIvNb * m;  // helpers' partial sums, laid out like ll
+    const unsigned long long tag = (unsigned long long)epoch << 32;
+    const bool al16 = (ld % 4 == 0) && ((reinterpret_cast<uintptr_t>(L) & 15) == 0);
+    if (helper) {  // a wide helper: coupling terms of positions [grp G, ...) for 64 columns
+        const int64_t q0 = (int64_t)grp * kIvGroup, q1 = min(q0 + kIvGroup, iv_qlo(pb));
+        iv_wide_helper<TRANS>(L, ld, B, ldb, n, m, R, rb, q0, q1, cc, nchunks, pw + slot * kIvTile,
+                              flags + R * nchunks + slot, flags, tag, err_word, &s_abort, iv_smem, al16);
+        return;
+    }
     const int ta = tid % kIvNb, tb = tid / kIvNb;
     const int64_t grow = rb * kIvNb + ta;
     const int64_t col0 = (int64_t)cc * C;
-    const unsigned long long tag = (unsigned long long)epoch << 32;
-    const bool al16 = (ld % 4 == 0) && ((reinterpret_cast<uintptr_t>(L) & 15) == 0);
 
     const int bc = tid % C, rg = tid / C;  // bulk mapping: column bc, rows 4 rg .. 4 rg + 3
     float acc[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int64_t row = rb * kIvNb + 4 * rg + i, col = col0 + bc;
-        acc[i] = (!helper && row < n && col < m) ? B[row + col * ldb] : 0.f;
+        acc[i] = (row < n && col < m) ? B[row + col * ldb] : 0.f;
     }
     // this block's inverse and coupling matrix (element (ta, tb + 4u) of each), needed only at the end
     float preW[LPT], preM[LPT];
@@ -280,11 +454,9 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
             preM[u] = Mr[u * 4 * kIvNb];
         }
     }
-    // coupling terms of this item, positions q_lo .. q_lo + nbulk - 1: a helper
-    // takes q < pb/2, its owner the rest before the two neighbours'
-    const bool has_helper = pb >= hmin;
-    const int64_t q_lo = (!helper && has_helper) ? pb / 2 : 0;
-    const int64_t nbulk = helper ? pb / 2 : (pb > 1 ? pb - 2 - q_lo : 0);
+    // the owner's own coupling terms: positions q_lo .. pb-3 (the wide helpers have the earlier ones)
+    const int64_t q_lo = iv_qlo(pb);
+    const int64_t nbulk = pb > 1 ? pb - 2 - q_lo : 0;
 
     // Stage s <- coupling tile and solved words of processing position pq.
     // Tile: 64 columns a of 64 contiguous rows b (non-trans: a = k, b = i;
@@ -352,7 +524,7 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
                     p[2 * j + h] = (gk < n && col < m) ? ll + gk + col * ldl : nullptr;
                 }
             }
-            iv_settle4(w, p, tag, err_word, &s_abort);
+            iv_settle4<256>(w, p, tag, err_word, &s_abort);  // blocks solved a few steps back
         }
 #pragma unroll
         for (int j = 0; j < YCH; ++j) {
@@ -371,6 +543,43 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
         for (int jj = 0; jj < 4; ++jj) part[j][jj] = 0.f;
 #pragma unroll
     for (int s = 0; s < NS - 1; ++s) issue(s, s);
+    {  // the wide helpers' partial sums, group by group: read while the first stages copy and
+       // long before the neighbours are solved, off the critical path.  One warp waits on the
+       // helpers' flags (sleeping between polls), then the barrier passes them on.
+        const int cg64 = (int)(col0 / kIvNb), cl = (int)(col0 % kIvNb) + bc;  // column group, column in it
+        const int64_t ng = iv_ngroups(pb);
+        const int64_t slot0 = (int64_t)ngrp * iv_groups_before(pb) + cg64;  // slot of group 0
+        const unsigned long long *pw0 = pw + slot0 * kIvTile;
+        if (tid < 32) {
+            const unsigned long long *hflags = flags + R * nchunks;
+            for (int64_t g = tid; g < ng; g += 32) {
+                long long spins = 0;
+                while (iv_ld_acquire(hflags + slot0 + g * ngrp) != (tag | 1ull)) {
+                    if (*(volatile int *)err_word != 0 || ++spins > kSpinLimit) {
+                        atomicCAS(err_word, 0, (int)LLA_ERR_TIMEOUT);
+                        s_abort = 1;
+                        break;
+                    }
+                    __nanosleep(256);
+                }
+            }
+        }
+        __syncthreads();
+        for (int64_t g = 0; g < ng; ++g) {
+            unsigned long long w[4];
+            const unsigned long long *p[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int64_t row = rb * kIvNb + 4 * rg + i;
+                p[i] = (row < n && col0 + bc < m) ? pw0 + g * ngrp * kIvTile + (4 * rg + i) + kIvNb * cl : nullptr;
+                w[i] = p[i] ? iv_ld_word(p[i]) : 0ull;
+            }
+            iv_settle4<256>(w, p, tag, err_word, &s_abort);  // published before the flag: no wait
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (p[i]) acc[i] += __uint_as_float((unsigned)(w[i] & 0xffffffffull));
+        }
+    }  // a timed-out wait is seen after the next barrier (the copies in flight drain first)
     for (int64_t pq = 0; pq < nbulk; ++pq) {
         const int s = (int)(pq % NS), buf = (int)(pq & 1);
         iv_wait<NS - 2>();
@@ -431,29 +640,6 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
         }
     }
     if (s_abort) return;
-    if (helper) {  // publish the partial sum (its coupling terms, negated) for the owner
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const int64_t row = rb * kIvNb + 4 * rg + i, col = col0 + bc;
-            if (row < n && col < m) iv_st_word(pl + row + col * ldl, tag | (unsigned long long)__float_as_uint(acc[i]));
-        }
-        return;
-    }
-    if (has_helper) {  // add the helper's partial sum (bounded wait)
-        unsigned long long w[4];
-        const unsigned long long *p[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const int64_t row = rb * kIvNb + 4 * rg + i, col = col0 + bc;
-            p[i] = (row < n && col < m) ? pl + row + col * ldl : nullptr;
-            w[i] = p[i] ? iv_ld_word(p[i]) : 0ull;
-        }
-        iv_settle4(w, p, tag, err_word, &s_abort);
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-            if (p[i]) acc[i] += __uint_as_float((unsigned)(w[i] & 0xffffffffull));
-    }
-
     // 2. t = W_r acc (W_r^T acc when trans); both neighbours' words and the
     // second neighbour's coupling matrix are read meanwhile
     unsigned long long wy[4], wy2[4];
@@ -528,7 +714,8 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
         if (s_abort) return;
         iv_dot64<-1>(t, sM, sN, ta, tb);
     }
-    // 4. publish
+    // 4. publish: the tagged words for the next blocks' owners, then (off the
+    // critical path) the flag that lets wide helpers read the values from B
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
         const int64_t col = col0 + tb * 4 + u;
@@ -537,6 +724,9 @@ __global__ void __launch_bounds__(256, 2) trsm_inv_kernel(const float *__restric
             iv_st_word(ll + grow + col * ldl, tag | (unsigned long long)__float_as_uint(t[u]));
         }
     }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) iv_st_release(flags + pb * nchunks + cc, tag | 1ull);
 }
 
 // ---------------------------------------------------------------------------
@@ -891,9 +1081,14 @@ __global__ void __launch_bounds__(256, 2) trsm_chain_kernel(const float *__restr
 
 size_t trsm_inv_ws_ints(int64_t, int64_t) { return 1; }
 
-// solved values, then the helpers' partial sums
+// solved words, then the wide helpers' partial sums (64 x 64 words a slot),
+// then one flag word per (position, chunk), then one per helper slot
+static int iv_ngrp(int64_t m) { return (int)((m + kIvNb - 1) / kIvNb); }
+static int iv_nch(int64_t m) { return (int)((m + kIvCols - 1) / kIvCols); }
 size_t trsm_inv_stage_words(int64_t n, int64_t m) {
-    return 2 * (size_t)((n + kIvNb - 1) / kIvNb) * kIvNb * (size_t)m;
+    const int64_t R = (n + kIvNb - 1) / kIvNb;
+    return (size_t)R * kIvNb * (size_t)m + (size_t)iv_ngrp(m) * iv_groups_before(R) * (kIvTile + 1) +
+           (size_t)R * iv_nch(m);
 }
 
 // chain form: the solved words, then the helpers' partial sums (Gmax groups a position)
@@ -923,20 +1118,20 @@ int trsm_inv_launch(const float *L, int64_t ld, const float *W, int64_t n, float
                     cudaStream_t st, const int *state) {
     if (n == 0 || m == 0) return 0;
     if (epoch == 0) return -1;
-    const int nchunks = (int)((m + kIvCols - 1) / kIvCols);
+    const int nchunks = iv_nch(m), ngrp = iv_ngrp(m);
     const int64_t R = (n + kIvNb - 1) / kIvNb;
     auto kern = trans ? trsm_inv_kernel<true> : trsm_inv_kernel<false>;
-    const size_t smem = kIvSmem;
+    const size_t smem = kIvLaunchSmem;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return -1;
     if (cudaMemsetAsync(ws, 0, sizeof(int), st) != cudaSuccess) return -1;
     // algorithmic work: n^2 m flops
     LaunchScope ls(K_MIXED_TRSM, st, (double)n * n * m);
-    // positions from kIvHelperMin on get a helper for the first half of their coupling terms
-    const int64_t hmin = kIvHelperMin;
-    const int64_t items = iv_items_before(R, R, hmin, nchunks);  // every group
+    unsigned long long *pw = stage + R * kIvNb * m;
+    unsigned long long *flags = pw + (int64_t)ngrp * iv_groups_before(R) * kIvTile;
+    const int64_t items = iv_items_before(R, R, nchunks, ngrp);
     kern<<<(unsigned)items, 256, smem, st>>>(L, ld, W, n, B, ldb, m, nchunks, stage, R * kIvNb, epoch, ws,
-                                            err_word, hmin, state);
+                                            err_word, ngrp, pw, flags, state);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

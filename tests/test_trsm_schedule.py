@@ -1,9 +1,11 @@
 """Ticket order of the FP32 substitutions (csrc/lla_trsm_sched.h), checked on the
 host with the kernel's own header: every work item is decoded exactly once, and
 every item waits only on items with smaller tickets (owners on the previous
-owners of their column chunk, which includes the two neighbours; owners on
-their helper; helpers on the owners of the positions they sum), so CTAs that
-take tickets in order can never wait on a CTA that has not been scheduled."""
+owners of their column chunk, which includes the two neighbours; owners on the
+wide helpers of their position; helpers on the owners of the positions they
+sum), so CTAs that take tickets in order can never wait on a CTA that has not
+been scheduled; the helper groups and the owner's own range cover every
+coupling term once."""
 import os
 import shutil
 import subprocess
@@ -22,47 +24,58 @@ HARNESS = r"""
 #include "lla_trsm_sched.h"
 using namespace lla;
 int main() {
-    const int64_t Rs[] = {1, 2, 3, 4, 5, 16, 17, 18, 33, 40, 100, 129, 256, 257};
-    const int nchs[] = {1, 2, 3, 4, 7};
-    const int64_t hmins[] = {2, 3, 16, 1 << 30};
+    const int64_t Rs[] = {1, 2, 3, 4, 5, 16, 18, 19, 20, 21, 32, 33, 35, 36, 37, 48, 50, 51, 52, 53, 64, 67, 80, 100, 129, 256, 257, 1024};
+    const int nchs[] = {1, 2, 3, 4, 5, 7, 8};
     long long checked = 0;
     for (int64_t R : Rs)
-        for (int nch : nchs)
-            for (int64_t hmin : hmins) {
-                const int64_t total = iv_items_before(R, R, hmin, nch);
-                std::map<std::tuple<int, int64_t, int>, int64_t> seen;
-                for (int64_t t = 0; t < total; ++t) {
-                    bool helper; int64_t pos; int chunk;
-                    iv_decode(t, R, hmin, nch, helper, pos, chunk);
-                    if (pos < 0 || pos >= R || chunk < 0 || chunk >= nch || (helper && pos < hmin)) {
-                        std::printf("bad item R=%lld nch=%d hmin=%lld t=%lld\n", (long long)R, nch, (long long)hmin, (long long)t);
-                        return 1;
-                    }
-                    if (!seen.emplace(std::make_tuple((int)helper, pos, chunk), t).second) {
-                        std::printf("duplicate R=%lld t=%lld\n", (long long)R, (long long)t);
-                        return 1;
-                    }
+        for (int nch : nchs) {
+            const int ngrp = (nch + 3) / 4;  // 64-column groups of the 16-column chunks
+            const int64_t total = iv_items_before(R, R, nch, ngrp);
+            // key: (helper, position, group, chunk or column group)
+            std::map<std::tuple<int, int64_t, int, int>, int64_t> seen;
+            std::map<int64_t, int> slots;
+            for (int64_t t = 0; t < total; ++t) {
+                bool helper; int64_t pos, slot; int g, sub;
+                iv_decode(t, R, nch, ngrp, helper, pos, g, sub, slot);
+                const bool ok = pos >= 0 && pos < R &&
+                                (helper ? (g >= 0 && g < iv_ngroups(pos) && sub >= 0 && sub < ngrp && slot >= 0 &&
+                                           slot < (int64_t)ngrp * iv_groups_before(R))
+                                        : (sub >= 0 && sub < nch));
+                if (!ok) { std::printf("bad item R=%lld nch=%d t=%lld\n", (long long)R, nch, (long long)t); return 1; }
+                if (!seen.emplace(std::make_tuple((int)helper, pos, g, sub), t).second) {
+                    std::printf("duplicate R=%lld t=%lld\n", (long long)R, (long long)t); return 1;
                 }
-                const int64_t helpers = R > hmin ? R - hmin : 0;
-                if ((int64_t)seen.size() != nch * (R + helpers)) {
-                    std::printf("count R=%lld nch=%d hmin=%lld: %zu\n", (long long)R, nch, (long long)hmin, seen.size());
-                    return 1;
-                }
-                for (const auto &kv : seen) {
-                    const int helper = std::get<0>(kv.first);
-                    const int64_t p = std::get<1>(kv.first);
-                    const int c = std::get<2>(kv.first);
-                    const int64_t t = kv.second;
-                    if (helper) {  // sums the coupling terms q < p/2
-                        for (int64_t q = 0; q < p / 2; ++q)
-                            if (seen.at(std::make_tuple(0, q, c)) >= t) { std::printf("helper wait\n"); return 1; }
-                    } else {
-                        if (p > 0 && seen.at(std::make_tuple(0, p - 1, c)) >= t) { std::printf("owner wait\n"); return 1; }
-                        if (p >= hmin && seen.at(std::make_tuple(1, p, c)) >= t) { std::printf("helper order\n"); return 1; }
-                    }
-                    ++checked;
-                }
+                if (helper && !slots.emplace(slot, 1).second) { std::printf("slot twice\n"); return 1; }
             }
+            if ((int64_t)seen.size() != R * nch + (int64_t)ngrp * iv_groups_before(R)) { std::printf("count\n"); return 1; }
+            for (const auto &kv : seen) {
+                const int helper = std::get<0>(kv.first);
+                const int64_t p = std::get<1>(kv.first);
+                const int g = std::get<2>(kv.first), sub = std::get<3>(kv.first);
+                const int64_t t = kv.second;
+                if (helper) {  // waits on the owners of its positions, for the chunks of its column group
+                    const int64_t lo = g * kIvGroup, hi = lo + kIvGroup < iv_qlo(p) ? lo + kIvGroup : iv_qlo(p);
+                    if (hi <= lo || hi > p - 2) { std::printf("empty or late group\n"); return 1; }
+                    for (int64_t q = lo; q < hi; ++q)
+                        for (int c = 4 * sub; c < 4 * sub + 4 && c < nch; ++c)
+                            if (seen.at(std::make_tuple(0, q, 0, c)) >= t) { std::printf("helper wait\n"); return 1; }
+                } else {  // the previous owner of its chunk, and every helper of its position
+                    if (p > 0 && seen.at(std::make_tuple(0, p - 1, 0, sub)) >= t) { std::printf("owner wait\n"); return 1; }
+                    for (int gg = 0; gg < iv_ngroups(p); ++gg)
+                        if (seen.at(std::make_tuple(1, p, gg, sub / 4)) >= t) { std::printf("helper order\n"); return 1; }
+                    // the groups and the owner's own range cover positions 0 .. p-3 exactly once
+                    int64_t covered = 0;
+                    for (int gg = 0; gg < iv_ngroups(p); ++gg) {
+                        const int64_t lo = gg * kIvGroup, hi = lo + kIvGroup < iv_qlo(p) ? lo + kIvGroup : iv_qlo(p);
+                        covered += hi - lo;
+                    }
+                    covered += (p - 2 > iv_qlo(p)) ? p - 2 - iv_qlo(p) : 0;
+                    if (covered != (p > 2 ? p - 2 : 0)) { std::printf("cover p=%lld\n", (long long)p); return 1; }
+                    if (p - 2 - iv_qlo(p) > kIvOwn) { std::printf("owner range\n"); return 1; }
+                }
+                ++checked;
+            }
+        }
     std::printf("ok %lld\n", checked);
     return 0;
 }
