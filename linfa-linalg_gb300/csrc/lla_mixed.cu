@@ -26,6 +26,7 @@
 #include "lla_api_internal.h"
 #include "lla_autotune.h"
 #include "lla_common.cuh"
+#include "lla_f32_bits.h"
 #include "lla_kernels.h"
 #include "lla_mixed.h"
 #include "lla_prof.h"
@@ -75,11 +76,18 @@ __global__ void equil_scale_kernel(const double *A, int64_t lda, int64_t n, int 
 // No atomics: sym_rows_kernel adds the partials of each row in a fixed order.
 // Partials, n_pad = R * 64 apart: P[0][J] row sums, P[1][J] row maxima (tile
 // column J), P[2][I] column sums, P[3][I] column maxima (tile row I).
-// FP64 arithmetic is scarce on this GPU, so every element costs one FP64 add
-// for its row and one for its column; the maxima are taken on the bit
-// patterns (non-negative doubles order like unsigned integers).
+// FP64 arithmetic is scarce on this GPU (about 1/64 of the FP32 rate), so the
+// kernel avoids it: the scaling adds e_i + e_k to the exponent field, the
+// conversion to FP32 rounds to nearest even on the bit patterns (the
+// hardware conversion only for results outside the FP32 normal range), the
+// maxima are taken on the bit patterns (non-negative doubles order like
+// unsigned integers), and a tile whose nonzero |a| all lie in [2^-100, 2^100]
+// sums its 64-term row and column partials in FP32 (relative error below
+// 64 u_fp32 = 4e-6, harmless for the norm of the stopping test; the partials
+// are then added in FP64); any other tile sums in FP64.
 // Thread (r = tid % 64, cg = tid / 64): row r, columns 16 cg .. 16 cg + 15.
 constexpr int kSymT = 64;
+
 template <bool MAX>
 __global__ void __launch_bounds__(256) sym_tile_kernel(const double *__restrict__ A, int64_t lda, int64_t n,
                                                        const double *__restrict__ s, float *W, int64_t ldw,
@@ -95,8 +103,8 @@ __global__ void __launch_bounds__(256) sym_tile_kernel(const double *__restrict_
     const double si = i < n ? s[i] : 0.0;
     // s holds powers of two: the scaling adds e_i + e_k to the exponent field
     const int ei = (int)((__double_as_longlong(si) >> 52) & 0x7ff) - 1023;
-    double rs = 0.0;
-    unsigned long long rm = 0ull;
+    unsigned long long v[16];
+    bool in_range = true;
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
         const int c = 16 * cg + u;
@@ -110,15 +118,31 @@ __global__ void __launch_bounds__(256) sym_tile_kernel(const double *__restrict_
             const int ex = (int)((ab >> 52) & 0x7ff), ne = ex + es;
             // normal in and out: exact exponent shift; otherwise (zero, subnormal,
             // inf/NaN, out of range) the plain product
-            const double as = (ex != 0 && ex != 0x7ff && ne > 0 && ne < 0x7ff)
-                                  ? __longlong_as_double(ab + ((long long)es << 52))
-                                  : si * a * sk;
-            W[i + k * ldw] = (float)as;
+            const long long asb = (ex != 0 && ex != 0x7ff && ne > 0 && ne < 0x7ff)
+                                      ? ab + ((long long)es << 52)
+                                      : __double_as_longlong(si * a * sk);
+            W[i + k * ldw] = sym_to_f32(asb);
         }
-        const unsigned long long v = (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull;
-        rs += __longlong_as_double((long long)v);
-        if (MAX) rm = v > rm ? v : rm;
-        sv[c][r] = (I > J || r > c) ? v : 0ull;
+        v[u] = (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull;
+        in_range &= sym_f32_range(v[u]);
+        sv[c][r] = (I > J || r > c) ? v[u] : 0ull;
+    }
+    const bool f32 = __syncthreads_and(in_range) != 0;  // also orders the sv stores before the column sums
+    double rs;
+    unsigned long long rm = 0ull;
+    if (f32) {
+        float t = 0.f;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) t += sym_abs_f32(v[u]);
+        rs = (double)t;
+    } else {
+        rs = 0.0;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) rs += __longlong_as_double((long long)v[u]);
+    }
+    if (MAX) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) rm = v[u] > rm ? v[u] : rm;
     }
     prs[cg][r] = rs;
     if (MAX) prm[cg][r] = rm;
@@ -133,13 +157,25 @@ __global__ void __launch_bounds__(256) sym_tile_kernel(const double *__restrict_
         }
     } else if (tid < 2 * kSymT) {  // column partial of column c
         const int c = tid - kSymT;
-        double cs = 0.0;
+        double cs;
         unsigned long long cm = 0ull;
+        if (f32) {
+            float t = 0.f;
 #pragma unroll 8
-        for (int q = 0; q < kSymT; ++q) {
-            const unsigned long long v = sv[c][q];
-            cs += __longlong_as_double((long long)v);
-            if (MAX) cm = v > cm ? v : cm;
+            for (int q = 0; q < kSymT; ++q) {
+                const unsigned long long w = sv[c][q];
+                t += sym_abs_f32(w);
+                if (MAX) cm = w > cm ? w : cm;
+            }
+            cs = (double)t;
+        } else {
+            cs = 0.0;
+#pragma unroll 8
+            for (int q = 0; q < kSymT; ++q) {
+                const unsigned long long w = sv[c][q];
+                cs += __longlong_as_double((long long)w);
+                if (MAX) cm = w > cm ? w : cm;
+            }
         }
         P[(2 * R + I) * npad + J * kSymT + c] = cs;
         if (MAX) P[(3 * R + I) * npad + J * kSymT + c] = __longlong_as_double((long long)cm);

@@ -158,15 +158,24 @@ __global__ void __launch_bounds__(256) oz_slice_a_kernel(const double *__restric
         tile[r][c] = v;
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
-        const int r = e / 32, c = e % 32;  // consecutive e -> consecutive k in the output row
-        const int64_t i = i0 + r, k = k0 + c;
-        if (i >= n || k >= ldp) continue;
+    // thread (r = tid / 8, quad c4 = 4 (tid % 8)): row r, columns c4 .. c4 + 3, one
+    // 8-byte store per plane (ldp and the plane stride are multiples of 64)
+    const int r = threadIdx.x >> 3, c4 = (threadIdx.x & 7) * 4;
+    const int64_t i = i0 + r, k = k0 + c4;
+    if (i < n && k < ldp) {
         const double rm = rowmax[i];
-        __nv_bfloat16 q[kOzS];
-        oz_digits(isfinite(rm) ? tile[r][c] : 0.0, oz_exponent(rm), q);
+        const bool fin = isfinite(rm);
+        const int e = oz_exponent(rm);
+        __nv_bfloat16 q[4][kOzS];
 #pragma unroll
-        for (int p = 0; p < kOzS; ++p) planes[p * plane_stride + i * ldp + k] = q[p];
+        for (int u = 0; u < 4; ++u) oz_digits(fin ? tile[r][c4 + u] : 0.0, e, q[u]);
+#pragma unroll
+        for (int p = 0; p < kOzS; ++p) {
+            uint2 w;
+            w.x = (unsigned)__bfloat16_as_ushort(q[0][p]) | ((unsigned)__bfloat16_as_ushort(q[1][p]) << 16);
+            w.y = (unsigned)__bfloat16_as_ushort(q[2][p]) | ((unsigned)__bfloat16_as_ushort(q[3][p]) << 16);
+            *reinterpret_cast<uint2 *>(planes + p * plane_stride + i * ldp + k) = w;
+        }
     }
 }
 
