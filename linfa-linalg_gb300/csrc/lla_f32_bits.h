@@ -32,6 +32,15 @@ __host__ __device__ __forceinline__ double f64_from_bits(int64_t b) {
     return d;
 }
 
+#ifdef __CUDACC__
+#define LLA_OUT_OF_LINE __noinline__
+#else
+#define LLA_OUT_OF_LINE __attribute__((noinline))
+#endif
+// The hardware conversion, out of line: a predicated copy in the common path
+// would still take FP64 issue slots for every element.
+static LLA_OUT_OF_LINE __host__ __device__ float f32_hw_convert(int64_t b) { return (float)f64_from_bits(b); }
+
 // fp32(x) rounded to nearest even, from the bits b of a double whose FP32
 // exponent is normal (the mantissa's low 29 bits decide the rounding; a carry
 // into the exponent field is the correctly rounded result, infinity
@@ -39,7 +48,7 @@ __host__ __device__ __forceinline__ double f64_from_bits(int64_t b) {
 // through the hardware conversion.
 __host__ __device__ __forceinline__ float sym_to_f32(int64_t b) {
     const int fe = (int)((b >> 52) & 0x7ff) - (1023 - 127);
-    if (fe < 1 || fe > 254) return (float)f64_from_bits(b);
+    if (fe < 1 || fe > 254) return f32_hw_convert(b);
     const uint64_t mant = (uint64_t)b & 0xfffffffffffffull;
     const uint32_t m = (uint32_t)(mant >> 29), rem = (uint32_t)(mant & 0x1fffffffull);
     uint32_t w = ((uint32_t)fe << 23) | m;

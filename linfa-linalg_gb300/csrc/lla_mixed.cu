@@ -88,6 +88,10 @@ __global__ void equil_scale_kernel(const double *A, int64_t lda, int64_t n, int 
 // Thread (r = tid % 64, cg = tid / 64): row r, columns 16 cg .. 16 cg + 15.
 constexpr int kSymT = 64;
 
+__device__ __noinline__ long long sym_plain_product(double si, double a, double sk) {
+    return __double_as_longlong(si * a * sk);
+}
+
 template <bool MAX>
 __global__ void __launch_bounds__(256) sym_tile_kernel(const double *__restrict__ A, int64_t lda, int64_t n,
                                                        const double *__restrict__ s, float *W, int64_t ldw,
@@ -98,11 +102,24 @@ __global__ void __launch_bounds__(256) sym_tile_kernel(const double *__restrict_
     __shared__ double prs[4][kSymT];
     __shared__ unsigned long long prm[4][kSymT];
     __shared__ unsigned long long sv[kSymT][kSymT + 1];  // sv[c][r]: bits of |a| for the column partials
+    __shared__ unsigned long long sdg[kSymT];             // |a_rr| of a diagonal tile (FP64 row sums)
+    __shared__ double ss[kSymT];                          // the tile's column scales
     const int tid = threadIdx.x, r = tid % kSymT, cg = tid / kSymT;
+    if (tid < kSymT) ss[tid] = J * kSymT + tid < n ? s[J * kSymT + tid] : 0.0;
     const int64_t i = I * kSymT + r;
     const double si = i < n ? s[i] : 0.0;
     // s holds powers of two: the scaling adds e_i + e_k to the exponent field
     const int ei = (int)((__double_as_longlong(si) >> 52) & 0x7ff) - 1023;
+    // every load of the thread first (16 elements in flight)
+    double av[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+        const int c = 16 * cg + u;
+        const int64_t k = J * kSymT + c;
+        const bool lower = i < n && k < n && (I > J || r >= c);
+        av[u] = lower ? A[i + k * lda] : 0.0;
+    }
+    __syncthreads();  // ss
     unsigned long long v[16];
     bool in_range = true;
 #pragma unroll
@@ -110,24 +127,25 @@ __global__ void __launch_bounds__(256) sym_tile_kernel(const double *__restrict_
         const int c = 16 * cg + u;
         const int64_t k = J * kSymT + c;
         const bool lower = i < n && k < n && (I > J || r >= c);
-        const double a = lower ? A[i + k * lda] : 0.0;
+        const double a = av[u];
         if (lower) {
-            const double sk = s[k];
-            const int es = ei + (int)((__double_as_longlong(sk) >> 52) & 0x7ff) - 1023;
+            const double sku = ss[c];
+            const int es = ei + (int)((__double_as_longlong(sku) >> 52) & 0x7ff) - 1023;
             const long long ab = __double_as_longlong(a);
             const int ex = (int)((ab >> 52) & 0x7ff), ne = ex + es;
             // normal in and out: exact exponent shift; otherwise (zero, subnormal,
-            // inf/NaN, out of range) the plain product
-            const long long asb = (ex != 0 && ex != 0x7ff && ne > 0 && ne < 0x7ff)
-                                      ? ab + ((long long)es << 52)
-                                      : __double_as_longlong(si * a * sk);
+            // inf/NaN, out of range) the plain product, in a call so that the
+            // compiler cannot evaluate its two FP64 multiplies for every element
+            long long asb = ab + ((long long)es << 52);
+            if (!(ex != 0 && ex != 0x7ff && ne > 0 && ne < 0x7ff)) asb = sym_plain_product(si, a, sku);
             W[i + k * ldw] = sym_to_f32(asb);
         }
         v[u] = (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull;
         in_range &= sym_f32_range(v[u]);
         sv[c][r] = (I > J || r > c) ? v[u] : 0ull;
+        if (I == J && c == r) sdg[r] = v[u];
     }
-    const bool f32 = __syncthreads_and(in_range) != 0;  // also orders the sv stores before the column sums
+    const bool f32 = __syncthreads_and(in_range) != 0;  // also orders the shared stores before the sums
     double rs;
     unsigned long long rm = 0ull;
     if (f32) {
@@ -135,10 +153,13 @@ __global__ void __launch_bounds__(256) sym_tile_kernel(const double *__restrict_
 #pragma unroll
         for (int u = 0; u < 16; ++u) t += sym_abs_f32(v[u]);
         rs = (double)t;
-    } else {
+    } else {  // FP64 from shared memory, in a loop the compiler keeps as a branch
         rs = 0.0;
-#pragma unroll
-        for (int u = 0; u < 16; ++u) rs += __longlong_as_double((long long)v[u]);
+#pragma unroll 1
+        for (int u = 0; u < 16; ++u) {
+            const int c = 16 * cg + u;
+            rs += __longlong_as_double((long long)(c == r && I == J ? sdg[r] : sv[c][r]));
+        }
     }
     if (MAX) {
 #pragma unroll
@@ -170,7 +191,7 @@ __global__ void __launch_bounds__(256) sym_tile_kernel(const double *__restrict_
             cs = (double)t;
         } else {
             cs = 0.0;
-#pragma unroll 8
+#pragma unroll 1
             for (int q = 0; q < kSymT; ++q) {
                 const unsigned long long w = sv[c][q];
                 cs += __longlong_as_double((long long)w);
