@@ -34,6 +34,7 @@
 
 #include "lla_common.cuh"
 #include "lla_mixed.h"
+#include "lla_oz_digits.h"
 #include "lla_prof.h"
 #include "lla_tcgen05.cuh"
 
@@ -105,99 +106,91 @@ __device__ __forceinline__ int oz_exponent(double v) { return v > 0.0 ? ilogb(v)
 // Digits of a with respect to the scale 2^e (|a| < 2^e): the magnitude
 // |a| 2^(56 - e) as a 56-bit integer T (low bits truncated -- below 2^-56 of
 // the scale), cut into eight 7-bit digits T = sum_p alpha_p 2^(7 (7 - p)), each
-// carrying the sign of a.  Integer operations only (the FP64 pipe is slow).
-__device__ __forceinline__ void oz_digits(double a, int e, __nv_bfloat16 (&q)[kOzS]) {
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(a);
-    const int eb = (int)((bits >> 52) & 0x7ff);
-    unsigned long long mant = bits & ((1ull << 52) - 1);
-    int ea;  // a = mant * 2^ea
-    if (eb == 0) {
-        ea = -1074;
-    } else {
-        mant |= 1ull << 52;
-        ea = eb - 1075;
-    }
-    const int shift = ea + 56 - e;  // <= 3 since |a| < 2^e
-    unsigned long long T = 0;
-    if (mant != 0 && eb != 0x7ff) {
-        if (shift >= 0)
-            T = mant << shift;
-        else if (shift > -64)
-            T = mant >> (-shift);
-    }
-    const bool neg = (bits >> 63) != 0;
-#pragma unroll
-    for (int p = 0; p < kOzS; ++p) {
-        const int d = (int)((T >> (7 * (kOzS - 1 - p))) & 127);
-        q[p] = __int2bfloat16_rn(neg ? -d : d);  // exact: at most 7 bits
-    }
-}
+// carrying the sign of a (lla_oz_digits.h: integer and FP32 operations only --
+// the FP64 pipe is slow -- four elements at a time, packed BF16 pairs).
+static_assert(kOzS == kOzDigits, "one plane per digit");
 
 // Slices of A_sym, planes [p][i][k] (row-major, row stride ldp >= n, zero for
-// k >= n).  32 x 32 tiles through shared memory: lower tiles read column-major
-// A coalesced along i, upper tiles (mirrored) along k.
+// k >= n).  64 x 64 tiles through shared memory (16 loads in flight per
+// thread): lower tiles read column-major A coalesced along i, upper tiles
+// (mirrored) along k.  Then thread t writes row t / 16, columns 4 (t % 16) ..
+// + 3 and the same for the next three groups of 16 rows: one 8-byte store per
+// plane (ldp and the plane stride are multiples of 64).
 __global__ void __launch_bounds__(256) oz_slice_a_kernel(const double *__restrict__ A, int64_t lda,
                                                          int64_t n, int64_t ldp,
                                                          const double *__restrict__ rowmax,
                                                          __nv_bfloat16 *planes, int64_t plane_stride) {
-    __shared__ double tile[32][33];
-    const int64_t i0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
+    __shared__ double tile[64][65];
+    const int64_t i0 = (int64_t)blockIdx.y * 64, k0 = (int64_t)blockIdx.x * 64;
     const bool upper = k0 > i0;  // strictly above the diagonal block: mirror of a lower tile
-    for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
+    double v[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+        const int e = threadIdx.x + 256 * u;
         int r, c;
         if (upper) {
-            c = e % 32;
-            r = e / 32;  // consecutive e -> consecutive k -> A[k + i*lda]
+            c = e % 64;
+            r = e / 64;  // consecutive e -> consecutive k -> A[k + i*lda]
         } else {
-            r = e % 32;
-            c = e / 32;  // consecutive e -> consecutive i -> A[i + k*lda]
+            r = e % 64;
+            c = e / 64;  // consecutive e -> consecutive i -> A[i + k*lda]
         }
         const int64_t i = i0 + r, k = k0 + c;
-        double v = 0.0;
-        if (i < n && k < n) v = (k <= i) ? A[i + k * lda] : A[k + i * lda];
-        tile[r][c] = v;
+        v[u] = 0.0;
+        if (i < n && k < n) v[u] = (k <= i) ? A[i + k * lda] : A[k + i * lda];
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+        const int e = threadIdx.x + 256 * u;
+        if (upper)
+            tile[e / 64][e % 64] = v[u];
+        else
+            tile[e % 64][e / 64] = v[u];
     }
     __syncthreads();
-    // thread (r = tid / 8, quad c4 = 4 (tid % 8)): row r, columns c4 .. c4 + 3, one
-    // 8-byte store per plane (ldp and the plane stride are multiples of 64)
-    const int r = threadIdx.x >> 3, c4 = (threadIdx.x & 7) * 4;
-    const int64_t i = i0 + r, k = k0 + c4;
-    if (i < n && k < ldp) {
+    const int c4 = (threadIdx.x & 15) * 4;
+#pragma unroll 1
+    for (int g = 0; g < 4; ++g) {
+        const int r = (threadIdx.x >> 4) + 16 * g;
+        const int64_t i = i0 + r, k = k0 + c4;
+        if (i >= n || k >= ldp) continue;
         const double rm = rowmax[i];
         const bool fin = isfinite(rm);
-        const int e = oz_exponent(rm);
-        __nv_bfloat16 q[4][kOzS];
+        int64_t b[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) oz_digits(fin ? tile[r][c4 + u] : 0.0, e, q[u]);
+        for (int u = 0; u < 4; ++u) b[u] = fin ? __double_as_longlong(tile[r][c4 + u]) : 0ll;
+        uint32_t q[kOzDigits][2];
+        oz_digits_packed4(b, oz_exponent(rm), q);
 #pragma unroll
-        for (int p = 0; p < kOzS; ++p) {
-            uint2 w;
-            w.x = (unsigned)__bfloat16_as_ushort(q[0][p]) | ((unsigned)__bfloat16_as_ushort(q[1][p]) << 16);
-            w.y = (unsigned)__bfloat16_as_ushort(q[2][p]) | ((unsigned)__bfloat16_as_ushort(q[3][p]) << 16);
-            *reinterpret_cast<uint2 *>(planes + p * plane_stride + i * ldp + k) = w;
-        }
+        for (int p = 0; p < kOzS; ++p)
+            *reinterpret_cast<uint2 *>(planes + p * plane_stride + i * ldp + k) = make_uint2(q[p][0], q[p][1]);
     }
 }
 
-// Slices of X^T, planes [q][j][k] (m_pad = 64 rows, zero for j >= m or k >= n).
+// Slices of X^T, planes [q][j][k] (m_pad = 64 rows, zero for j >= m or k >= n):
+// thread (k4, j) writes columns 4 k4 .. 4 k4 + 3 of row j, one 8-byte store a plane.
 __global__ void oz_slice_x_kernel(const double *__restrict__ X, int64_t ldx, int64_t n, int64_t m,
                                   int64_t ldp, const double *__restrict__ colmax,
                                   __nv_bfloat16 *planes, int64_t plane_stride, const int *state) {
     if (refine_done(state)) return;
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t k = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x);
     const int64_t j = blockIdx.y;
     if (k >= ldp) return;
-    double t = 0.0;
+    int64_t b[4] = {0, 0, 0, 0};
     int e = 0;
-    if (j < m && k < n) {
+    if (j < m) {
         const double cm = colmax[j];
-        t = isfinite(cm) ? X[k + j * ldx] : 0.0;
         e = oz_exponent(cm);
-    }
-    __nv_bfloat16 q[kOzS];
-    oz_digits(t, e, q);
+        if (isfinite(cm)) {
 #pragma unroll
-    for (int p = 0; p < kOzS; ++p) planes[p * plane_stride + j * ldp + k] = q[p];
+            for (int u = 0; u < 4; ++u) b[u] = k + u < n ? __double_as_longlong(X[k + u + j * ldx]) : 0ll;
+        }
+    }
+    uint32_t q[kOzDigits][2];
+    oz_digits_packed4(b, e, q);
+#pragma unroll
+    for (int p = 0; p < kOzS; ++p)
+        *reinterpret_cast<uint2 *>(planes + p * plane_stride + j * ldp + k) = make_uint2(q[p][0], q[p][1]);
 }
 
 // ---- the tensor-core kernel ------------------------------------------------
@@ -502,7 +495,7 @@ int oz_prepare(const double *A, int64_t lda, int64_t n, int64_t m, void *ws, boo
     }
     {
         LaunchScope ls(K_OZ_SLICE, st, 8.0 * n * n + 2.0 * kOzS * n * o.ldp);
-        oz_slice_a_kernel<<<dim3((unsigned)((o.ldp + 31) / 32), (unsigned)((n + 31) / 32)), 256, 0, st>>>(
+        oz_slice_a_kernel<<<dim3((unsigned)(o.ldp / 64), (unsigned)((n + 63) / 64)), 256, 0, st>>>(
             A, lda, n, o.ldp, o.rowmax, o.A, n * o.ldp);
     }
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
@@ -547,7 +540,7 @@ int oz_residual_launch(const double *X, int64_t ldx, const double *B, int64_t ld
         const int64_t mc = std::min<int64_t>(kOzN, m - c0);
         {
             LaunchScope ls(K_OZ_SLICE, st, 8.0 * n * mc + 2.0 * kOzS * kOzN * o.ldp);
-            oz_slice_x_kernel<<<dim3((unsigned)((o.ldp + 255) / 256), kOzN), 256, 0, st>>>(
+            oz_slice_x_kernel<<<dim3((unsigned)((o.ldp / 4 + 255) / 256), kOzN), 256, 0, st>>>(
                 X + c0 * ldx, ldx, n, mc, o.ldp, colmax_x + c0, o.X, kOzN * o.ldp, state);
         }
         {
