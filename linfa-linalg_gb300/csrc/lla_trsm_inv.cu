@@ -18,12 +18,16 @@
 // helper CTAs sum the earlier ones in groups of kIvGroup positions for 64
 // columns at a time (lla_trsm_sched.h gives the ticket order).
 //
-// Hand-off between CTAs: a solved value is published as one 64-bit word
+// Hand-off between owners: a solved value is published as one 64-bit word
 // (launch epoch << 32 | float bits) in a staging array, so a consumer polls
 // the data itself -- one memory round trip per hand-off, no separate flag.
+// Wide helpers, which read 64 x 64 tiles of solved values, take them as
+// plain floats from B once the owners' (position, chunk) flags (epoch << 32 |
+// 1, released after the stores) are set, and publish their partial sums as
+// tagged words followed by one flag per slot, on which the owner waits.
 // The host gives every launch a fresh nonzero epoch and clears the staging
-// array whenever it is (re)allocated, so a word from an earlier launch never
-// matches.  Every wait is bounded and reports LLA_ERR_TIMEOUT.
+// array whenever it is (re)allocated, so a word or flag from an earlier
+// launch never matches.  Every wait is bounded and reports LLA_ERR_TIMEOUT.
 #include <cuda_runtime.h>
 
 #include <algorithm>
